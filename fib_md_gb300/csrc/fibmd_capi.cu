@@ -1,0 +1,959 @@
+// fibmd_capi.cu — the C-ABI of libfibmd_gpu.so: context lifetime, transfers,
+// and the TI/onestep driver (src/timeint.f90:123-242) issuing the kernels.
+//
+// Host arithmetic in this file that feeds decisions the reference makes
+// (radii, cell counts, the 2-body table, regime switches, loop exits) keeps
+// the reference's binary64 operation order; the library is compiled with
+// -ffp-contract=off on the host side.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fibmd_internal.cuh"
+
+using namespace fibmd;
+
+namespace {
+
+std::string g_create_error;
+
+enum Phase { PH_AT = 0, PH_NT = 1, PH_DS = 2, PH_F = 3 };
+
+struct TimedRange {
+  int phase;
+  cudaEvent_t a, b;
+};
+
+}  // namespace
+
+struct fibmd_ctx {
+  fibmd_params p;
+  int dev = 0;
+  int sms = 152;
+  cudaStream_t stream = nullptr;
+  DevParams P;
+  DevState S;
+  DevScalars* h_sc = nullptr;  // pinned mirror
+  double* d_stage = nullptr;   // 3N doubles
+  unsigned long long* d_u64 = nullptr;
+  std::vector<void*> allocs;
+  std::vector<double> tab, tabu;
+  // regime (prms.f90 module variables)
+  double Ts = 0, Tau = 0;
+  int ntlist = 1, atlist = 1, dslist = 1, atm_out = 0;
+  int tic = 1;
+  int impact = 0;
+  bool atom_is_fast = true;
+  bool uploaded = false, lists_built = false, spec_ready = false;
+  // timers
+  bool timers_on = true;
+  double t[4] = {0, 0, 0, 0};
+  long long c[4] = {0, 0, 0, 0};
+  std::vector<TimedRange> pending;
+  std::vector<cudaEvent_t> pool;
+  long long spec_lt = 0;
+  std::string err;
+};
+
+// ---- helpers -------------------------------------------------------------------
+static int fail(fibmd_ctx* ctx, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (ctx) ctx->err = buf;
+  else g_create_error = buf;
+  return code;
+}
+
+#define CK(call)                                                                  \
+  do {                                                                            \
+    cudaError_t e_ = (call);                                                      \
+    if (e_ != cudaSuccess)                                                        \
+      return fail(ctx, FIBMD_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+static int dalloc(fibmd_ctx* ctx, T** ptr, size_t count) {
+  void* p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc(&p, sizeof(T) * count);
+  if (e != cudaSuccess)
+    return fail(ctx, FIBMD_ENOMEM, "cudaMalloc(%zu bytes): %s", sizeof(T) * count,
+                cudaGetErrorString(e));
+  ctx->allocs.push_back(p);
+  *ptr = static_cast<T*>(p);
+  return FIBMD_OK;
+}
+
+static Launch launch_of(const fibmd_ctx* ctx) {
+  Launch L;
+  L.stream = ctx->stream;
+  L.sms = ctx->sms;
+  return L;
+}
+
+static cudaEvent_t get_event(fibmd_ctx* ctx) {
+  if (!ctx->pool.empty()) {
+    cudaEvent_t e = ctx->pool.back();
+    ctx->pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+static void flush_timers(fibmd_ctx* ctx) {
+  for (auto& r : ctx->pending) {
+    float ms = 0.f;
+    cudaEventSynchronize(r.b);
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) ctx->t[r.phase] += 1e-3 * ms;
+    ctx->pool.push_back(r.a);
+    ctx->pool.push_back(r.b);
+  }
+  ctx->pending.clear();
+}
+
+struct PhaseTimer {
+  fibmd_ctx* ctx;
+  int phase;
+  cudaEvent_t a = nullptr;
+  PhaseTimer(fibmd_ctx* c, int ph) : ctx(c), phase(ph) {
+    ctx->c[phase]++;
+    if (ctx->timers_on) {
+      a = get_event(ctx);
+      cudaEventRecord(a, ctx->stream);
+    }
+  }
+  ~PhaseTimer() {
+    if (!a) return;
+    cudaEvent_t b = get_event(ctx);
+    cudaEventRecord(b, ctx->stream);
+    ctx->pending.push_back({phase, a, b});
+    if (ctx->pending.size() > 4096) flush_timers(ctx);
+  }
+};
+
+// ---- parameter derivation --------------------------------------------------------
+// mktables, src/si.f90:575-597, in the reference's operation order.
+static void build_table(const fibmd_params& p, std::vector<double>& tab,
+                        std::vector<double>& tabu, double* umax_out, int* last_nz) {
+  const int Nt = p.Ntable;
+  tab.assign((size_t)Nt + 2, 0.0);
+  tabu.assign((size_t)Nt + 2, 0.0);
+  const double umax = 2.5 * p.listfac * p.al;
+  const double du = umax / (double)(Nt - 1);
+  int last = 0;
+  for (int i = 2; i <= Nt; i++) {
+    const double ui = umax * (double)(i - 1) / (double)(Nt - 1);
+    tabu[i - 1] = ui;
+    if (ui < .999 * p.al) {
+      const double ex = std::exp(1. / (ui - p.al));
+      const double y = (p.B * std::pow(ui, -p.psi) - std::pow(ui, -p.qsi)) /
+                           ((ui - p.al) * (ui - p.al)) +
+                       (p.psi * p.B * std::pow(ui, -p.psi - 1) - p.qsi * std::pow(ui, -p.qsi - 1));
+      tab[i - 1] = -(p.A * ex * y / (du * du));
+      if (tab[i - 1] != 0.0) last = i - 1;
+    }
+  }
+  // u(1) is never set by the reference; a listed pair never reads it
+  *umax_out = umax;
+  *last_nz = last;
+}
+
+static int derive_params(fibmd_ctx* ctx) {
+  const fibmd_params& p = ctx->p;
+  DevParams& P = ctx->P;
+  std::memset(&P, 0, sizeof P);
+  P.N = p.Natm;
+  P.Nsg = p.Nsg;
+  P.nfired = p.Nsg + ctx->impact;
+  P.mode = p.mode;
+  P.precision = p.precision;
+  P.max_sw = p.max_sw_nbrs > 0 ? p.max_sw_nbrs : 48;
+  const double sigmax = p.sigmaGe > p.sigmaSi ? p.sigmaGe : p.sigmaSi;
+  // init_nlist, si.f90:56-61
+  const double rc = p.listfac * p.al * sigmax;
+  const double rlj = 2.5 * sigmax;
+  const double rclj = p.listfac * rlj;
+  long long ncell = 1;
+  for (int d = 0; d < 3; d++) {
+    P.Lb[d] = p.Lb[d];
+    P.iLb[d] = 1. / p.Lb[d];
+    const int n = (int)(p.Lb[d] / rc);
+    P.nc[d] = n > 1 ? n : 1;
+    P.hcell[d] = p.Lb[d] / (double)P.nc[d];  // chainlist's HMf = Lb/REAL(N)
+    P.qscale[d] = 4294967296.0 / p.Lb[d];
+    P.qinvA[d] = (float)(p.Lb[d] * 1.0e10 / 4294967296.0);
+    ncell *= P.nc[d];
+  }
+  if (ncell > (1ll << 30)) return fail(ctx, FIBMD_EINVAL, "cell grid too large (%lld)", ncell);
+  P.ncell = (int)ncell;
+  P.rv2 = rc * rc;
+  P.rv2lj = rclj * rclj;
+  P.rlj2 = rlj * rlj;
+  const double rcA = rc * 1e10, rcljA = rclj * 1e10;
+  P.pre_sw2A = (float)((rcA * (1 + 1e-4)) * (rcA * (1 + 1e-4)));
+  P.acc_sw2A = (float)((rcA * (1 - 1e-4)) * (rcA * (1 - 1e-4)));
+  P.pre_mol2A = (float)((rcljA * (1 + 1e-4)) * (rcljA * (1 + 1e-4)));
+  P.acc_mol2A = (float)((rcljA * (1 - 1e-4)) * (rcljA * (1 - 1e-4)));
+  // Stillinger-Weber constants, setupSiGe (prms.f90:452-480)
+  P.al = p.al;
+  P.gam = p.gamma;
+  P.cut3 = 0.999 * p.al;
+  P.thrd = 1. / 3.;
+  P.A = p.A;
+  P.B = p.B;
+  P.psi = p.psi;
+  P.qsi = p.qsi;
+  P.eps[0][0] = p.epsSi;
+  P.eps[0][1] = 0.5 * (p.epsSi + p.epsGe);
+  P.eps[1][1] = p.epsGe;
+  P.eps[1][0] = 0.5 * (p.epsSi + p.epsGe);
+  P.isig[0][0] = 1. / p.sigmaSi;
+  P.isig[0][1] = 2. / (p.sigmaSi + p.sigmaGe);
+  P.isig[1][1] = 1. / p.sigmaGe;
+  P.isig[1][0] = 2. / (p.sigmaSi + p.sigmaGe);
+  const double l112 = 2. * p.lambdaSi * p.epsSi / 3. + p.lambdaGe * p.epsGe / 3.;
+  const double l122 = p.lambdaSi * p.epsSi / 3. + 2. * p.lambdaGe * p.epsGe / 3.;
+  P.leps[0][0][0] = p.lambdaSi * p.epsSi;
+  P.leps[0][0][1] = P.leps[0][1][0] = P.leps[1][0][0] = l112;
+  P.leps[0][1][1] = P.leps[1][1][0] = P.leps[1][0][1] = l122;
+  P.leps[1][1][1] = p.lambdaGe * p.epsGe;
+  P.epssig[0][0] = p.epsSi / p.sigmaSi;
+  P.epssig[0][1] = P.epssig[1][0] = (p.epsSi + p.epsGe) / (p.sigmaSi + p.sigmaGe);
+  P.epssig[1][1] = p.epsGe / p.sigmaGe;
+  // Moliere constants, setupMol (prms.f90:433-449)
+  const double Pi = 4. * std::atan(1.0);
+  P.Zmol[0] = p.ZSi;
+  P.Zmol[1] = p.ZGe;
+  P.Zmol[2] = p.ZGa;
+  std::memset(P.aamol, 0, sizeof P.aamol);
+  P.aamol[0][2] = 0.885 * p.ao * std::pow(std::sqrt(p.ZSi) + std::sqrt(p.ZGa), -(2. / 3.));
+  P.aamol[1][2] = 0.885 * p.ao * std::pow(std::sqrt(p.ZGe) + std::sqrt(p.ZGa), -(2. / 3.));
+  P.aamol[2][0] = P.aamol[0][2];
+  P.aamol[2][1] = P.aamol[1][2];
+  P.aamol[2][2] = 0.885 * p.ao * std::pow(std::sqrt(p.ZGa) + std::sqrt(p.ZGa), -(2. / 3.));
+  P.ie0 = 1 / (4 * Pi * p.eps0);
+  P.ec = p.ec;
+  P.Amol = p.Amol;
+  P.Bmol = p.Bmol;
+  P.Cmol = p.Cmol;
+  P.amol = p.alpha_mol;
+  P.bmol = p.beta_mol;
+  P.gmol = p.gamma_mol;
+  // 2-body table
+  build_table(p, ctx->tab, ctx->tabu, &P.umax, &P.tab_last);
+  P.Ntable = p.Ntable;
+  const double usup = std::max(P.cut3, ctx->tabu[(size_t)P.tab_last + 1]);
+  const double rsupA = usup * sigmax * 1e10 * (1 + 1e-4);
+  P.pre3A2 = (float)(rsupA * rsupA);
+  // fast atoms: displaced by at least half the smaller list skin
+  const double skin = std::min(rc - P.cut3 * sigmax, rclj - rlj);
+  const double half = 0.5 * skin * 0.99;
+  P.disp_fast2 = half * half;
+  // binary32 reduced units
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++) {
+      P.epsA[a][b] = (float)(P.eps[a][b] / p.ec);
+      P.sigA[a][b] = (float)(1e10 / P.isig[a][b]);
+      for (int c = 0; c < 2; c++) P.lepsA[a][b][c] = (float)(P.leps[a][b][c] / p.ec);
+    }
+  for (int a = 0; a < 3; a++)
+    for (int b = 0; b < 3; b++) {
+      P.molKA[a][b] = (float)(P.ie0 * P.Zmol[a] * P.Zmol[b] * p.ec * 1e10);
+      P.amolA[a][b] = (float)(P.aamol[a][b] * 1e10);
+    }
+  P.f_evA_to_N = p.ec * 1e10;
+  P.e_eV_to_J = p.ec;
+  P.mol_fp64_rA = (float)(p.mixed_mol_fp64_r * 1e10);
+  // integrator geometry
+  P.kB = p.kB;
+  const double nm = 1.0e-9;
+  const double L3 = p.Lb[2];
+  P.side_sw = p.sidewidth * nm;
+  P.side_zlo = p.outz[0] * L3 / 10.0;
+  P.side_zhi = p.outz[3] * L3 / 10.0;
+  for (int k = 0; k < 4; k++) P.park_o[k] = p.outz[k] * L3 / 10.0;
+  const double buffer = 0.3;
+  for (int k = 0; k < 2; k++) {
+    P.park_a[k] = p.atomz[k] * L3 / 10.0;
+    P.park_al[k] = (p.atomz[k] - buffer) * L3 / 10.0;
+    P.park_ah[k] = (p.atomz[k] + buffer) * L3 / 10.0;
+  }
+  P.park_il = (p.ionz - buffer) * L3 / 10.0;
+  P.park_ih = (p.ionz + buffer) * L3 / 10.0;
+  P.remove_z = p.remove_z;
+  P.dt_max = p.dt_max;
+  P.dx_max = p.dx_max;
+  P.tau_spec = p.tau_spec;
+  // Moliere full-list capacity: at least the reference's MLlj = 1500*Nlj
+  long long mlj = 1500ll * (p.Nlj > 0 ? p.Nlj : 1);
+  P.mol_cap = p.max_mol_pairs > 0 ? p.max_mol_pairs : (int)std::max<long long>(mlj, 1 << 16);
+  return FIBMD_OK;
+}
+
+// ionrun, src/prms.f90:563-584
+static void set_regime(fibmd_ctx* ctx, int tic) {
+  const fibmd_params& p = ctx->p;
+  if (tic == 1) {
+    ctx->Ts = p.Ts_i;
+    ctx->atm_out = p.atm_out_i;
+    ctx->ntlist = p.ntlist_i;
+    ctx->atlist = p.atlist_i;
+    ctx->Tau = p.Tau_i;
+    ctx->dslist = p.dslist_i;
+  } else if (tic == 2) {
+    ctx->Ts = p.Ts_r;
+    ctx->atm_out = p.atm_out_r;
+    ctx->ntlist = p.ntlist_r;
+    ctx->atlist = p.atlist_r;
+    ctx->Tau = p.Tau_r;
+    ctx->dslist = p.dslist_r;
+  }
+  ctx->tic = tic;
+}
+
+static int sync_scalars(fibmd_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->h_sc, ctx->S.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
+}
+
+// ---- C-ABI -----------------------------------------------------------------------
+extern "C" {
+
+int fibmd_gpu_abi_version(void) { return FIBMD_ABI_VERSION; }
+
+int fibmd_gpu_params_size(void) { return (int)sizeof(fibmd_params); }
+
+int fibmd_gpu_params_default(fibmd_params* p) {
+  if (!p) return FIBMD_EINVAL;
+  std::memset(p, 0, sizeof(*p));
+  p->abi_version = FIBMD_ABI_VERSION;
+  p->mode = FIBMD_MODE_REF;
+  p->precision = FIBMD_PREC_FP64;
+  // prms.f90:172-216
+  p->A = 7.049556277;
+  p->B = 0.6022245584;
+  p->psi = 4.0;
+  p->qsi = 0.0;
+  p->al = 1.8;
+  p->gamma = 1.2;
+  p->lambdaSi = 21.0;
+  p->lambdaGe = 31.0;
+  p->epsSi = 3.473928E-19;
+  p->epsGe = 3.085E-19;
+  p->sigmaSi = 2.0951E-10;
+  p->sigmaGe = 2.0951E-10;
+  p->massSi = 46.637063E-27;
+  p->massGe = 120.6049350E-27;
+  p->massGa = 1.157777417E-25;
+  p->ZSi = 14.0;
+  p->ZGe = 32.0;
+  p->ZGa = 31.0;
+  p->Amol = 0.35;
+  p->Bmol = 0.55;
+  p->Cmol = 0.10;
+  p->alpha_mol = 0.3;
+  p->beta_mol = 1.2;
+  p->gamma_mol = 6.0;
+  p->kB = 1.381E-23;
+  p->eps0 = 8.854187E-12;
+  p->ec = 1.60217646E-19;
+  p->ao = 0.053E-09;
+  p->listfac = 1.1;
+  p->Ntable = 12000;
+  // siga.in as shipped with the reference
+  p->Ts_i = 2.0E-17;
+  p->Ts_r = 2.0E-16;
+  p->Ttar1 = 300.0;
+  p->ke_limit_1 = 600.0;
+  p->Tau_i = 1.E-13;
+  p->Tau_r = 1.E-13;
+  p->Teps = 30.0;
+  p->ntlist_i = 50;
+  p->ntlist_r = 20;
+  p->atlist_i = 50;
+  p->atlist_r = 20;
+  p->dslist_i = 500;
+  p->dslist_r = 500;
+  p->atm_out_i = 50;
+  p->atm_out_r = 500;
+  p->res_out = -5000;
+  p->outz[0] = 1.3;
+  p->outz[1] = 3.5;
+  p->outz[2] = 7.5;
+  p->outz[3] = 9.8;
+  p->atomz[0] = 4.5;
+  p->atomz[1] = 6.5;
+  p->ionz = 5.5;
+  p->knockz = 1.25;
+  p->sidewidth = 1.5;
+  p->dti = 1e-12;
+  // spec-mode defaults: 1 fs cap, 0.05 A per step, 0.1 ps thermostat
+  p->dt_max = 1.0e-15;
+  p->dx_max = 0.05e-10;
+  p->tau_spec = 1.0e-13;
+  p->remove_z = -1.0;
+  p->mixed_mol_fp64_r = 1.0e-10;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_last_error(const fibmd_ctx* ctx, char* buf, int len) {
+  if (!buf || len <= 0) return FIBMD_EINVAL;
+  const std::string& s = ctx ? ctx->err : g_create_error;
+  std::snprintf(buf, (size_t)len, "%s", s.c_str());
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
+  fibmd_ctx* ctx = nullptr;
+  if (!p || !out) return fail(nullptr, FIBMD_EINVAL, "null argument");
+  *out = nullptr;
+  if (p->abi_version != FIBMD_ABI_VERSION)
+    return fail(nullptr, FIBMD_EINVAL, "abi_version %d, library has %d", p->abi_version,
+                FIBMD_ABI_VERSION);
+  if (p->Natm <= 0 || p->Nsg < 0 || p->Nsg > p->Natm || p->Lb[0] <= 0 || p->Lb[1] <= 0 ||
+      p->Lb[2] <= 0 || p->Ntable < 8)
+    return fail(nullptr, FIBMD_EINVAL, "bad sizes (Natm %d Nsg %d Ntable %d)", p->Natm, p->Nsg,
+                p->Ntable);
+  if (p->precision == FIBMD_PREC_MIXED && (p->psi != 4.0 || p->qsi != 0.0))
+    return fail(nullptr, FIBMD_EINVAL, "mixed precision implements psi = 4, qsi = 0 only");
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+
+  ctx = new fibmd_ctx();
+  ctx->p = *p;
+  int rc = derive_params(ctx);
+  if (rc) {
+    g_create_error = ctx->err;
+    delete ctx;
+    return rc;
+  }
+  cudaGetDevice(&ctx->dev);
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->dev);
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    g_create_error = "cudaStreamCreate failed";
+    delete ctx;
+    return FIBMD_ECUDA;
+  }
+  const size_t N = (size_t)p->Natm;
+  DevState& S = ctx->S;
+  std::memset(&S, 0, sizeof S);
+  S.N = (int)N;
+  int nscan = (ctx->P.ncell + 1 + 1023) / 1024;
+#define AL(ptr, n)                       \
+  do {                                   \
+    int r_ = dalloc(ctx, &(ptr), (n));   \
+    if (r_) {                            \
+      g_create_error = ctx->err;         \
+      fibmd_gpu_destroy(ctx);            \
+      return r_;                         \
+    }                                    \
+  } while (0)
+  AL(S.pos, N);
+  AL(S.vel, N);
+  AL(S.frc, N);
+  AL(S.frc_new, N);
+  AL(S.xi, N);
+  AL(S.pos_build, N);
+  AL(S.posq, N);
+  AL(S.mass, N);
+  AL(S.atype, N);
+  AL(S.flags, N);
+  AL(S.cell_count, (size_t)ctx->P.ncell + 1);
+  AL(S.cell_start, (size_t)ctx->P.ncell + 1);
+  AL(S.cell_atoms, N);
+  AL(S.atom_cell, N);
+  AL(S.scan_blocks, (size_t)nscan + 1);
+  AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
+  AL(S.n_sw, N);
+  AL(S.mol_pairs, (size_t)ctx->P.mol_cap);
+  AL(S.fast_flag, N);
+  AL(S.fast_list, N);
+  AL(S.heavy_list, N);
+  double* tab = nullptr;
+  double* tabu = nullptr;
+  AL(tab, ctx->tab.size());
+  AL(tabu, ctx->tabu.size());
+  S.tab = tab;
+  S.tabu = tabu;
+  AL(S.epot, N);
+  AL(S.partials, 3 * (size_t)kMaxRedBlocks);
+  AL(S.sc, 1);
+  AL(ctx->d_stage, 3 * N);
+  AL(ctx->d_u64, 4);
+#undef AL
+  if (cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
+    g_create_error = "cudaMallocHost failed";
+    fibmd_gpu_destroy(ctx);
+    return FIBMD_ENOMEM;
+  }
+  cudaMemcpyAsync(tab, ctx->tab.data(), sizeof(double) * ctx->tab.size(),
+                  cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemcpyAsync(tabu, ctx->tabu.data(), sizeof(double) * ctx->tabu.size(),
+                  cudaMemcpyHostToDevice, ctx->stream);
+  cudaMemsetAsync(S.sc, 0, sizeof(DevScalars), ctx->stream);
+  cudaMemsetAsync(S.fast_flag, 0, N, ctx->stream);
+  cudaMemsetAsync(S.n_sw, 0, sizeof(int) * N, ctx->stream);
+  cudaMemsetAsync(S.frc, 0, sizeof(double4_32a) * N, ctx->stream);
+  cudaMemsetAsync(S.flags, 0, sizeof(uint32_t) * N, ctx->stream);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
+    g_create_error = "initialisation copies failed";
+    fibmd_gpu_destroy(ctx);
+    return FIBMD_ECUDA;
+  }
+  set_regime(ctx, 1);
+  *out = ctx;
+  return FIBMD_OK;
+}
+
+void fibmd_gpu_destroy(fibmd_ctx* ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  flush_timers(ctx);
+  for (auto e : ctx->pool) cudaEventDestroy(e);
+  for (void* p : ctx->allocs) cudaFree(p);
+  if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+void* fibmd_gpu_stream(fibmd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const double* F,
+                     const double* Xi, const double* mass, const int* atype,
+                     const int* xsides) {
+  if (!ctx || !X || !V || !Xi || !mass || !atype || !xsides)
+    return fail(ctx, FIBMD_EINVAL, "upload: null array");
+  const int N = ctx->P.N;
+  const size_t b3 = sizeof(double) * 3 * (size_t)N;
+  Launch L = launch_of(ctx);
+  std::vector<int8_t> t8((size_t)N);
+  std::vector<uint32_t> fl((size_t)N);
+  for (int i = 0; i < N; i++) {
+    if (atype[i] < 1 || atype[i] > 3)
+      return fail(ctx, FIBMD_EINVAL, "atype(%d) = %d is not 1, 2 or 3", i + 1, atype[i]);
+    t8[i] = (int8_t)atype[i];
+    fl[i] = xsides[i] > 0 ? FL_FROZEN : 0u;
+  }
+  const double* src[4] = {X, V, F, Xi};
+  double4_32a* dst[4] = {ctx->S.pos, ctx->S.vel, ctx->S.frc, ctx->S.xi};
+  for (int k = 0; k < 4; k++) {
+    if (!src[k]) {
+      CK(cudaMemsetAsync(dst[k], 0, sizeof(double4_32a) * (size_t)N, ctx->stream));
+      continue;
+    }
+    CK(cudaMemcpyAsync(ctx->d_stage, src[k], b3, cudaMemcpyHostToDevice, ctx->stream));
+    CK(launch_pack(L, N, dst[k], ctx->d_stage));
+  }
+  CK(cudaMemcpyAsync(ctx->S.mass, mass, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(cudaMemcpyAsync(ctx->S.atype, t8.data(), (size_t)N, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->S.flags, fl.data(), sizeof(uint32_t) * (size_t)N,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_update_posq(L, ctx->P, ctx->S));
+  if (ctx->lists_built) CK(launch_track_all(L, ctx->P, ctx->S));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->uploaded = true;
+  ctx->spec_ready = false;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags) {
+  if (!ctx || !tags) return FIBMD_EINVAL;
+  const int N = ctx->P.N;
+  CK(cudaMemcpyAsync(ctx->S.flags, tags, sizeof(uint32_t) * (size_t)N, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  CK(launch_update_posq(launch_of(ctx), ctx->P, ctx->S));
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->spec_ready = false;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F) {
+  if (!ctx) return FIBMD_EINVAL;
+  if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "download before upload");
+  const int N = ctx->P.N;
+  const size_t b3 = sizeof(double) * 3 * (size_t)N;
+  Launch L = launch_of(ctx);
+  double* dstv[3] = {X, V, F};
+  const double4_32a* srcv[3] = {ctx->S.pos, ctx->S.vel, ctx->S.frc};
+  for (int k = 0; k < 3; k++) {
+    if (!dstv[k]) continue;
+    CK(launch_unpack(L, N, srcv[k], ctx->d_stage));
+    CK(cudaMemcpyAsync(dstv[k], ctx->d_stage, b3, cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_set_atom(fibmd_ctx* ctx, int i, const double x[3], const double v[3]) {
+  if (!ctx || i < 1 || i > ctx->P.N || !x || !v) return fail(ctx, FIBMD_EINVAL, "set_atom: bad args");
+  double4_32a px = make_double4_32a(x[0], x[1], x[2], 0.0);
+  double4_32a pv = make_double4_32a(v[0], v[1], v[2], 0.0);
+  CK(cudaMemcpyAsync(ctx->S.pos + (i - 1), &px, sizeof px, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->S.vel + (i - 1), &pv, sizeof pv, cudaMemcpyHostToDevice, ctx->stream));
+  CK(launch_update_posq(launch_of(ctx), ctx->P, ctx->S));
+  if (ctx->lists_built) CK(launch_track_all(launch_of(ctx), ctx->P, ctx->S));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_set_impact(fibmd_ctx* ctx, int impact) {
+  if (!ctx || impact < 0) return FIBMD_EINVAL;
+  ctx->impact = impact;
+  ctx->P.nfired = ctx->p.Nsg + impact;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_ionrun(fibmd_ctx* ctx, int tic) {
+  if (!ctx || (tic != 1 && tic != 2)) return FIBMD_EINVAL;
+  set_regime(ctx, tic);
+  ctx->atom_is_fast = (tic == 1);
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_set_tau(fibmd_ctx* ctx, double tau) {
+  if (!ctx || !(tau > 0)) return FIBMD_EINVAL;
+  ctx->Tau = tau;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_regime(fibmd_ctx* ctx, double* Ts, int* tic) {
+  if (!ctx) return FIBMD_EINVAL;
+  if (Ts) *Ts = ctx->Ts;
+  if (tic) *tic = ctx->tic;
+  return FIBMD_OK;
+}
+
+static int check_list_status(fibmd_ctx* ctx) {
+  const DevScalars& h = *ctx->h_sc;
+  if (h.overflow_sw)
+    return fail(ctx, FIBMD_EOVERFLOW, "%d atoms exceeded %d SW list slots", h.overflow_sw,
+                ctx->P.max_sw);
+  if (h.overflow_mol)
+    return fail(ctx, FIBMD_EOVERFLOW, "Moliere list needs %d entries, capacity %d",
+                h.overflow_mol, ctx->P.mol_cap);
+  if (h.table_err)
+    return fail(ctx, FIBMD_ETABLE, "2-body table index beyond Ntable (%d pairs)", h.table_err);
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_nlist(fibmd_ctx* ctx) {
+  if (!ctx) return FIBMD_EINVAL;
+  if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "nlist before upload");
+  {
+    PhaseTimer t(ctx, PH_NT);
+    CK(launch_build_lists(launch_of(ctx), ctx->P, ctx->S, 0));
+  }
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  ctx->lists_built = true;
+  return check_list_status(ctx);
+}
+
+int fibmd_gpu_list_counts(fibmd_ctx* ctx, long long* n_sw_full, long long* n_mol_full,
+                          long long* n_triplets) {
+  if (!ctx || !ctx->lists_built) return fail(ctx, FIBMD_ESTATE, "lists not built");
+  const int N = ctx->P.N;
+  if (n_sw_full) {
+    std::vector<int> n((size_t)N);
+    CK(cudaMemcpy(n.data(), ctx->S.n_sw, sizeof(int) * (size_t)N, cudaMemcpyDeviceToHost));
+    long long s = 0;
+    for (int v : n) s += v;
+    *n_sw_full = s;
+  }
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  if (n_mol_full) *n_mol_full = ctx->h_sc->mol_count;
+  if (n_triplets) {
+    CK(cudaMemsetAsync(ctx->d_u64, 0, sizeof(unsigned long long), ctx->stream));
+    CK(launch_count_triplets(launch_of(ctx), ctx->P, ctx->S, ctx->d_u64, nullptr, 0));
+    unsigned long long c = 0;
+    CK(cudaMemcpyAsync(&c, ctx->d_u64, sizeof c, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    *n_triplets = (long long)c;
+  }
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_get_pairs(fibmd_ctx* ctx, int kind, int* n, int* ij, int cap) {
+  if (!ctx || !n || (kind != 0 && kind != 1)) return FIBMD_EINVAL;
+  if (!ctx->lists_built) return fail(ctx, FIBMD_ESTATE, "lists not built");
+  const int N = ctx->P.N;
+  std::vector<std::pair<int, int>> pr;
+  if (kind == 0) {
+    std::vector<int> cnt((size_t)N), nb((size_t)ctx->P.max_sw * N);
+    CK(cudaMemcpy(cnt.data(), ctx->S.n_sw, sizeof(int) * (size_t)N, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(nb.data(), ctx->S.nbr_sw, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < N; i++)
+      for (int k = 0; k < cnt[i]; k++) {
+        int j = nb[(size_t)k * N + i];
+        if (j > i) pr.emplace_back(i + 1, j + 1);
+      }
+  } else {
+    int rc = sync_scalars(ctx);
+    if (rc) return rc;
+    int m = std::min(ctx->h_sc->mol_count, ctx->P.mol_cap);
+    std::vector<int2> mp((size_t)m);
+    if (m) CK(cudaMemcpy(mp.data(), ctx->S.mol_pairs, sizeof(int2) * (size_t)m, cudaMemcpyDeviceToHost));
+    for (auto& q : mp)
+      if (q.y > q.x) pr.emplace_back(q.x + 1, q.y + 1);
+  }
+  std::sort(pr.begin(), pr.end());
+  *n = (int)pr.size();
+  if (ij)
+    for (int k = 0; k < (int)pr.size() && k < cap; k++) {
+      ij[2 * k] = pr[k].first;
+      ij[2 * k + 1] = pr[k].second;
+    }
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_get_triplets(fibmd_ctx* ctx, long long* n, int* ijk, long long cap) {
+  if (!ctx || !n) return FIBMD_EINVAL;
+  long long total = 0;
+  int rc = fibmd_gpu_list_counts(ctx, nullptr, nullptr, &total);
+  if (rc) return rc;
+  *n = total;
+  if (!ijk || total == 0) return FIBMD_OK;
+  int3* d = nullptr;
+  CK(cudaMalloc(&d, sizeof(int3) * (size_t)total));
+  CK(cudaMemsetAsync(ctx->d_u64, 0, sizeof(unsigned long long), ctx->stream));
+  CK(launch_count_triplets(launch_of(ctx), ctx->P, ctx->S, ctx->d_u64, d, total));
+  std::vector<int3> h((size_t)total);
+  CK(cudaMemcpyAsync(h.data(), d, sizeof(int3) * (size_t)total, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(d);
+  std::sort(h.begin(), h.end(), [](const int3& a, const int3& b) {
+    if (a.x != b.x) return a.x < b.x;
+    if (a.y != b.y) return a.y < b.y;
+    return a.z < b.z;
+  });
+  for (long long k = 0; k < total && k < cap; k++) {
+    ijk[3 * k] = h[k].x + 1;
+    ijk[3 * k + 1] = h[k].y + 1;
+    ijk[3 * k + 2] = h[k].z + 1;
+  }
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_force(fibmd_ctx* ctx, double* F_out, double* u_out, double* Utot) {
+  if (!ctx) return FIBMD_EINVAL;
+  if (!ctx->lists_built) return fail(ctx, FIBMD_ESTATE, "force before nlist");
+  const bool energy = u_out || Utot;
+  {
+    PhaseTimer t(ctx, PH_F);
+    CK(launch_force(launch_of(ctx), ctx->P, ctx->S, energy, true));
+  }
+  std::swap(ctx->S.frc, ctx->S.frc_new);
+  if (F_out) {
+    int rc = fibmd_gpu_download(ctx, nullptr, nullptr, F_out);
+    if (rc) return rc;
+  }
+  if (energy) {
+    const int N = ctx->P.N;
+    std::vector<double> u((size_t)N);
+    CK(cudaMemcpyAsync(u.data(), ctx->S.epot, sizeof(double) * (size_t)N,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (u_out) std::memcpy(u_out, u.data(), sizeof(double) * (size_t)N);
+    if (Utot) {
+      double s = 0.0;
+      for (double v : u) s += v;
+      *Utot = s;
+    }
+  }
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  return check_list_status(ctx);
+}
+
+int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[4]) {
+  if (!ctx || !counts) return FIBMD_EINVAL;
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  counts[0] = (long long)(ctx->h_sc->counters[0] / 2);
+  counts[1] = (long long)ctx->h_sc->counters[1];
+  counts[2] = (long long)(ctx->h_sc->counters[2] / 2);
+  counts[3] = (long long)ctx->h_sc->counters[3];
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_temperature(fibmd_ctx* ctx, double* T) {
+  if (!ctx || !T) return FIBMD_EINVAL;
+  CK(launch_temperature(launch_of(ctx), ctx->P, ctx->S));
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  *T = ctx->h_sc->temp;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds, double* f,
+                     long long* counts4, int reset) {
+  if (!ctx) return FIBMD_EINVAL;
+  cudaStreamSynchronize(ctx->stream);
+  flush_timers(ctx);
+  if (at) *at = ctx->t[PH_AT];
+  if (nt) *nt = ctx->t[PH_NT];
+  if (ds) *ds = ctx->t[PH_DS];
+  if (f) *f = ctx->t[PH_F];
+  if (counts4)
+    for (int k = 0; k < 4; k++) counts4[k] = ctx->c[k];
+  if (reset)
+    for (int k = 0; k < 4; k++) {
+      ctx->t[k] = 0;
+      ctx->c[k] = 0;
+    }
+  return FIBMD_OK;
+}
+
+// ---- one reference step (onestep, timeint.f90:158-242) ---------------------------
+static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, int* why) {
+  const Launch L = launch_of(ctx);
+  const DevParams& P = ctx->P;
+  const double Ttar = ctx->p.Ttar1;
+  *time = *time + ctx->Ts;
+  if (whichctrl == 0) CK(launch_adjust_and_temp(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar));
+  if (whichctrl > 0) CK(launch_side_reduce(L, P, ctx->S));
+  CK(launch_drift(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar, whichctrl > 0));
+  if (ctx->atlist > 0 && lt % ctx->atlist == 0) {
+    PhaseTimer t(ctx, PH_AT);
+    CK(launch_park(L, P, ctx->S));
+  }
+  if (ctx->ntlist > 0 && lt % ctx->ntlist == 0) {
+    PhaseTimer t(ctx, PH_NT);
+    CK(launch_build_lists(L, P, ctx->S, 0));
+  }
+  if (ctx->dslist > 0 && lt % ctx->dslist == 0 && whichctrl == 1) {
+    {
+      PhaseTimer t(ctx, PH_DS);
+      CK(launch_ke_max(L, P, ctx->S));
+    }
+    int rc = sync_scalars(ctx);
+    if (rc) return rc;
+    if (ctx->h_sc->ke_max < ctx->p.ke_limit_1 && ctx->atom_is_fast) {
+      set_regime(ctx, 2);
+      ctx->atom_is_fast = false;
+      *why |= FIBMD_STOP_REGIME;
+    }
+  }
+  {
+    PhaseTimer t(ctx, PH_F);
+    CK(launch_force(L, P, ctx->S, false, false));
+  }
+  CK(launch_kick(L, P, ctx->S, ctx->Ts));
+  std::swap(ctx->S.frc, ctx->S.frc_new);
+  return FIBMD_OK;
+}
+
+static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double* time,
+                      double* temp, int* reason) {
+  const Launch L = launch_of(ctx);
+  const DevParams& P = ctx->P;
+  const double Ttar = ctx->p.Ttar1;
+  if (!ctx->spec_ready) {
+    double t0 = *time;
+    CK(cudaMemcpyAsync(&ctx->S.sc->time, &t0, sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(launch_spec_kick(L, P, ctx->S, Ttar, 0));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->spec_ready = true;
+  }
+  for (long long n = 0; n < max_steps; n++) {
+    CK(launch_spec_drift(L, P, ctx->S, Ttar));
+    {
+      PhaseTimer t(ctx, PH_NT);
+      CK(launch_build_lists(L, P, ctx->S, 1));
+    }
+    {
+      PhaseTimer t(ctx, PH_F);
+      CK(launch_force(L, P, ctx->S, false, false));
+    }
+    CK(launch_spec_kick(L, P, ctx->S, Ttar, 1));
+    std::swap(ctx->S.frc, ctx->S.frc_new);
+    *lt = *lt + 1;
+  }
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  *time = ctx->h_sc->time;
+  if (temp) {
+    rc = fibmd_gpu_temperature(ctx, temp);
+    if (rc) return rc;
+  }
+  *reason = FIBMD_STOP_MAXSTEPS;
+  return check_list_status(ctx);
+}
+
+int fibmd_gpu_steps(fibmd_ctx* ctx, int whichctrl, long long max_steps, long long* lt,
+                    double* time, double* temp, int* reason) {
+  if (!ctx || !lt || !time || !temp || !reason) return FIBMD_EINVAL;
+  if (!ctx->uploaded || !ctx->lists_built)
+    return fail(ctx, FIBMD_ESTATE, "steps before upload and nlist");
+  if (whichctrl < 0 || whichctrl > 2) return fail(ctx, FIBMD_EINVAL, "whichctrl %d", whichctrl);
+  *reason = 0;
+  if (ctx->p.mode == FIBMD_MODE_SPEC) return spec_steps(ctx, max_steps, lt, time, temp, reason);
+  const double Ttar = ctx->p.Ttar1;
+  int why = 0;
+  if (whichctrl == 0) {
+    // adjusttemp uses the temperature the caller's loop holds
+    CK(cudaMemcpyAsync(&ctx->S.sc->temp, temp, sizeof(double), cudaMemcpyHostToDevice,
+                       ctx->stream));
+  }
+  long long n = 0;
+  for (;;) {
+    if (whichctrl == 0 && !(std::fabs(*temp - Ttar) > ctx->p.Teps)) {
+      why |= FIBMD_STOP_DONE;
+      break;
+    }
+    if (n >= max_steps) {
+      why |= FIBMD_STOP_MAXSTEPS;
+      break;
+    }
+    const long long l = *lt + 1;
+    *lt = l;
+    if (whichctrl == 1 && *time > (double)ctx->impact * ctx->p.dti) {
+      why |= FIBMD_STOP_DONE;
+      break;
+    }
+    int rc = onestep(ctx, whichctrl, l, time, &why);
+    if (rc) return rc;
+    n++;
+    if (whichctrl == 0) {
+      rc = sync_scalars(ctx);
+      if (rc) return rc;
+      *temp = ctx->h_sc->temp;
+    } else {
+      // iostuff: atm_out/res_out steps hand the state to the host writer
+      const bool dump = (ctx->p.res_out > 0 && l % ctx->p.res_out == 0) ||
+                        (ctx->atm_out > 0 && l % ctx->atm_out == 0);
+      if (dump) {
+        rc = fibmd_gpu_temperature(ctx, temp);
+        if (rc) return rc;
+        why |= FIBMD_STOP_DUMP;
+        break;
+      }
+    }
+  }
+  *reason = why;
+  int rc = sync_scalars(ctx);
+  if (rc) return rc;
+  return check_list_status(ctx);
+}
+
+}  // extern "C"

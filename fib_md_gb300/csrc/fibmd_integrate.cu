@@ -1,0 +1,445 @@
+// fibmd_integrate.cu — velocity-Verlet step and its reductions.
+//
+// Replaces onestep's position and velocity updates (src/timeint.f90:185-188,
+// 231-236), controlsidetemp (src/temp.f90:32-67), adjusttemp/temperature
+// (src/temp.f90:160-205), freezsidesN and rebox (src/tools.f90:26-51),
+// frzsptrdatms (src/temp.f90:99-127) and calc_atm (src/timeint.f90:277-298).
+// All updates are binary64 and keep the reference's operation order. Sums
+// use a deterministic two-level reduction (block partials summed in block
+// order by the last block), so repeated runs give identical thermostat
+// factors.
+#include "fibmd_internal.cuh"
+
+namespace fibmd {
+
+// controlsidetemp's predicate, temp.f90:45-47. Fortran's .and. binds tighter
+// than .or.: x-edge .or. (y-edge .and. z-band).
+__device__ __forceinline__ bool ref_side_atom(const DevParams& P, double x, double y,
+                                              double z) {
+  const bool xe = (x < P.side_sw) || (x > (P.Lb[0] - P.side_sw));
+  const bool ye = (y < P.side_sw) || (y > (P.Lb[1] - P.side_sw));
+  const bool zb = (z < P.side_zlo) || (z > P.side_zhi);
+  return xe || (ye && zb);
+}
+
+// Marks an atom displaced by at least half the list skin since the last
+// build (its angle terms may include stale-list terms, ref mode) and returns
+// the squared displacement (spec-mode rebuild trigger).
+__device__ __forceinline__ double track_displacement(const DevParams& P, const DevState& S,
+                                                     int i, double x, double y, double z) {
+  const double4_32a b = S.pos_build[i];
+  const double dx = min_image(x, b.x, P.iLb[0], P.Lb[0]);
+  const double dy = min_image(y, b.y, P.iLb[1], P.Lb[1]);
+  const double dz = min_image(z, b.z, P.iLb[2], P.Lb[2]);
+  const double d2 = dx * dx + dy * dy + dz * dz;
+  if (P.mode == FIBMD_MODE_REF && d2 >= P.disp_fast2 && !S.fast_flag[i]) {
+    S.fast_flag[i] = 1;
+    const int slot = atomicAdd(&S.sc->fast_count, 1);
+    S.fast_list[slot] = i;
+  }
+  return d2;
+}
+
+__device__ __forceinline__ void store_posq(const DevParams& P, const DevState& S, int i,
+                                           double x, double y, double z, uint32_t fl) {
+  int4 q;
+  q.x = (int)fixq(x, P.qscale[0]);
+  q.y = (int)fixq(y, P.qscale[1]);
+  q.z = (int)fixq(z, P.qscale[2]);
+  q.w = (int)(uint8_t)S.atype[i] | (int)(fl << 8);
+  S.posq[i] = q;
+}
+
+static int red_blocks(const DevParams& P) {
+  int nb = (P.N + kRedThreads * 4 - 1) / (kRedThreads * 4);
+  if (nb < 1) nb = 1;
+  if (nb > kMaxRedBlocks) nb = kMaxRedBlocks;
+  return nb;
+}
+
+// ---- controlsidetemp: sum m v^2 and count over edge atoms (atype < 3) -----
+__global__ void __launch_bounds__(kRedThreads) k_side_reduce(DevParams P, DevState S) {
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    if (S.atype[i] >= 3) continue;
+    const double4_32a p = S.pos[i];
+    if (!ref_side_atom(P, p.x, p.y, p.z)) continue;
+    const double4_32a u = S.vel[i];
+    v[0] += S.mass[i] * (u.x * u.x + u.y * u.y + u.z * u.z);
+    v[1] += 1.0;
+  }
+  block_sum<2>(v);
+  if (grid_finish<2, false>(v, S.partials, &S.sc->ticket[0])) {
+    S.sc->side_sum = v[0];
+    S.sc->side_cnt = v[1];
+  }
+}
+
+cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S) {
+  k_side_reduce<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// ---- adjusttemp followed by temperature (warm-up, whichctrl 0) -------------
+__global__ void __launch_bounds__(kRedThreads) k_adjust_temp(DevParams P, DevState S,
+                                                             double Ts, double Tau,
+                                                             double Ttar) {
+  const double Temp = ((volatile DevScalars*)S.sc)->temp;
+  const double s = sqrt(1. + Ts / Tau * (Ttar / Temp - 1.));
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    if (S.atype[i] >= 3) continue;
+    double4_32a u = S.vel[i];
+    u.x = s * u.x;
+    u.y = s * u.y;
+    u.z = s * u.z;
+    S.vel[i] = u;
+    v[0] += S.mass[i] * (u.x * u.x + u.y * u.y + u.z * u.z);
+  }
+  block_sum<1>(v);
+  // the last block writes the new temperature after every block has read
+  // the old one
+  if (grid_finish<1, false>(v, S.partials, &S.sc->ticket[1]))
+    S.sc->temp = v[0] / 3. / (double)P.Nsg / P.kB;
+}
+
+cudaError_t launch_adjust_and_temp(const Launch& L, const DevParams& P, const DevState& S,
+                                   double Ts, double Tau, double Ttar) {
+  k_adjust_temp<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S, Ts, Tau, Ttar);
+  return cudaGetLastError();
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_temperature(DevParams P, DevState S) {
+  double v[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    if (S.atype[i] >= 3) continue;
+    const double4_32a u = S.vel[i];
+    v[0] += S.mass[i] * (u.x * u.x + u.y * u.y + u.z * u.z);
+  }
+  block_sum<1>(v);
+  if (grid_finish<1, false>(v, S.partials, &S.sc->ticket[2]))
+    S.sc->temp = v[0] / 3. / (double)P.Nsg / P.kB;
+}
+
+cudaError_t launch_temperature(const Launch& L, const DevParams& P, const DevState& S) {
+  k_temperature<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// ---- drift: edge thermostat, X += V Ts + F Ts^2/(2m), freeze, rebox --------
+__global__ void __launch_bounds__(256) k_drift(DevParams P, DevState S, double Ts, double Tau,
+                                               double Ttar, int side) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.N) return;
+  double4_32a x = S.pos[i];
+  double4_32a v = S.vel[i];
+  if (side && S.atype[i] < 3) {
+    const double cnt = S.sc->side_cnt;
+    if (cnt > 0.0 && ref_side_atom(P, x.x, x.y, x.z)) {
+      const double ts = S.sc->side_sum / 3. / cnt / P.kB;
+      const double s = sqrt(1. + Ts / Tau * (Ttar / ts - 1.));
+      v.x = s * v.x;
+      v.y = s * v.y;
+      v.z = s * v.z;
+    }
+  }
+  const double4_32a f = S.frc[i];
+  const double m = S.mass[i];
+  x.x = x.x + v.x * Ts + 0.5 * f.x * Ts * Ts / m;
+  x.y = x.y + v.y * Ts + 0.5 * f.y * Ts * Ts / m;
+  x.z = x.z + v.z * Ts + 0.5 * f.z * Ts * Ts / m;
+  const uint32_t fl = S.flags[i];
+  if (fl & FL_FROZEN) {
+    const double4_32a xi = S.xi[i];
+    x.x = xi.x;
+    x.y = xi.y;
+    x.z = xi.z;
+    v.x = 0.;
+    v.y = 0.;
+    v.z = 0.;
+  }
+  // rebox: MOD(X + 2 Lb, Lb); fmod is exact, as Fortran's MOD of reals
+  x.x = fmod(x.x + 2. * P.Lb[0], P.Lb[0]);
+  x.y = fmod(x.y + 2. * P.Lb[1], P.Lb[1]);
+  x.z = fmod(x.z + 2. * P.Lb[2], P.Lb[2]);
+  S.pos[i] = x;
+  S.vel[i] = v;
+  store_posq(P, S, i, x.x, x.y, x.z, fl);
+  track_displacement(P, S, i, x.x, x.y, x.z);
+}
+
+cudaError_t launch_drift(const Launch& L, const DevParams& P, const DevState& S, double Ts,
+                         double Tau, double Ttar, int side_thermo) {
+  k_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ts, Tau, Ttar, side_thermo);
+  return cudaGetLastError();
+}
+
+// ---- frzsptrdatms: park sputtered atoms in the vacuum bands ----------------
+__global__ void __launch_bounds__(256) k_park(DevParams P, DevState S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.N) return;
+  double4_32a x = S.pos[i];
+  const double z = x.z;
+  bool hit = false, moved = false;
+  if ((z > P.park_o[0]) && (z < P.park_o[1])) {
+    x.z = P.park_a[0];
+    hit = moved = true;
+  } else if ((z > P.park_o[2]) && (z < P.park_o[3])) {
+    x.z = P.park_a[1];
+    hit = moved = true;
+  } else if ((z > P.park_al[0]) && (z < P.park_ah[0])) {
+    hit = true;
+  } else if ((z > P.park_al[1]) && (z < P.park_ah[1])) {
+    hit = true;
+  } else if ((z > P.park_il) && (z < P.park_ih)) {
+    hit = true;
+  }
+  if (!hit) return;
+  S.vel[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+  S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+  if (moved) {
+    S.pos[i] = x;
+    store_posq(P, S, i, x.x, x.y, x.z, S.flags[i]);
+    track_displacement(P, S, i, x.x, x.y, x.z);
+  }
+}
+
+cudaError_t launch_park(const Launch& L, const DevParams& P, const DevState& S) {
+  k_park<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// ---- kick: V += (F + Fp) Ts / (2m) -----------------------------------------
+__global__ void __launch_bounds__(256) k_kick(DevParams P, DevState S, double Ts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.N) return;
+  double4_32a v = S.vel[i];
+  const double4_32a f = S.frc[i];
+  const double4_32a g = S.frc_new[i];
+  const double m = S.mass[i];
+  v.x = v.x + 0.5 * (f.x + g.x) * Ts / m;
+  v.y = v.y + 0.5 * (f.y + g.y) * Ts / m;
+  v.z = v.z + 0.5 * (f.z + g.z) * Ts / m;
+  S.vel[i] = v;
+}
+
+cudaError_t launch_kick(const Launch& L, const DevParams& P, const DevState& S, double Ts) {
+  k_kick<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ts);
+  return cudaGetLastError();
+}
+
+// ---- calc_atm: max over atoms of 0.5 m |v|^2 / ec --------------------------
+__global__ void __launch_bounds__(kRedThreads) k_ke_max(DevParams P, DevState S) {
+  double v[1] = {-1.0e300};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    const double4_32a u = S.vel[i];
+    double ss = 0.0;
+    ss += u.x * u.x;
+    ss += u.y * u.y;
+    ss += u.z * u.z;
+    v[0] = fmax(v[0], 0.5 * S.mass[i] * ss / P.ec);
+  }
+  v[0] = block_max(v[0]);
+  if (grid_finish<1, true>(v, S.partials, &S.sc->ticket[3])) S.sc->ke_max = v[0];
+}
+
+cudaError_t launch_ke_max(const Launch& L, const DevParams& P, const DevState& S) {
+  k_ke_max<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// Re-evaluates every atom's displacement since the last list build after the
+// host replaced positions (upload, set_atom), so stale-list terms stay
+// covered.
+__global__ void k_track_all(DevParams P, DevState S) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P.N) return;
+  const double4_32a x = S.pos[i];
+  track_displacement(P, S, i, x.x, x.y, x.z);
+}
+
+cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S) {
+  k_track_all<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// ---- layout conversion: (N,3) column-major <-> double4_32a ---------------------
+__global__ void k_pack(int N, double4_32a* dst, const double* src) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  dst[i] = make_double4_32a(src[i], src[(size_t)N + i], src[2 * (size_t)N + i], 0.0);
+}
+
+__global__ void k_unpack(int N, const double4_32a* src, double* dst) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double4_32a v = src[i];
+  dst[i] = v.x;
+  dst[(size_t)N + i] = v.y;
+  dst[2 * (size_t)N + i] = v.z;
+}
+
+cudaError_t launch_pack(const Launch& L, int N, double4_32a* dst, const double* src_cm) {
+  k_pack<<<(N + 255) / 256, 256, 0, L.stream>>>(N, dst, src_cm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_unpack(const Launch& L, int N, const double4_32a* src, double* dst_cm) {
+  k_unpack<<<(N + 255) / 256, 256, 0, L.stream>>>(N, src, dst_cm);
+  return cudaGetLastError();
+}
+
+// ---- total energies ---------------------------------------------------------
+__global__ void __launch_bounds__(kRedThreads) k_energy_sum(DevParams P, DevState S) {
+  double v[2] = {0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    if (S.flags[i] & FL_REMOVED) continue;
+    const double4_32a u = S.vel[i];
+    v[0] += 0.5 * S.mass[i] * (u.x * u.x + u.y * u.y + u.z * u.z);
+    v[1] += S.epot[i];
+  }
+  block_sum<2>(v);
+  if (grid_finish<2, false>(v, S.partials, &S.sc->ticket[4])) {
+    S.sc->ekin = v[0];
+    S.sc->epot = v[1];
+  }
+}
+
+cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevState& S) {
+  k_energy_sum<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S);
+  return cudaGetLastError();
+}
+
+// ---- spec mode ----------------------------------------------------------------
+// Drift with the variable step held on the device, Berendsen scaling of the
+// tagged thermostat layer, fixed-layer pinning, removal of atoms above
+// remove_z, and the rebuild trigger at half the list skin.
+__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, double Ttar) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double dt = ((volatile DevScalars*)S.sc)->dt;
+  bool trig = false;
+  if (i < P.N) {
+    uint32_t fl = S.flags[i];
+    if (!(fl & FL_REMOVED)) {
+      double4_32a x = S.pos[i];
+      double4_32a v = S.vel[i];
+      if (fl & FL_THERMO) {
+        const double cnt = S.sc->thermo_cnt;
+        const double T = cnt > 0.0 ? S.sc->thermo_sum / 3. / cnt / P.kB : 0.0;
+        if (T > 0.0) {
+          const double s = sqrt(1. + dt / P.tau_spec * (Ttar / T - 1.));
+          v.x *= s;
+          v.y *= s;
+          v.z *= s;
+        }
+      }
+      const double4_32a f = S.frc[i];
+      const double m = S.mass[i];
+      x.x = x.x + v.x * dt + 0.5 * f.x * dt * dt / m;
+      x.y = x.y + v.y * dt + 0.5 * f.y * dt * dt / m;
+      x.z = x.z + v.z * dt + 0.5 * f.z * dt * dt / m;
+      if (fl & FL_FROZEN) {
+        const double4_32a xi = S.xi[i];
+        x.x = xi.x;
+        x.y = xi.y;
+        x.z = xi.z;
+        v.x = v.y = v.z = 0.0;
+      }
+      x.x = fmod(x.x + 2. * P.Lb[0], P.Lb[0]);
+      x.y = fmod(x.y + 2. * P.Lb[1], P.Lb[1]);
+      x.z = fmod(x.z + 2. * P.Lb[2], P.Lb[2]);
+      if (P.remove_z > 0.0 && x.z > P.remove_z && S.atype[i] < 3) {
+        fl |= FL_REMOVED;
+        S.flags[i] = fl;
+        v.x = v.y = v.z = 0.0;
+        trig = true;
+        atomicAdd(&S.sc->removed_count, 1);
+      }
+      S.pos[i] = x;
+      S.vel[i] = v;
+      store_posq(P, S, i, x.x, x.y, x.z, fl);
+      if (track_displacement(P, S, i, x.x, x.y, x.z) >= P.disp_fast2) trig = true;
+    }
+  }
+  if (__syncthreads_or(trig) && threadIdx.x == 0) S.sc->need_rebuild = 1;
+}
+
+cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
+                              double Ttar) {
+  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ttar);
+  return cudaGetLastError();
+}
+
+// Kick (apply != 0) followed by the reductions the next step needs: the
+// largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
+// thermostat layer's sum m v^2 and count. The last block also advances the
+// device time by the step just taken and installs the next dt.
+__global__ void __launch_bounds__(kRedThreads) k_spec_kick(DevParams P, DevState S, int apply) {
+  const double dt = ((volatile DevScalars*)S.sc)->dt;
+  double sums[2] = {0.0, 0.0};
+  double vmax2[1] = {0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+    const uint32_t fl = S.flags[i];
+    if (fl & FL_REMOVED) continue;
+    double4_32a v = S.vel[i];
+    if (apply) {
+      const double4_32a f = S.frc[i];
+      const double4_32a g = S.frc_new[i];
+      const double m = S.mass[i];
+      v.x = v.x + 0.5 * (f.x + g.x) * dt / m;
+      v.y = v.y + 0.5 * (f.y + g.y) * dt / m;
+      v.z = v.z + 0.5 * (f.z + g.z) * dt / m;
+      S.vel[i] = v;
+    }
+    const double v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+    vmax2[0] = fmax(vmax2[0], v2);
+    if ((fl & FL_THERMO) && S.atype[i] < 3) {
+      sums[0] += S.mass[i] * v2;
+      sums[1] += 1.0;
+    }
+  }
+  vmax2[0] = block_max(vmax2[0]);
+  block_sum<2>(sums);
+  double all[3] = {sums[0], sums[1], vmax2[0]};
+  // grid_finish sums; the max travels separately through its own partials
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    S.partials[0 * kMaxRedBlocks + blockIdx.x] = all[0];
+    S.partials[1 * kMaxRedBlocks + blockIdx.x] = all[1];
+    S.partials[2 * kMaxRedBlocks + blockIdx.x] = all[2];
+    __threadfence();
+    last = atomicAdd(&S.sc->ticket[5], 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  double acc[2] = {0.0, 0.0};
+  double mx = 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
+    acc[0] += ((volatile double*)S.partials)[b];
+    acc[1] += ((volatile double*)S.partials)[kMaxRedBlocks + b];
+    mx = fmax(mx, ((volatile double*)S.partials)[2 * kMaxRedBlocks + b]);
+  }
+  block_sum<2>(acc);
+  mx = block_max(mx);
+  if (threadIdx.x == 0) {
+    S.sc->thermo_sum = acc[0];
+    S.sc->thermo_cnt = acc[1];
+    S.sc->vmax2 = mx;
+    if (apply) S.sc->time += dt;
+    const double vm = sqrt(mx);
+    double nd = P.dt_max;
+    if (vm > 0.0 && P.dx_max / vm < nd) nd = P.dx_max / vm;
+    S.sc->dt = nd;
+    S.sc->ticket[5] = 0u;
+  }
+}
+
+cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
+                             double Ttar, int apply) {
+  (void)Ttar;
+  k_spec_kick<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S, apply);
+  return cudaGetLastError();
+}
+
+}  // namespace fibmd

@@ -1,0 +1,305 @@
+// fibmd_internal.cuh — device-side data layout and helpers shared by the
+// kernels of the FIB_MD GB300 backend.
+//
+// HBM layout (one context, N atoms, 0-based index = Fortran index - 1):
+//   pos, vel, frc, frc_new, xi, pos_build : double4_32a[N]  (x, y, z, unused)
+//   posq      : int4[N]   fixed-point positions, x = round(x/Lb * 2^32) mod
+//               2^32, w = atype | flags << 8. Differences of two fixed-point
+//               coordinates wrap modulo 2^32, which is the minimum image, and
+//               convert to binary32 with the precision of the separation
+//               itself (not of the absolute coordinate).
+//   mass      : double[N];  atype : int8[N];  flags : uint32[N]
+//   cells     : cell_start[ncell+1], cell_atoms[N] (counting sort by cell)
+//   nbr_sw    : int[max_sw * N], slot-major (nbr_sw[k*N + i]) so a warp of
+//               consecutive centres reads one coalesced row per slot
+//   mol_pairs : int2[cap] full Moliere pair list (both orders)
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/fibmd_gpu.h"
+
+namespace fibmd {
+
+constexpr int kMaxLegs = 8;        // active 3-body legs held per centre
+constexpr int kRedThreads = 256;   // threads of reduction kernels
+constexpr int kMaxRedBlocks = 4096;
+
+enum : uint32_t {
+  FL_FROZEN = 1u,   // xsides > 0 (ref) / FIBMD_TAG_FROZEN (spec)
+  FL_THERMO = 2u,   // spec-mode thermostat layer
+  FL_REMOVED = 4u,  // spec-mode sputtered and removed
+};
+
+// Derived constants handed to every kernel by value.
+struct DevParams {
+  int N, Nsg, nfired;  // atoms with index >= nfired are unfired ions
+  int mode, precision;
+  int max_sw;
+  int mol_cap;
+  int Ntable, tab_last;  // tab_last: last 0-based index with a non-zero entry
+  int nc[3];
+  int ncell;
+  double Lb[3], iLb[3], hcell[3];
+  double qscale[3];      // 2^32 / Lb
+  float qinvA[3];        // Lb / 2^32 in Angstrom
+  double rv2, rv2lj, rlj2;
+  float pre_sw2A, pre_mol2A;   // binary32 prefilter radii^2 (A^2), widened
+  float acc_sw2A, acc_mol2A;   // binary32 accept radii^2 (A^2), narrowed
+  float pre3A2;                // prefilter for active SW legs (A^2)
+  // Stillinger-Weber (types 1, 2 -> index 0, 1)
+  double al, gam, cut3, thrd, A, B, psi, qsi;
+  double eps[2][2], isig[2][2], leps[2][2][2], epssig[2][2];
+  // Moliere (types 1..3 -> index 0..2)
+  double Zmol[3], aamol[3][3], ie0, ec;
+  double Amol, Bmol, Cmol, amol, bmol, gmol;
+  // 2-body table
+  double umax;
+  // stale-list bookkeeping
+  double disp_fast2;  // squared displacement (m^2) that marks an atom fast
+  // mixed precision, reduced units (A, eV)
+  float epsA[2][2], sigA[2][2], lepsA[2][2][2];
+  float molKA[3][3];       // ie0*Zi*Zj*ec*ec in eV*A
+  float amolA[3][3];       // screening length in A
+  double f_evA_to_N;       // eV/A -> N
+  double e_eV_to_J;        // eV -> J
+  float mol_fp64_rA;       // Moliere pairs below this stay binary64 (A)
+  // integrator geometry (siga.in values resolved once per context)
+  double kB;
+  double side_sw, side_zlo, side_zhi;        // controlsidetemp band (m)
+  double park_o[4], park_a[2];               // outz(k)*Lb3/10, atomz(k)*Lb3/10
+  double park_al[2], park_ah[2];             // (atomz(k) -/+ 0.3)*Lb3/10
+  double park_il, park_ih;                   // (ionz -/+ 0.3)*Lb3/10
+  // spec mode
+  double remove_z, dt_max, dx_max, tau_spec;
+};
+
+// Device scalars written by reductions and read by later kernels or the
+// host (through a pinned mirror).
+struct DevScalars {
+  double side_sum;     // controlsidetemp: sum m v^2 over edge atoms
+  double side_cnt;     //                  number of edge atoms
+  double temp;         // temperature() of the current velocities
+  double ke_max;       // calc_atm: max 0.5 m v^2 / ec
+  double vmax2;        // spec: max |v|^2
+  double dt;           // spec: current step
+  double dt_next;      // spec: step chosen from this step's velocities
+  double thermo_sum, thermo_cnt;  // spec thermostat layer
+  double ekin, epot;   // energies (J)
+  double time;         // spec: simulated time
+  double disp_max2;    // spec: max squared displacement since build
+  int fast_count;
+  int mol_count;
+  int heavy_count;
+  int overflow_sw;
+  int overflow_mol;
+  int table_err;
+  int cell_oob;
+  int nan_flag;
+  int need_rebuild;
+  int removed_count;
+  unsigned int ticket[8];
+  unsigned long long counters[4];
+};
+
+struct DevState {
+  int N;
+  double4_32a* pos;
+  double4_32a* vel;
+  double4_32a* frc;      // F (previous step)
+  double4_32a* frc_new;  // Fp (this step)
+  double4_32a* xi;
+  double4_32a* pos_build;
+  int4* posq;
+  double* mass;
+  int8_t* atype;
+  uint32_t* flags;
+  // cells
+  int* cell_count;
+  int* cell_start;
+  int* cell_atoms;
+  int* atom_cell;
+  int* scan_blocks;
+  // lists
+  int* nbr_sw;
+  int* n_sw;
+  int2* mol_pairs;
+  // stale-list and heavy-centre work lists
+  uint8_t* fast_flag;
+  int* fast_list;
+  int* heavy_list;
+  // 2-body table
+  const double* tab;
+  const double* tabu;
+  // energy
+  double* epot;
+  // reductions
+  double* partials;
+  DevScalars* sc;
+};
+
+// ---- small device helpers ------------------------------------------------
+
+__device__ __forceinline__ int type_index(int8_t t) { return t - 1; }
+
+// The reference's minimum image, X(i)-X(j) - NINT((X(i)-X(j))*iLb)*Lb,
+// with each operation rounded separately (no FMA), so neighbour decisions
+// reproduce binary64 host arithmetic bit for bit.
+__device__ __forceinline__ double min_image_exact(double xi, double xj,
+                                                  double iLb, double Lb) {
+  double d = __dsub_rn(xi, xj);
+  double n = round(__dmul_rn(d, iLb));
+  return __dsub_rn(d, __dmul_rn(n, Lb));
+}
+
+// Same separation for force arithmetic (contraction allowed).
+__device__ __forceinline__ double min_image(double xi, double xj, double iLb,
+                                            double Lb) {
+  double d = xi - xj;
+  return d - round(d * iLb) * Lb;
+}
+
+__device__ __forceinline__ unsigned int fixq(double x, double qscale) {
+  return (unsigned int)(long long)__double2ll_rn(x * qscale);
+}
+
+// binary32 separation (Angstrom) of two fixed-point positions.
+__device__ __forceinline__ float3 qsep(const int4& a, const int4& b,
+                                       const float qinvA[3]) {
+  float3 d;
+  d.x = (float)(int)((unsigned)a.x - (unsigned)b.x) * qinvA[0];
+  d.y = (float)(int)((unsigned)a.y - (unsigned)b.y) * qinvA[1];
+  d.z = (float)(int)((unsigned)a.z - (unsigned)b.z) * qinvA[2];
+  return d;
+}
+
+__device__ __forceinline__ void atomic_add3(double4_32a* f, int i, double x,
+                                            double y, double z) {
+  atomicAdd(&f[i].x, x);
+  atomicAdd(&f[i].y, y);
+  atomicAdd(&f[i].z, z);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide sum of n doubles per thread (kRedThreads threads). Result valid
+// in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV]) {
+  __shared__ double sh[NV][kRedThreads / 32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = warp_sum(v[q]);
+  if (lane == 0)
+#pragma unroll
+    for (int q = 0; q < NV; q++) sh[q][w] = v[q];
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      double t = lane < (kRedThreads / 32) ? sh[q][lane] : 0.0;
+      v[q] = warp_sum(t);
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ double block_max(double v) {
+  __shared__ double sh[kRedThreads / 32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_max(v);
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    double t = lane < (kRedThreads / 32) ? sh[lane] : -1.0e300;
+    v = warp_max(t);
+  }
+  __syncthreads();
+  return v;
+}
+
+// Deterministic grid reduction: every block stores its partial(s); the last
+// block to finish (ticket) sums them in block order. Returns true in thread 0
+// of the last block, with the totals in out[].
+template <int NV, bool MAXOP>
+__device__ __forceinline__ bool grid_finish(double (&v)[NV], double* partials,
+                                            unsigned int* ticket) {
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) partials[q * kMaxRedBlocks + blockIdx.x] = v[q];
+    __threadfence();
+    unsigned int t = atomicAdd(ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  double acc[NV];
+#pragma unroll
+  for (int q = 0; q < NV; q++) acc[q] = MAXOP ? -1.0e300 : 0.0;
+  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      double x = ((volatile double*)partials)[q * kMaxRedBlocks + b];
+      acc[q] = MAXOP ? fmax(acc[q], x) : acc[q] + x;
+    }
+  if (MAXOP) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) acc[q] = block_max(acc[q]);
+  } else {
+    block_sum<NV>(acc);
+  }
+#pragma unroll
+  for (int q = 0; q < NV; q++) v[q] = acc[q];
+  if (threadIdx.x == 0) *ticket = 0u;
+  return threadIdx.x == 0;
+}
+
+// ---- launchers (defined in the .cu files) --------------------------------
+struct Launch {
+  cudaStream_t stream;
+  int sms;
+};
+
+// fibmd_nlist.cu
+cudaError_t launch_update_posq(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevState& S,
+                               int rebuild_from_flag);
+cudaError_t launch_count_triplets(const Launch& L, const DevParams& P, const DevState& S,
+                                  unsigned long long* d_count, int3* out, long long cap);
+// fibmd_force.cu
+cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
+                         bool energy, bool count);
+// fibmd_integrate.cu
+cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_adjust_and_temp(const Launch& L, const DevParams& P, const DevState& S,
+                                   double Ts, double Tau, double Ttar);
+cudaError_t launch_drift(const Launch& L, const DevParams& P, const DevState& S, double Ts,
+                         double Tau, double Ttar, int side_thermo);
+cudaError_t launch_park(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_kick(const Launch& L, const DevParams& P, const DevState& S, double Ts);
+cudaError_t launch_temperature(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_ke_max(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_pack(const Launch& L, int N, double4_32a* dst, const double* src_cm);
+cudaError_t launch_unpack(const Launch& L, int N, const double4_32a* src, double* dst_cm);
+cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
+                              double Ttar);
+cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
+                             double Ttar, int apply);
+
+}  // namespace fibmd

@@ -1,0 +1,288 @@
+"""Python host interface of the GB300 backend for FIB_MD's per-step hot path.
+
+Method names follow the reference routines the calls replace (si_nlist,
+si_force, si_potential, temperature, ionrun, knock, onestep/TI); arrays are
+numpy arrays shaped (Natm, 3) like the Fortran X(Natm,3) and are passed to
+the library in Fortran (column-major) order. Every call goes to
+libfibmd_gpu.so; errors raise FibmdError with the library's message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi
+from ._abi import Params, Rng, Siga
+
+
+class FibmdError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_abi.STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _fortran(a, dtype=np.float64) -> np.ndarray:
+    return np.asfortranarray(np.asarray(a, dtype=dtype))
+
+
+def params_default() -> Params:
+    """prms.f90's constants and the reference's shipped siga.in."""
+    p = Params()
+    _abi.load().fibmd_gpu_params_default(C.byref(p))
+    return p
+
+
+def read_siga(path: str, p: Params | None = None) -> tuple[Params, Siga]:
+    """Read siga.in's 45 values (prms.f90:221-275) into a Params/Siga pair."""
+    lib = _abi.load()
+    p = params_default() if p is None else p.copy()
+    s = Siga()
+    msg = C.create_string_buffer(512)
+    rc = lib.fibmd_host_read_siga(str(path).encode(), C.byref(p), C.byref(s), msg, 512)
+    if rc:
+        raise FibmdError(rc, msg.value.decode())
+    return p, s
+
+
+class Ran1:
+    """ran1 (src/ran1.f). A seed <= 0 initialises the shuffle table."""
+
+    def __init__(self, seed: int):
+        self.state = Rng()
+        _abi.load().fibmd_host_rng_seed(C.byref(self.state), int(seed))
+
+    def __call__(self) -> float:
+        return _abi.load().fibmd_host_ran1(C.byref(self.state))
+
+
+def pureepi(nc1: int, nc2: int, nc3: int):
+    """Diamond-cubic slab (prms.f90:484-557): (XX, xsides, Lb)."""
+    n = 8 * nc1 * nc2 * nc3
+    XX = np.zeros((n, 3), dtype=np.float64, order="F")
+    xs = np.zeros(n, dtype=np.int32)
+    Lb = np.zeros(3)
+    _abi.load().fibmd_host_pureepi(nc1, nc2, nc3, _dp(XX), _ip(xs), _dp(Lb))
+    return XX, xs, Lb
+
+
+@dataclass
+class System:
+    """Initial state of a reference run, as ic case 4 prepares it."""
+
+    params: Params
+    X: np.ndarray
+    Xi: np.ndarray
+    V: np.ndarray
+    mass: np.ndarray
+    atype: np.ndarray
+    xsides: np.ndarray
+    Xrand: np.ndarray
+    rng: Ran1
+
+
+def crystal_system(nc=(8, 8, 8), nlj: int = 1, seed: int = -1001, params: Params | None = None,
+                   nrand: int = 10000, fwhm: float = 2.0, Uo: float = 150.0) -> System:
+    """readprms/pureepi, initran, initdata (src/main.f90:31-43) for a
+    crystalline target with an explicit ran1 seed (the reference seeds from
+    the wall clock, prms.f90:220,296)."""
+    lib = _abi.load()
+    p = params_default() if params is None else params.copy()
+    XX, xs, Lb = pureepi(*nc)
+    nsg = XX.shape[0]
+    p.Nsg, p.Nlj, p.Natm = nsg, nlj, nsg + nlj
+    for d in range(3):
+        p.Lb[d] = Lb[d]
+    rng = Ran1(seed)
+    Xrand = np.zeros((nrand, 2), dtype=np.float64, order="F")
+    lib.fibmd_host_initranions(C.byref(rng.state), nrand, fwhm, _dp(Xrand))
+    N = p.Natm
+    X = np.zeros((N, 3), order="F")
+    X[:nsg] = XX
+    Xi = np.zeros((N, 3), order="F")
+    V = np.zeros((N, 3), order="F")
+    mass = np.zeros(N)
+    atype = np.zeros(N, dtype=np.int32)
+    rc = lib.fibmd_host_init_state(C.byref(p), C.byref(rng.state), Uo, _dp(X), _dp(Xi), _dp(V),
+                                   _dp(mass), _ip(atype))
+    if rc:
+        raise FibmdError(rc, "init_state")
+    xsides = np.zeros(N, dtype=np.int32)
+    xsides[:nsg] = xs
+    return System(p, X, Xi, V, mass, atype, xsides, Xrand, rng)
+
+
+def knock(p: Params, rng: Ran1, knc: int, eV: float, phiz: float, phixy: float,
+          Xrand: np.ndarray):
+    """knock (src/knock.f90:21-55): (1-based ion index, x[3], v[3])."""
+    x = np.zeros(3)
+    v = np.zeros(3)
+    Xr = _fortran(Xrand)
+    i = _abi.load().fibmd_host_knock(C.byref(p), C.byref(rng.state), knc, eV, phiz, phixy,
+                                     _dp(Xr), Xr.shape[0], _dp(x), _dp(v))
+    return i, x, v
+
+
+class FibMD:
+    """One device context (libfibmd_gpu's fibmd_ctx)."""
+
+    def __init__(self, params: Params):
+        self.lib = _abi.load()
+        self.params = params.copy()
+        self.N = params.Natm
+        h = C.c_void_p()
+        rc = self.lib.fibmd_gpu_create(C.byref(self.params), C.byref(h))
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.lib.fibmd_gpu_last_error(None, buf, 512)
+            raise FibmdError(rc, buf.value.decode())
+        self.h = h
+
+    # ---- helpers
+    def _check(self, rc: int, what: str):
+        if rc:
+            buf = C.create_string_buffer(1024)
+            self.lib.fibmd_gpu_last_error(self.h, buf, 1024)
+            raise FibmdError(rc, f"{what}: {buf.value.decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fibmd_gpu_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- state
+    def upload(self, X, V, F, Xi, mass, atype, xsides):
+        X, V, Xi = _fortran(X), _fortran(V), _fortran(Xi)
+        Fa = None if F is None else _fortran(F)
+        mass = np.ascontiguousarray(mass, dtype=np.float64)
+        atype = np.ascontiguousarray(atype, dtype=np.int32)
+        xsides = np.ascontiguousarray(xsides, dtype=np.int32)
+        self._check(self.lib.fibmd_gpu_upload(self.h, _dp(X), _dp(V),
+                                              None if Fa is None else _dp(Fa), _dp(Xi),
+                                              _dp(mass), _ip(atype), _ip(xsides)), "upload")
+
+    def upload_system(self, s: System, F=None):
+        self.upload(s.X, s.V, F, s.Xi, s.mass, s.atype, s.xsides)
+
+    def download(self):
+        X = np.zeros((self.N, 3), order="F")
+        V = np.zeros((self.N, 3), order="F")
+        F = np.zeros((self.N, 3), order="F")
+        self._check(self.lib.fibmd_gpu_download(self.h, _dp(X), _dp(V), _dp(F)), "download")
+        return X, V, F
+
+    def set_tags(self, tags):
+        t = np.ascontiguousarray(tags, dtype=np.uint32)
+        self._check(self.lib.fibmd_gpu_set_tags(self.h, t.ctypes.data_as(C.POINTER(C.c_uint32))),
+                    "set_tags")
+
+    def set_atom(self, i: int, x, v):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        self._check(self.lib.fibmd_gpu_set_atom(self.h, int(i), _dp(x), _dp(v)), "set_atom")
+
+    def set_impact(self, impact: int):
+        self._check(self.lib.fibmd_gpu_set_impact(self.h, int(impact)), "set_impact")
+
+    def ionrun(self, tic: int):
+        self._check(self.lib.fibmd_gpu_ionrun(self.h, int(tic)), "ionrun")
+
+    def set_tau(self, tau: float):
+        self._check(self.lib.fibmd_gpu_set_tau(self.h, float(tau)), "set_tau")
+
+    # ---- si.f90
+    def si_nlist(self):
+        self._check(self.lib.fibmd_gpu_nlist(self.h), "si_nlist")
+
+    def list_counts(self):
+        a, b, c = C.c_longlong(), C.c_longlong(), C.c_longlong()
+        self._check(self.lib.fibmd_gpu_list_counts(self.h, C.byref(a), C.byref(b), C.byref(c)),
+                    "list_counts")
+        return a.value, b.value, c.value
+
+    def get_pairs(self, kind: int = 0) -> np.ndarray:
+        n = C.c_int()
+        self._check(self.lib.fibmd_gpu_get_pairs(self.h, kind, C.byref(n), None, 0), "get_pairs")
+        out = np.zeros((max(n.value, 1), 2), dtype=np.int32)
+        self._check(self.lib.fibmd_gpu_get_pairs(self.h, kind, C.byref(n), _ip(out), n.value),
+                    "get_pairs")
+        return out[: n.value]
+
+    def get_triplets(self) -> np.ndarray:
+        n = C.c_longlong()
+        self._check(self.lib.fibmd_gpu_get_triplets(self.h, C.byref(n), None, 0), "get_triplets")
+        out = np.zeros((max(n.value, 1), 3), dtype=np.int32)
+        self._check(self.lib.fibmd_gpu_get_triplets(self.h, C.byref(n), _ip(out), n.value),
+                    "get_triplets")
+        return out[: n.value]
+
+    def si_force(self) -> np.ndarray:
+        F = np.zeros((self.N, 3), order="F")
+        self._check(self.lib.fibmd_gpu_force(self.h, _dp(F), None, None), "si_force")
+        return F
+
+    def si_force_energy(self):
+        """Forces together with si_potential's per-atom and total energy."""
+        F = np.zeros((self.N, 3), order="F")
+        u = np.zeros(self.N)
+        U = C.c_double()
+        self._check(self.lib.fibmd_gpu_force(self.h, _dp(F), _dp(u), C.byref(U)), "si_force")
+        return F, u, U.value
+
+    def si_potential(self):
+        _, u, U = self.si_force_energy()
+        return U, u
+
+    def work_counters(self):
+        c = (C.c_longlong * 4)()
+        self._check(self.lib.fibmd_gpu_work_counters(self.h, c), "work_counters")
+        return list(c)
+
+    # ---- timeint.f90 / temp.f90
+    def steps(self, whichctrl: int, max_steps: int, lt: int, time: float, temp: float):
+        l = C.c_longlong(lt)
+        t = C.c_double(time)
+        T = C.c_double(temp)
+        why = C.c_int()
+        self._check(self.lib.fibmd_gpu_steps(self.h, whichctrl, max_steps, C.byref(l), C.byref(t),
+                                             C.byref(T), C.byref(why)), "steps")
+        return l.value, t.value, T.value, why.value
+
+    def temperature(self) -> float:
+        T = C.c_double()
+        self._check(self.lib.fibmd_gpu_temperature(self.h, C.byref(T)), "temperature")
+        return T.value
+
+    def regime(self):
+        Ts = C.c_double()
+        tic = C.c_int()
+        self._check(self.lib.fibmd_gpu_regime(self.h, C.byref(Ts), C.byref(tic)), "regime")
+        return Ts.value, tic.value
+
+    def timers(self, reset: bool = False):
+        v = [C.c_double() for _ in range(4)]
+        c = (C.c_longlong * 4)()
+        self._check(self.lib.fibmd_gpu_timers(self.h, *[C.byref(x) for x in v], c, int(reset)),
+                    "timers")
+        return [x.value for x in v], list(c)

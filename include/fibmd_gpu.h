@@ -1,0 +1,261 @@
+/*
+ * fibmd_gpu.h — C-ABI of the GB300 (sm_103a) backend for the FIB_MD per-step
+ * hot path: cell binning, Verlet-list build, the fused Stillinger-Weber 2/3-body
+ * + Moliere force, and the velocity-Verlet step with the Berendsen edge
+ * thermostat, side freezing, reboxing and sputter parking.
+ *
+ * The reference (nanoMFG/FIB_MD, Fortran 90 + MPI) has no plugin API: the hot
+ * path is a set of module subroutines called from `onestep`
+ * (src/timeint.f90:158-242). Each entry point below names the routine(s) it
+ * replaces. A Fortran host binds them with ISO_C_BINDING (see the binding
+ * module shown in INTEGRATION.md); the C++ host driver and the Python package
+ * `fib_md_gb300` bind the same symbols.
+ *
+ * Conventions (mirroring the reference's):
+ *   - Every real is IEEE binary64 (the reference builds with -fdefault-real-8,
+ *     src/Makefile:4). SI units: metres, seconds, kilograms, joules.
+ *   - Per-atom vectors are passed column-major as the Fortran arrays
+ *     X(Natm,3): all x, then all y, then all z (src/data.f90:19-24).
+ *   - Atom indices that cross the ABI are 1-based, as in Fortran.
+ *   - Every entry point returns an int status (FIBMD_OK == 0). No exception or
+ *     abort crosses the ABI; fibmd_gpu_last_error() gives the message.
+ *   - Ownership: the caller keeps its host arrays; the context owns all device
+ *     memory and copies on upload/download.
+ *   - Threading: one context per host thread; calls on one context are not
+ *     re-entrant. All work of a context is ordered on one CUDA stream.
+ */
+#ifndef FIBMD_GPU_H
+#define FIBMD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FIBMD_ABI_VERSION 1
+
+/* ---- status codes --------------------------------------------------------- */
+enum {
+  FIBMD_OK = 0,
+  FIBMD_EINVAL = 1,    /* bad argument / inconsistent parameters            */
+  FIBMD_ECUDA = 2,     /* a CUDA runtime call failed                          */
+  FIBMD_EOVERFLOW = 3, /* a neighbour-list capacity was exceeded (list kept
+                          truncated; the reference prints and continues,
+                          src/si.f90:264-272)                                 */
+  FIBMD_ENAN = 4,      /* non-finite position/velocity/force detected         */
+  FIBMD_ETIMEOUT = 5,  /* a bounded device wait gave up                       */
+  FIBMD_ESTATE = 6,    /* call order violated (e.g. steps before upload)      */
+  FIBMD_ENOMEM = 7,    /* device allocation failed                            */
+  FIBMD_ETABLE = 8     /* 2-body table index beyond Ntable (the reference
+                          prints "ERRRRRRROR" and uses 0, src/si.f90:562-564) */
+};
+
+/* ---- modes ------------------------------------------------------------------ */
+enum {
+  /* Exact reference semantics: two-level fixed time step switched by
+     calc_atm/ionrun, lists rebuilt every ntlist steps (stale lists kept),
+     lateral edge thermostat with the reference's predicate, sputter parking. */
+  FIBMD_MODE_REF = 0,
+  /* Specified physical set-up: variable dt = min(dt_max, dx_max/max|v|),
+     rebuild when the max displacement since the last build exceeds half the
+     skin, thermostat/fixed layers given as per-atom tags, removal of
+     sputtered atoms above a height. */
+  FIBMD_MODE_SPEC = 1
+};
+enum {
+  FIBMD_PREC_FP64 = 0,  /* all force arithmetic in binary64                   */
+  FIBMD_PREC_MIXED = 1  /* SW/Moliere arithmetic in binary32 (reduced units),
+                           binary64 accumulation, positions, velocities, VV,
+                           dt, and Moliere below mixed_mol_fp64_r           */
+};
+
+/* per-atom tag bits (fibmd_gpu_set_tags) */
+enum {
+  FIBMD_TAG_FROZEN = 1u,   /* pinned to Xi with V = 0 each step (spec mode's
+                              fixed bottom layers; ref mode uses xsides)      */
+  FIBMD_TAG_THERMO = 2u,   /* member of the Berendsen layer (spec mode)       */
+  FIBMD_TAG_REMOVED = 4u   /* sputtered and removed (spec mode); set by the
+                              device, excluded from lists, forces, dynamics   */
+};
+
+/* reasons a fibmd_gpu_steps() call returned (bit set) */
+enum {
+  FIBMD_STOP_MAXSTEPS = 1, /* ran the requested number of steps              */
+  FIBMD_STOP_DUMP = 2,     /* lt is an atm_out/res_out step: download + write */
+  FIBMD_STOP_DONE = 4,     /* the TI loop ended: warm-up converged
+                              (whichctrl 0) or time > impact*dti (1)          */
+  FIBMD_STOP_REGIME = 8    /* calc_atm switched to the slow regime (ionrun 2) */
+};
+
+/*
+ * Run parameters. fibmd_gpu_params_default() fills the potential constants
+ * hard-coded in src/prms.f90:172-216 and the siga.in defaults shipped with
+ * the reference (siga.in:1-53); the host overwrites what siga.in sets.
+ */
+typedef struct fibmd_params {
+  int abi_version;           /* must be FIBMD_ABI_VERSION                      */
+  int mode;                  /* FIBMD_MODE_*                                   */
+  int precision;             /* FIBMD_PREC_*                                   */
+  int Natm, Nsg, Nlj;        /* atoms; Si/Ge atoms (1..Nsg); ions (Nsg+1..)    */
+  double Lb[3];              /* periodic box (m); z is 10x the slab            */
+
+  /* Stillinger-Weber and Moliere constants (src/prms.f90:172-216, 433-480) */
+  double A, B, psi, qsi, al, gamma;
+  double lambdaSi, lambdaGe, epsSi, epsGe, sigmaSi, sigmaGe;
+  double massSi, massGe, massGa;
+  double ZSi, ZGe, ZGa;
+  double Amol, Bmol, Cmol, alpha_mol, beta_mol, gamma_mol;
+  double kB, eps0, ec, ao;
+  double listfac;            /* list radius factor (1.1)                      */
+  int Ntable;                /* 2-body table size (12000)                     */
+
+  /* run control read from siga.in (src/prms.f90:223-275) */
+  double Ts_i, Ts_r;         /* fast / slow regime time steps (s)             */
+  double Ttar1;              /* thermostat target (K)                         */
+  double ke_limit_1;         /* slow-regime switch threshold (eV)             */
+  double Tau_i, Tau_r;       /* Berendsen time constants (s)                  */
+  double Teps;               /* warm-up tolerance (K)                         */
+  int ntlist_i, ntlist_r, atlist_i, atlist_r, dslist_i, dslist_r;
+  int atm_out_i, atm_out_r, res_out;
+  double outz[4], atomz[2], ionz, knockz;  /* in units of Lb(3)/10            */
+  double sidewidth;          /* edge thermostat width (nm)                    */
+  double dti;                /* time between impacts (s)                      */
+
+  /* spec mode */
+  double dt_max;             /* variable-dt cap (s), default 1 fs             */
+  double dx_max;             /* max displacement per step (m), default 0.05 A */
+  double tau_spec;           /* Berendsen constant of the thermo layer (s)    */
+  double remove_z;           /* atoms above this z (m) are removed; <=0 off   */
+
+  /* mixed precision */
+  double mixed_mol_fp64_r;   /* Moliere pairs closer than this (m) stay fp64  */
+
+  /* capacities; 0 = defaults */
+  int max_sw_nbrs;           /* SW list slots per atom, default 48            */
+  int max_mol_pairs;         /* full Moliere list entries, default
+                                max(1500*Nlj, 65536) (the reference's MLlj is
+                                1500*Nlj, src/si.f90:51)                      */
+  int reserved[8];
+} fibmd_params;
+
+typedef struct fibmd_ctx fibmd_ctx;
+
+/* Fill prms.f90's constants and siga.in's shipped defaults. */
+int fibmd_gpu_params_default(fibmd_params* p);
+
+/* Library / device information. Returns the ABI version. */
+int fibmd_gpu_abi_version(void);
+/* sizeof(fibmd_params) as compiled into the library, for FFI layout checks. */
+int fibmd_gpu_params_size(void);
+
+/* Create a context on the current CUDA device: sizes the cell grid and the
+   list capacities (replaces init_nlist, src/si.f90:48-80) and builds the
+   2-body table bit-identically to mktables (src/si.f90:575-597). */
+int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out);
+void fibmd_gpu_destroy(fibmd_ctx* ctx);
+
+/* Last error message of this context (or of the last failed create when ctx
+   is NULL). Copies at most len-1 bytes plus NUL. */
+int fibmd_gpu_last_error(const fibmd_ctx* ctx, char* buf, int len);
+
+/* Upload the full atom state (replaces the host arrays of src/data.f90:19-24
+   and src/prms.f90:43). X, V, F, Xi: (Natm,3) column-major; mass: (Natm);
+   atype: (Natm) 1=Si 2=Ge 3=Ga; xsides: (Natm), >0 marks an atom pinned by
+   freezsidesN (src/tools.f90:38-51). F may be NULL (zeros). */
+int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V,
+                     const double* F, const double* Xi, const double* mass,
+                     const int* atype, const int* xsides);
+
+/* Download the atom state (what updateroot gathers, src/par.f90:94-121).
+   Any pointer may be NULL. */
+int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F);
+
+/* Spec-mode per-atom tags (FIBMD_TAG_* bits), (Natm) entries. */
+int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags);
+
+/* Overwrite one atom's position and velocity (1-based index). This is the
+   device side of knock (src/knock.f90:21-55): the host draws the ion's start
+   point and velocity and sends them here. */
+int fibmd_gpu_set_atom(fibmd_ctx* ctx, int i, const double x[3],
+                       const double v[3]);
+
+/* Set the impact counter (module variable `impact`, src/prms.f90:24): atoms
+   with index > Nsg+impact are unfired ions and are skipped by the force
+   (src/si.f90:415,428,457). */
+int fibmd_gpu_set_impact(fibmd_ctx* ctx, int impact);
+
+/* Switch regime (ionrun, src/prms.f90:563-584): tic 1 = fast (Ts_i,
+   ntlist_i, atlist_i, Tau_i, dslist_i, atm_out_i), tic 2 = slow. Also sets
+   the calc_atm latch atom_is_fast = (tic == 1). */
+int fibmd_gpu_ionrun(fibmd_ctx* ctx, int tic);
+
+/* Override the Berendsen constant Tau (tint sets Tau = 1e-14 s for the
+   warm-up, src/timeint.f90:85-88). */
+int fibmd_gpu_set_tau(fibmd_ctx* ctx, double tau);
+
+/* Build the neighbour lists at the current device positions (replaces
+   si_nlist -> si_nlistG + chainlist, src/si.f90:87-276, src/nlist.f90:20-66). */
+int fibmd_gpu_nlist(fibmd_ctx* ctx);
+
+/* Number of list entries: full SW pairs, full Moliere pairs, and the
+   connected SW triplets the reference would store in nlist3. Any pointer
+   may be NULL. */
+int fibmd_gpu_list_counts(fibmd_ctx* ctx, long long* n_sw_full,
+                          long long* n_mol_full, long long* n_triplets);
+
+/* Export the half lists the reference keeps after dropping j<i entries
+   (src/si.f90:234-260) as sorted 1-based (i,j) pairs, i<j. kind 0 = SW list
+   (nlist2), 1 = Moliere list (nlistlj). ij has room for 2*cap ints; *n
+   receives the pair count (which may exceed cap: nothing past cap is
+   written). */
+int fibmd_gpu_get_pairs(fibmd_ctx* ctx, int kind, int* n, int* ij, int cap);
+
+/* Export the connected-triplet set of the SW list graph, each triple sorted
+   (min,mid,max) and 1-based, in lexicographic order: the set si_nlistG
+   stores in nlist3 (src/si.f90:191-232). ijk has room for 3*cap ints. */
+int fibmd_gpu_get_triplets(fibmd_ctx* ctx, long long* n, int* ijk,
+                           long long cap);
+
+/* Force at the current device positions with the current lists; the result
+   becomes the state's F (tint's `call si_force(X,F,lt)`,
+   src/timeint.f90:69). F_out (Natm,3) may be NULL. If u_out or Utot is
+   non-NULL the per-atom and total potential energy of si_potential
+   (src/si.f90:278-380) are computed too. */
+int fibmd_gpu_force(fibmd_ctx* ctx, double* F_out, double* u_out,
+                    double* Utot);
+
+/* Run the TI loop (src/timeint.f90:123-155) over onestep
+   (src/timeint.f90:158-242) on the device for at most max_steps steps.
+   whichctrl: 0 warm-up (global Berendsen until |T-Ttar| <= Teps),
+   1 impact (until time > impact*dti), 2 free run (max_steps steps).
+   lt, time, temp are the caller's loop variables (in/out). Returns early at
+   an atm_out/res_out dump step (whichctrl > 0). *reason receives
+   FIBMD_STOP_* bits. */
+int fibmd_gpu_steps(fibmd_ctx* ctx, int whichctrl, long long max_steps,
+                    long long* lt, double* time, double* temp, int* reason);
+
+/* temperature (src/temp.f90:183-205) of the device velocities. */
+int fibmd_gpu_temperature(fibmd_ctx* ctx, double* T);
+
+/* Current time step Ts (s) and regime (1 fast, 2 slow). */
+int fibmd_gpu_regime(fibmd_ctx* ctx, double* Ts, int* tic);
+
+/* Phase timers since the last reset, in seconds, and call counts, as the
+   reference's calc_time report (src/timeint.f90:302-331): at = parking and
+   redistribution, nt = neighbour lists, ds = calc_atm, f = force. */
+int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds,
+                     double* f, long long* counts4, int reset);
+
+/* Counters of the last force evaluation: active SW pairs (i<j with a
+   non-zero table entry), non-zero 3-body angle terms, Moliere pairs
+   evaluated, and stale-list angle terms added by the correction pass. */
+int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[4]);
+
+/* CUDA stream the context orders its work on (cudaStream_t as void*). */
+void* fibmd_gpu_stream(fibmd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FIBMD_GPU_H */

@@ -1,0 +1,150 @@
+/*
+ * fibmd_oracle.h — CPU oracle for the FIB_MD hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This is a plain-C, binary64 restatement of the
+ * reference's Fortran routines on the per-step path (nanoMFG/FIB_MD,
+ * src/si.f90, src/nlist.f90, src/timeint.f90, src/temp.f90, src/tools.f90,
+ * src/prms.f90, src/data.f90, src/knock.f90, src/ran1.f). Only the tests,
+ * __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it, and
+ * only as the checker or the timed CPU baseline; the GPU library never links
+ * or calls it.
+ *
+ * Parity status: the reference is Fortran and no Fortran compiler exists
+ * where this is built, and the reference ships no tests, fixtures or golden
+ * vectors. Parity with the reference's own outputs is therefore UNPINNED;
+ * the restatement is pinned instead by known answers that follow from the
+ * reference's formulas (perfect-diamond energy -2*eps per atom, Newton's
+ * third law, F = -dU/dX of si_potential for the 3-body and Moliere terms,
+ * the published Park-Miller/Bays-Durham sequence of ran1).
+ *
+ * Semantics: Fortran 1-based indexing is kept (atom ids in the lists are
+ * 1-based), arrays are column-major (Natm,3), and each expression keeps the
+ * reference's left-to-right evaluation order. Build with -ffp-contract=off
+ * and without fast-math so no FMA contraction changes the rounding.
+ */
+#ifndef FIBMD_ORACLE_H
+#define FIBMD_ORACLE_H
+
+#include "../include/fibmd_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_sys {
+  fibmd_params p;
+  int Natm, Nsg, Nlj;
+  double Lb[3], iLb[3];
+
+  /* derived constants (prms.f90 readprms/setupSiGe/setupMol) */
+  double Pi, thrd;
+  double eps[2][2], isigma[2][2], leps[2][2][2], epssig[2][2];
+  double Zmol[3], aamol[3][3], ie0;
+
+  /* neighbour lists (si.f90 module variables) */
+  double rc, rclj, rlj2;
+  int Nc[3];
+  int ML2, ML3, MLlj;          /* reference capacities (warning thresholds) */
+  int cap2, cap3, caplj;       /* allocated sizes (grown on demand)          */
+  int* nss;                    /* (Natm,2) col-major                          */
+  int* nsslj;                  /* (Natm,2)                                    */
+  int* nlist2;                 /* full list, then halved in place             */
+  int* nlistlj;
+  int* nlist3;                 /* (cap3,3) col-major                          */
+  int Nbrs;                    /* triplet count                               */
+  long long nbr_cnt_full;      /* full SW entries before halving              */
+  long long nbr_cntlj_full;    /* full Moliere entries before halving         */
+  int overflow;                /* bit0 ML2, bit1 ML3, bit2 MLlj exceeded      */
+  int cell_oob;                /* atoms whose cell index fell outside 0..N+1  */
+
+  /* 2-body table (mktables) */
+  double umax;
+  double* table2bd;            /* 1-based: table2bd[i-1]                      */
+  double* u;
+  int table_err;               /* itable2bd index > Ntable events             */
+
+  /* state */
+  double *X, *Xi, *V, *F, *mass;
+  int *atype, *xsides;
+
+  /* regime (prms.f90 ionrun) and impact counter */
+  double Ts, Tau;
+  int ntlist, atlist, dslist, atm_out;
+  int impact;
+  int atom_is_fast, atom_is_slow;
+} orc_sys;
+
+/* Park-Miller minimal standard with Bays-Durham shuffle (ran1, src/ran1.f). */
+typedef struct orc_rng {
+  int iv[32];
+  int iy;
+  int idum;
+} orc_rng;
+
+/* prms.f90:172-216 constants and the reference's shipped siga.in */
+void orc_params_default(fibmd_params* p);
+int orc_init(orc_sys* s, const fibmd_params* p);
+void orc_free(orc_sys* s);
+
+/* si.f90 */
+void orc_si_nlist(orc_sys* s, const double* X);
+double orc_itable2bd(orc_sys* s, double ue);
+void orc_si_force(orc_sys* s, const double* Xp, double* F);
+void orc_si_force_omp(orc_sys* s, const double* Xp, double* F, int nthreads);
+void orc_si_potential(orc_sys* s, const double* X, double* Utot, double* u);
+
+/* temp.f90 / tools.f90 / timeint.f90 */
+double orc_temperature(orc_sys* s, const double* V);
+void orc_adjusttemp(orc_sys* s, double Temp, double Ttar);
+void orc_controlsidetemp(orc_sys* s, double Ttar);
+void orc_frzsptrdatms(orc_sys* s);
+void orc_rebox(orc_sys* s);
+void orc_freezsidesN(orc_sys* s);
+void orc_calc_atm(orc_sys* s);
+void orc_ionrun(orc_sys* s, int tic);
+void orc_onestep(orc_sys* s, int whichctrl, double Ttar, long long lt,
+                 double* time, double* temp, int nthreads);
+/* TI loop; returns the number of onestep calls made (bounded by max_steps
+   when max_steps > 0). */
+long long orc_TI(orc_sys* s, int whichctrl, double Ttar, long long Nt,
+                 double* time, long long* lt, double* temp,
+                 long long max_steps, int nthreads);
+
+/* set-up restatements (prms.f90 pureepi, data.f90, knock.f90, ran1.f) */
+void orc_rng_seed(orc_rng* r, int seed);
+double orc_ran1(orc_rng* r);
+/* pureepi: fills XX (8*Nc1*Nc2*Nc3,3) already rounded through the si.dat
+   text format (3E20.10) as readlat reads it back, xsides from the unrounded
+   lattice, and Lb. Returns Nsg. */
+int orc_pureepi(int Nc1, int Nc2, int Nc3, double* XX, int* xsides,
+                double Lb[3]);
+/* initranions: Xrand (Nrand,2) rounded through fwhm.dat's E12.6 format. */
+void orc_initranions(orc_rng* r, int Nrand, double fwhm, double Pi,
+                     double* Xrand);
+void orc_initIons(orc_sys* s, orc_rng* r);
+void orc_assignmass(orc_sys* s);
+void orc_randvel(orc_sys* s, orc_rng* r, double Uo);
+void orc_knock(orc_sys* s, orc_rng* r, int knc, double eV, double phiz,
+               double phixy, const double* Xrand, int Nrand);
+
+/* accessors for the Python test harness */
+orc_sys* orc_create(const fibmd_params* p);
+void orc_destroy(orc_sys* s);
+void orc_arrays(orc_sys* s, double** X, double** Xi, double** V, double** F, double** mass,
+                int** atype, int** xsides);
+void orc_set_impact(orc_sys* s, int impact);
+void orc_set_tau(orc_sys* s, double tau);
+void orc_set_fast(orc_sys* s, int fast, int slow);
+void orc_regime(orc_sys* s, double* Ts, double* Tau, int* ints5);
+void orc_list_info(orc_sys* s, long long* out6);
+void orc_geometry(orc_sys* s, double* rc_rclj_rlj2_umax, int* Nc);
+const double* orc_table(orc_sys* s, int which);
+
+/* helpers for tests: half lists as sorted 1-based pairs, triplets sorted */
+long long orc_get_pairs(orc_sys* s, int kind, int* ij, long long cap);
+long long orc_get_triplets(orc_sys* s, int* ijk, long long cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
