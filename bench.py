@@ -1,0 +1,431 @@
+#!/usr/bin/env python
+"""Throughput of the FIB_MD hot path on GB300: atom-steps/s.
+
+Workload (BASELINE config 2): a diamond-cubic Si slab of 40 x 40 x 20 unit
+cells (256,000 Si; the named atom count) plus one Ga ion at
+5 keV, 7 degrees off normal, seeded azimuth and impact point 10 A above the
+surface; Maxwell-Boltzmann velocities at 300 K (seeded); bottom 2 atomic
+layers fixed, next 4 Berendsen-thermostatted at 300 K; variable dt
+= min(1 fs, 0.05 A / max|v|); lists rebuilt at half the skin. Synthetic data.
+
+One bench step = `--md-steps` (default 50) MD steps through fibmd_gpu_steps.
+`value` is the mixed-precision path (binary32 force arithmetic, binary64
+accumulation/integration) with the state resident in HBM; `fp64` is the
+plain binary64 path on the same workload. L2 (129 MB) is flushed between
+timed steps (the resident working set is ~70 MB). `e2e` times the C-ABI
+calls a host makes with host buffers: upload (pinned) -> steps -> download.
+
+--impl reference times the CPU oracle (the binary64 restatement of the
+reference's onestep, OpenMP over all host cores) on a bounded sample of the
+same slab.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+KB = 1.381e-23
+A_LAT = 5.431073e-10
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--md-steps", type=int, default=50)
+    ap.add_argument("--cells", default="40,40,20")
+    ap.add_argument("--fp64-steps", type=int, default=-1)
+    ap.add_argument("--cpu-sample-steps", type=int, default=12)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# workload
+def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0):
+    import fib_md_gb300 as fm
+
+    p = fm.params_default()
+    p.mode = fm.MODE_SPEC
+    s = fm.crystal_system(cells, 1, -seed, params=p)
+    p = s.params
+    N, nsg = p.Natm, p.Nsg
+    rs = np.random.default_rng(seed)
+    # Maxwell-Boltzmann at 300 K, zero net momentum
+    V = np.zeros((N, 3), order="F")
+    sd = np.sqrt(KB * 300.0 / s.mass[:nsg])
+    V[:nsg] = rs.normal(size=(nsg, 3)) * sd[:, None]
+    V[:nsg] -= (s.mass[:nsg, None] * V[:nsg]).sum(0) / s.mass[:nsg].sum()
+    # layers: (001) planes are a/4 apart; bottom 2 fixed, next 4 thermostatted
+    z = s.X[:nsg, 2]
+    tags = np.zeros(N, dtype=np.uint32)
+    layer = np.rint(z / (A_LAT / 4)).astype(int)
+    tags[:nsg][layer < 2] = fm.TAG_FROZEN
+    tags[:nsg][(layer >= 2) & (layer < 6)] = fm.TAG_THERMO
+    V[:nsg][layer < 2] = 0.0
+    # the ion: 10 A above the surface, seeded point and azimuth
+    surf = z.max()
+    az = rs.uniform(0.0, 2 * np.pi)
+    th = np.deg2rad(polar_deg)
+    speed = np.sqrt(2 * energy_eV * p.ec / p.massGa)
+    X = s.X.copy(order="F")
+    X[nsg] = [rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1]), surf + 10e-10]
+    V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
+    p.Ttar1 = 300.0
+    p.tau_spec = 1.0e-13
+    p.remove_z = surf + 15e-10 + 20e-10  # sputtered atoms well above the surface leave
+    return dict(params=p, X=X, V=V, Xi=s.Xi.copy(order="F"), mass=s.mass.copy(),
+                atype=s.atype.copy(), xsides=np.zeros(N, dtype=np.int32), tags=tags)
+
+
+def make_ctx(w, precision):
+    import fib_md_gb300 as fm
+
+    p = w["params"].copy()
+    p.precision = precision
+    g = fm.FibMD(p)
+    g.upload(w["X"], w["V"], None, w["Xi"], w["mass"], w["atype"], w["xsides"])
+    g.set_tags(w["tags"])
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+    return g
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = list(csv.reader(io.StringIO(getattr(self, "out", "") or "")))
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+            except ValueError:
+                continue
+            for k, name in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def run_device(g, torch, stream, steps, md_steps, flush):
+    """Times `steps` bench steps on the device; returns per-step seconds."""
+    times = []
+    lt, t, T = 0, 0.0, 300.0
+    for _ in range(steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        lt, t, T, _ = g.steps(2, md_steps, lt, t, T)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    return times
+
+
+def flops_per_force(counts):
+    """Algorithmic flop model (+ - * / sqrt and exp count 1): 40 per active
+    SW pair, 100 per non-zero angle term, 60 per Moliere pair, 100 per
+    stale-list angle term."""
+    pairs, angles, mol, stale = counts
+    return 40 * pairs + 100 * angles + 60 * mol + 100 * stale
+
+
+def bench_ours(args, rank, world, dist):
+    import torch
+
+    import fib_md_gb300 as fm
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    cells = tuple(int(x) for x in args.cells.split(","))
+    w = make_workload(cells)
+    N = w["params"].Natm
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    fp64_peak, fp32_peak = fm.md.pipe_peaks()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- mixed precision (the headline)
+    g = make_ctx(w, fm.PREC_MIXED)
+    g.set_option("timers", 0)
+    stream = torch.cuda.ExternalStream(g.stream_ptr)
+    run_device(g, torch, stream, args.warmup, args.md_steps, flush)
+    g.set_option("kernel_timing", 1)
+    g.kernel_time(reset=True)
+    barrier()
+    with ClockSampler(dev) as clk:
+        w0 = time.perf_counter()
+        times = run_device(g, torch, stream, args.steps, args.md_steps, flush)
+        barrier()
+        wall = time.perf_counter() - w0
+    fk_total, fk_n = g.kernel_time(reset=True)
+    g.set_option("kernel_timing", 0)
+    t_dev = sum(times)
+    if dist is not None:
+        tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    atom_steps = float(N) * args.md_steps * args.steps * world
+    value = atom_steps / t_dev
+    g.si_force()
+    counts = g.work_counters()
+    flops = flops_per_force(counts)
+    fk_avg = fk_total / max(fk_n, 1)
+    achieved = flops / fk_avg / 1e12
+
+    # ---- end to end through the C-ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        def pinned(shape_fortran):
+            n = int(np.prod(shape_fortran))
+            t = torch.empty(n, dtype=torch.float64, pin_memory=True)
+            a = t.numpy()
+            return a.reshape(shape_fortran[::-1]).T if len(shape_fortran) > 1 else a
+
+        X, V, F = g.download()
+        hX, hV, hF, hXi = (pinned((N, 3)) for _ in range(4))
+        hX[:], hV[:], hF[:], hXi[:] = X, V, F, w["Xi"]
+        hm = pinned((N,))
+        hm[:] = w["mass"]
+        ha = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+        ha[:] = w["atype"]
+        hs = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+        hs[:] = w["xsides"]
+        lt, tm, T = 0, 0.0, 300.0
+        barrier()
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            g.upload(hX, hV, hF, hXi, hm, ha, hs)
+            lt, tm, T, _ = g.steps(2, args.md_steps, lt, tm, T)
+            X, V, F = g.download()
+            hX[:], hV[:], hF[:] = X, V, F
+        barrier()
+        t_e2e = time.perf_counter() - w0
+        if dist is not None:
+            tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_e2e = float(tt.item())
+        e2e = {"value": atom_steps / t_e2e, "unit": "atom-steps/s",
+               "h2d_bytes_per_step": N * (4 * 24 + 8 + 4 + 4),
+               "d2h_bytes_per_step": N * 3 * 24}
+    g.close()
+
+    # ---- plain binary64 on the same workload
+    g64 = make_ctx(w, fm.PREC_FP64)
+    g64.set_option("timers", 0)
+    s64 = torch.cuda.ExternalStream(g64.stream_ptr)
+    n64 = args.fp64_steps if args.fp64_steps > 0 else max(2, args.steps // 2)
+    run_device(g64, torch, s64, max(1, args.warmup - 1), args.md_steps, flush)
+    g64.set_option("kernel_timing", 1)
+    g64.kernel_time(reset=True)
+    barrier()
+    t64 = run_device(g64, torch, s64, n64, args.md_steps, flush)
+    f64_total, f64_n = g64.kernel_time(reset=True)
+    g64.si_force()
+    c64 = g64.work_counters()
+    g64.close()
+    t64_sum = sum(t64)
+    if dist is not None:
+        tt = torch.tensor([t64_sum], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t64_sum = float(tt.item())
+    value64 = float(N) * args.md_steps * n64 * world / t64_sum
+    f64_avg = f64_total / max(f64_n, 1)
+
+    # HBM view of the whole step: 150 algorithmic bytes per atom-step
+    step_bytes = 150.0 * N
+    md_step_s = t_dev / (args.md_steps * args.steps)
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    traffic = None
+    tr_file = ROOT / "profiles" / "force_kernel_traffic.json"
+    if tr_file.exists():
+        tr = json.loads(tr_file.read_text())
+        bpa = tr.get("mixed_bytes_per_atom")
+        if bpa:
+            traffic = bpa * N
+
+    out = {
+        "metric": "atom-steps/s (256k-atom Si slab, 5 keV Ga, mixed precision)",
+        "value": value,
+        "unit": "atom-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_dev / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 force arithmetic, f64 accumulation/positions/VV",
+        "data": "synthetic",
+        "config": {
+            "workload": f"Si slab {cells[0]}x{cells[1]}x{cells[2]} unit cells "
+                        f"({N - 1} Si + 1 Ga), 5 keV Ga at 7 deg, variable dt, "
+                        f"{args.md_steps} MD steps per bench step",
+            "atoms": N, "md_steps_per_step": args.md_steps, "mode": "spec",
+            "parallelism": f"replicas x{world}", "l2": "flushed between timed steps",
+        },
+        "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
+                 "mixed_over_fp64": value / value64,
+                 "force_kernel_ms": 1e3 * f64_avg,
+                 "roofline": {"bound": "fp64", "achieved": flops_per_force(c64) / f64_avg / 1e12,
+                              "peak": fp64_peak, "unit": "TFLOP/s",
+                              "frac": flops_per_force(c64) / f64_avg / 1e12 / fp64_peak,
+                              "peak_source": "measured in this run (DFMA loop)"}},
+        "roofline": {"bound": "fp32", "kernel": "k_force<mixed>", "achieved": achieved,
+                     "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": traffic, "flops_per_launch": flops,
+                     "force_kernel_ms": 1e3 * fk_avg, "launches": fk_n,
+                     "peak_source": "measured in this run (FFMA loop)"},
+        "roofline_hbm": {"bound": "hbm", "achieved": step_bytes / md_step_s / 1e9,
+                         "peak": hbm_peak, "unit": "GB/s",
+                         "frac": step_bytes / md_step_s / 1e9 / hbm_peak,
+                         "bytes_per_atom_step": 150,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "work_counters": {"sw_pairs": counts[0], "angle_terms": counts[1],
+                          "moliere_pairs": counts[2], "stale_terms": counts[3]},
+        "gpu_launches": (15 * args.md_steps + 1) * args.steps,
+        "wall_s_timed": wall,
+        "clocks": clk.summary(),
+    }
+    if e2e:
+        out["e2e"] = e2e
+    return out
+
+
+# ---------------------------------------------------------------------------
+def cpu_baseline(cells, sample_steps, nthreads=None):
+    """The oracle's onestep (binary64, the reference's algorithm) on the same
+    slab over all host cores; one list build per 50 steps as ntlist_i."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_ffi as of
+
+    nthreads = nthreads or os.cpu_count() or 1
+    o, rng, Xr = of.crystal(cells, 1, -2001)
+    w = make_workload(cells)
+    o.X[:] = w["X"]
+    o.V[:] = w["V"]
+    o.set_impact(1)
+    t0 = time.perf_counter()
+    o.si_nlist()
+    t_nl = time.perf_counter() - t0
+    o.F[:] = o.si_force(nthreads=nthreads)
+    lt, tm, T = 0, 0.0, 300.0
+    t0 = time.perf_counter()
+    for k in range(sample_steps):
+        tm, T = o.onestep(2, k + 1, tm, T, nthreads)
+    t_st = time.perf_counter() - t0
+    per_step = t_st / sample_steps + t_nl / 50.0
+    N = o.N
+    o.close()
+    return {"value": N / per_step, "unit": "atom-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{sample_steps} onestep calls + 1 si_nlist (weighted 1/50) on the "
+                      f"{N}-atom slab, OpenMP over {nthreads} threads"}
+
+
+def main():
+    args = parse()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    cells = tuple(int(x) for x in args.cells.split(","))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        vals = []
+        cb = None
+        for _ in range(max(1, args.steps)):
+            cb = cpu_baseline(cells, max(2, args.cpu_sample_steps // 2))
+            vals.append(cb["value"])
+            if len(vals) >= 3:
+                break
+        v = statistics.median(vals)
+        cb["value"] = v
+        out = {"impl": "reference", "metric": "atom-steps/s (256k-atom Si slab, 5 keV Ga, mixed precision)",
+               "value": v, "unit": "atom-steps/s", "n_gpus": 0, "steps": len(vals),
+               "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "f64", "data": "synthetic",
+               "config": {"workload": f"Si slab {cells[0]}x{cells[1]}x{cells[2]} unit cells, "
+                                      "reference onestep (CPU oracle port)"},
+               "cpu_baseline": cb,
+               "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
+                       "d2h_bytes_per_step": 0}}
+        print(json.dumps(out))
+        return 0
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    out = bench_ours(args, rank, world, dist)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(cells, args.cpu_sample_steps)
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -107,6 +107,9 @@ SIGNATURES = {
     "fibmd_gpu_timers": (_I, [_VP, _DP, _DP, _DP, _DP, _LLP, _I]),
     "fibmd_gpu_work_counters": (_I, [_VP, _LLP]),
     "fibmd_gpu_stream": (_VP, [_VP]),
+    "fibmd_gpu_set_option": (_I, [_VP, C.c_char_p, _D]),
+    "fibmd_gpu_kernel_time": (_I, [_VP, _DP, _LLP, _I]),
+    "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),
     # fibmd_host.h
     "fibmd_host_rng_seed": (None, [C.POINTER(Rng), _I]),
     "fibmd_host_ran1": (_D, [C.POINTER(Rng)]),

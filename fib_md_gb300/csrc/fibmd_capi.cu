@@ -24,7 +24,7 @@ namespace {
 
 std::string g_create_error;
 
-enum Phase { PH_AT = 0, PH_NT = 1, PH_DS = 2, PH_F = 3 };
+enum Phase { PH_AT = 0, PH_NT = 1, PH_DS = 2, PH_F = 3, PH_FK = 4 };
 
 struct TimedRange {
   int phase;
@@ -54,8 +54,9 @@ struct fibmd_ctx {
   bool uploaded = false, lists_built = false, spec_ready = false;
   // timers
   bool timers_on = true;
-  double t[4] = {0, 0, 0, 0};
-  long long c[4] = {0, 0, 0, 0};
+  bool kernel_timing = false;
+  double t[5] = {0, 0, 0, 0, 0};
+  long long c[5] = {0, 0, 0, 0, 0};
   std::vector<TimedRange> pending;
   std::vector<cudaEvent_t> pool;
   long long spec_lt = 0;
@@ -327,6 +328,22 @@ static int sync_scalars(fibmd_ctx* ctx) {
   CK(cudaMemcpyAsync(ctx->h_sc, ctx->S.sc, sizeof(DevScalars), cudaMemcpyDeviceToHost,
                      ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
+}
+
+// Force launch, with events around the main kernel when kernel timing is on.
+static int force_launch(fibmd_ctx* ctx, bool energy, bool count) {
+  Launch L = launch_of(ctx);
+  if (ctx->kernel_timing) {
+    L.force_a = get_event(ctx);
+    L.force_b = get_event(ctx);
+  }
+  cudaError_t e = launch_force(L, ctx->P, ctx->S, energy, count);
+  if (L.force_a) {
+    ctx->pending.push_back({PH_FK, L.force_a, L.force_b});
+    ctx->c[PH_FK]++;
+  }
+  if (e != cudaSuccess) return fail(ctx, FIBMD_ECUDA, "force launch: %s", cudaGetErrorString(e));
   return FIBMD_OK;
 }
 
@@ -759,7 +776,8 @@ int fibmd_gpu_force(fibmd_ctx* ctx, double* F_out, double* u_out, double* Utot) 
   const bool energy = u_out || Utot;
   {
     PhaseTimer t(ctx, PH_F);
-    CK(launch_force(launch_of(ctx), ctx->P, ctx->S, energy, true));
+    int rcf = force_launch(ctx, energy, true);
+    if (rcf) return rcf;
   }
   std::swap(ctx->S.frc, ctx->S.frc_new);
   if (F_out) {
@@ -823,6 +841,32 @@ int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds, double*
   return FIBMD_OK;
 }
 
+int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
+  if (!ctx || !key) return FIBMD_EINVAL;
+  if (!std::strcmp(key, "timers")) {
+    ctx->timers_on = value != 0.0;
+  } else if (!std::strcmp(key, "kernel_timing")) {
+    ctx->kernel_timing = value != 0.0;
+  } else {
+    return fail(ctx, FIBMD_EINVAL, "unknown option '%s'", key);
+  }
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_kernel_time(fibmd_ctx* ctx, double* force_kernel_s, long long* launches,
+                          int reset) {
+  if (!ctx) return FIBMD_EINVAL;
+  cudaStreamSynchronize(ctx->stream);
+  flush_timers(ctx);
+  if (force_kernel_s) *force_kernel_s = ctx->t[PH_FK];
+  if (launches) *launches = ctx->c[PH_FK];
+  if (reset) {
+    ctx->t[PH_FK] = 0;
+    ctx->c[PH_FK] = 0;
+  }
+  return FIBMD_OK;
+}
+
 // ---- one reference step (onestep, timeint.f90:158-242) ---------------------------
 static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, int* why) {
   const Launch L = launch_of(ctx);
@@ -855,7 +899,8 @@ static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, in
   }
   {
     PhaseTimer t(ctx, PH_F);
-    CK(launch_force(L, P, ctx->S, false, false));
+    int rcf = force_launch(ctx, false, false);
+    if (rcf) return rcf;
   }
   CK(launch_kick(L, P, ctx->S, ctx->Ts));
   std::swap(ctx->S.frc, ctx->S.frc_new);
@@ -883,7 +928,8 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     }
     {
       PhaseTimer t(ctx, PH_F);
-      CK(launch_force(L, P, ctx->S, false, false));
+      int rcf = force_launch(ctx, false, false);
+      if (rcf) return rcf;
     }
     CK(launch_spec_kick(L, P, ctx->S, Ttar, 1));
     std::swap(ctx->S.frc, ctx->S.frc_new);

@@ -30,17 +30,24 @@
 
 namespace fibmd {
 
-constexpr int kForceBlock = 128;
 constexpr int kLegF = 9;  // ux uy uz rinv E g fx fy fz
 
-template <typename R>
+// Threads per block of the main force kernel: binary64 stages 12 legs x 9
+// doubles per thread (55 KB per 64 threads, 3 blocks per SM); binary32
+// stages floats (55 KB per 128 threads).
+template <bool MIXED>
+struct ForceBlock {
+  static constexpr int value = MIXED ? 128 : 64;
+};
+
+template <typename R, int BLOCK>
 struct LegSmem {
   R* v;
   int* j;
   __device__ __forceinline__ R& at(int l, int f) {
-    return v[(l * kLegF + f) * kForceBlock + threadIdx.x];
+    return v[(l * kLegF + f) * BLOCK + threadIdx.x];
   }
-  __device__ __forceinline__ int& idx(int l) { return j[l * kForceBlock + threadIdx.x]; }
+  __device__ __forceinline__ int& idx(int l) { return j[l * BLOCK + threadIdx.x]; }
 };
 
 // 3-point Lagrange interpolation of the derivative table (itable2bd).
@@ -63,14 +70,15 @@ __device__ __forceinline__ double table_df(const DevParams& P, const double* __r
 
 // ---- main per-centre kernel ------------------------------------------------
 template <bool MIXED, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(kForceBlock) k_force(DevParams P, DevState S) {
+__global__ void __launch_bounds__(ForceBlock<MIXED>::value) k_force(DevParams P, DevState S) {
   using R = typename std::conditional<MIXED, float, double>::type;
+  constexpr int BLOCK = ForceBlock<MIXED>::value;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LegSmem<R> leg;
+  LegSmem<R, BLOCK> leg;
   leg.v = reinterpret_cast<R*>(smem_raw);
-  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(R) * kMaxLegs * kLegF * kForceBlock);
+  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(R) * kMaxLegs * kLegF * BLOCK);
 
-  const int i = blockIdx.x * kForceBlock + threadIdx.x;
+  const int i = blockIdx.x * BLOCK + threadIdx.x;
   if (i >= P.N) return;
   const int4 qi = S.posq[i];
   const int ti = qi.w & 0xff;
@@ -296,10 +304,11 @@ __device__ __forceinline__ Leg64 make_leg(const DevParams& P, const double4_32a&
   return L;
 }
 
-__device__ __forceinline__ double angle_term(const DevParams& P, int tc, const Leg64& A,
-                                             const Leg64& B, double fc[3], double fa[3],
-                                             double fb[3]) {
-  if (!(A.u < P.cut3 && B.u < P.cut3)) return 0.0;
+__device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg64& A,
+                                           const Leg64& B, double fc[3], double fa[3],
+                                           double fb[3], double* e) {
+  *e = 0.0;
+  if (!(A.u < P.cut3 && B.u < P.cut3)) return false;
   const double ia = 1.0 / (A.u - P.al), ib = 1.0 / (B.u - P.al);
   const double Ea = exp(P.gam * ia), Eb = exp(P.gam * ib);
   const double ga = -P.gam * ia * ia * A.isig, gb = -P.gam * ib * ib * B.isig;
@@ -320,7 +329,8 @@ __device__ __forceinline__ double angle_term(const DevParams& P, int tc, const L
   fc[0] = -(fa[0] + fb[0]);
   fc[1] = -(fa[1] + fb[1]);
   fc[2] = -(fa[2] + fb[2]);
-  return pref * W;
+  *e = pref * W;
+  return true;
 }
 
 // Centres with more than kMaxLegs active legs: every leg pair, direct.
@@ -340,9 +350,8 @@ __global__ void k_force_heavy(DevParams P, DevState S) {
       for (int b = a + 1; b < n; b++) {
         const int jb = S.nbr_sw[(size_t)b * P.N + c];
         const Leg64 B = make_leg(P, pc, S.pos[jb], tc, S.atype[jb]);
-        double f0[3], f1[3], f2[3];
-        const double e = angle_term(P, tc, A, B, f0, f1, f2);
-        if (e == 0.0 && f0[0] == 0.0) continue;
+        double f0[3], f1[3], f2[3], e;
+        if (!angle_term(P, tc, A, B, f0, f1, f2, &e)) continue;
         fcx += f0[0];
         fcy += f0[1];
         fcz += f0[2];
@@ -395,13 +404,12 @@ __global__ void k_force_stale(DevParams P, DevState S) {
         if (in_list(P, S, f, x)) continue;
         const int ta = S.atype[a], tx = S.atype[x];
         const double4_32a pa = S.pos[a], px = S.pos[x];
-        double f0[3], f1[3], f2[3];
+        double f0[3], f1[3], f2[3], e;
         // centre f, legs a and x
         {
           const Leg64 A = make_leg(P, pf, pa, tf, ta);
           const Leg64 X = make_leg(P, pf, px, tf, tx);
-          const double e = angle_term(P, tf, A, X, f0, f1, f2);
-          if (e != 0.0) {
+          if (angle_term(P, tf, A, X, f0, f1, f2, &e)) {
             atomic_add3(S.frc_new, f, f0[0], f0[1], f0[2]);
             atomic_add3(S.frc_new, a, f1[0], f1[1], f1[2]);
             atomic_add3(S.frc_new, x, f2[0], f2[1], f2[2]);
@@ -417,8 +425,7 @@ __global__ void k_force_stale(DevParams P, DevState S) {
         {
           const Leg64 A = make_leg(P, px, pa, tx, ta);
           const Leg64 Fl = make_leg(P, px, pf, tx, tf);
-          const double e = angle_term(P, tx, A, Fl, f0, f1, f2);
-          if (e != 0.0) {
+          if (angle_term(P, tx, A, Fl, f0, f1, f2, &e)) {
             atomic_add3(S.frc_new, x, f0[0], f0[1], f0[2]);
             atomic_add3(S.frc_new, a, f1[0], f1[1], f1[2]);
             atomic_add3(S.frc_new, f, f2[0], f2[1], f2[2]);
@@ -500,15 +507,17 @@ __global__ void k_force_begin(DevState S) {
 template <bool MIXED, bool ENERGY, bool COUNT>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
   const size_t rsz = MIXED ? sizeof(float) : sizeof(double);
-  const size_t smem = rsz * kMaxLegs * kLegF * kForceBlock + sizeof(int) * kMaxLegs * kForceBlock;
+  constexpr int BLOCK = ForceBlock<MIXED>::value;
+  const size_t smem = rsz * kMaxLegs * kLegF * BLOCK + sizeof(int) * kMaxLegs * BLOCK;
   static bool attr_set = false;
   if (!attr_set) {
     cudaFuncSetAttribute(k_force<MIXED, ENERGY, COUNT>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr_set = true;
   }
-  k_force<MIXED, ENERGY, COUNT><<<(P.N + kForceBlock - 1) / kForceBlock, kForceBlock, smem,
-                                  L.stream>>>(P, S);
+  if (L.force_a) cudaEventRecord(L.force_a, L.stream);
+  k_force<MIXED, ENERGY, COUNT><<<(P.N + BLOCK - 1) / BLOCK, BLOCK, smem, L.stream>>>(P, S);
+  if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
   k_force_heavy<ENERGY><<<side, 64, 0, L.stream>>>(P, S);

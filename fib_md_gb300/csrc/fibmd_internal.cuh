@@ -22,7 +22,7 @@
 
 namespace fibmd {
 
-constexpr int kMaxLegs = 8;        // active 3-body legs held per centre
+constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
 constexpr int kMaxRedBlocks = 4096;
 
@@ -272,6 +272,8 @@ __device__ __forceinline__ bool grid_finish(double (&v)[NV], double* partials,
 struct Launch {
   cudaStream_t stream;
   int sms;
+  cudaEvent_t force_a = nullptr;  // recorded around the main force kernel
+  cudaEvent_t force_b = nullptr;  // when kernel timing is on
 };
 
 // fibmd_nlist.cu

@@ -132,6 +132,15 @@ def knock(p: Params, rng: Ran1, knc: int, eV: float, phiz: float, phixy: float,
     return i, x, v
 
 
+def pipe_peaks():
+    """Measured (fp64, fp32) FMA TFLOP/s of the current device."""
+    a, b = C.c_double(), C.c_double()
+    rc = _abi.load().fibmd_gpu_pipe_peaks(C.byref(a), C.byref(b))
+    if rc:
+        raise FibmdError(rc, "pipe_peaks")
+    return a.value, b.value
+
+
 class FibMD:
     """One device context (libfibmd_gpu's fibmd_ctx)."""
 
@@ -279,6 +288,20 @@ class FibMD:
         tic = C.c_int()
         self._check(self.lib.fibmd_gpu_regime(self.h, C.byref(Ts), C.byref(tic)), "regime")
         return Ts.value, tic.value
+
+    def set_option(self, key: str, value: float):
+        self._check(self.lib.fibmd_gpu_set_option(self.h, key.encode(), float(value)), "set_option")
+
+    def kernel_time(self, reset: bool = False):
+        t = C.c_double()
+        n = C.c_longlong()
+        self._check(self.lib.fibmd_gpu_kernel_time(self.h, C.byref(t), C.byref(n), int(reset)),
+                    "kernel_time")
+        return t.value, n.value
+
+    @property
+    def stream_ptr(self) -> int:
+        return int(self.lib.fibmd_gpu_stream(self.h) or 0)
 
     def timers(self, reset: bool = False):
         v = [C.c_double() for _ in range(4)]

@@ -247,6 +247,21 @@ int fibmd_gpu_regime(fibmd_ctx* ctx, double* Ts, int* tic);
 int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds,
                      double* f, long long* counts4, int reset);
 
+/* Options: "timers" (phase timers of fibmd_gpu_timers, default 1) and
+   "kernel_timing" (CUDA events around every launch of the main force
+   kernel, default 0). */
+int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
+
+/* Total device time (s) and number of launches of the main force kernel
+   since the last reset, from the events of the "kernel_timing" option. */
+int fibmd_gpu_kernel_time(fibmd_ctx* ctx, double* force_kernel_s,
+                          long long* launches, int reset);
+
+/* Measured FMA throughput of the current device in TFLOP/s (an FMA is 2
+   flops): independent binary64 and binary32 FMA chains over every SM. A
+   diagnostic for reporting the force kernel against its arithmetic pipe. */
+int fibmd_gpu_pipe_peaks(double* fp64_tflops, double* fp32_tflops);
+
 /* Counters of the last force evaluation: active SW pairs (i<j with a
    non-zero table entry), non-zero 3-body angle terms, Moliere pairs
    evaluated, and stale-list angle terms added by the correction pass. */

@@ -196,8 +196,10 @@ def test_regime_switch_and_parking(gpu_lib):
     o = _slab((4, 4, 4), fire=False, params=p)
     nsg = o.p.Nsg
     L3 = o.p.Lb[2]
-    o.X[nsg - 1, 2] = 2.0 * L3 / 10  # inside outz(1)..outz(2)
-    o.X[nsg - 2, 2] = 8.0 * L3 / 10  # inside outz(3)..outz(4)
+    free = np.nonzero(o.xsides[:nsg] == 0)[0]  # edge atoms are pinned to Xi
+    a, b = int(free[-1]), int(free[-2])
+    o.X[a, 2] = 2.0 * L3 / 10  # inside outz(1)..outz(2)
+    o.X[b, 2] = 8.0 * L3 / 10  # inside outz(3)..outz(4)
     o.set_impact(1)
     o.set_fast(True)
     g = _gpu(o, impact=1)
@@ -211,7 +213,8 @@ def test_regime_switch_and_parking(gpu_lib):
     Ts_o, _, ints = o.regime()
     assert tic == 2 and Ts == Ts_o == o.p.Ts_r and ints[4] == 0
     X, V, F = g.download()
-    assert X[nsg - 1, 2] == o.X[nsg - 1, 2] == o.p.atomz[0] * L3 / 10.0
+    assert X[a, 2] == o.X[a, 2] == o.p.atomz[0] * L3 / 10.0
+    assert X[b, 2] == o.X[b, 2] == o.p.atomz[1] * L3 / 10.0
     assert np.abs(X - o.X).max() < TRAJ_ATOL_M
 
 
