@@ -8,7 +8,7 @@ surface; Maxwell-Boltzmann velocities at 300 K (seeded); bottom 2 atomic
 layers fixed, next 4 Berendsen-thermostatted at 300 K; variable dt
 = min(1 fs, 0.05 A / max|v|); lists rebuilt at half the skin. Synthetic data.
 
-One bench step = `--md-steps` (default 50) MD steps through fibmd_gpu_steps.
+One bench step = `--md-steps` (default 1000) MD steps through fibmd_gpu_steps.
 `value` is the mixed-precision path (binary32 force arithmetic, binary64
 accumulation/integration) with the state resident in HBM; `fp64` is the
 plain binary64 path on the same workload. L2 (129 MB) is flushed between
@@ -47,12 +47,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--md-steps", type=int, default=50)
+    ap.add_argument("--md-steps", type=int, default=1000)
     ap.add_argument("--cells", default="40,40,20")
     ap.add_argument("--fp64-steps", type=int, default=-1)
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
+                    help="set up the workload, evaluate the force 3 times, exit (for ncu)")
     return ap.parse_args()
 
 
@@ -123,7 +125,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -410,6 +412,16 @@ def main():
                "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
+        return 0
+
+    if args.profile:
+        import fib_md_gb300 as fm
+
+        w = make_workload(cells)
+        g = make_ctx(w, fm.PREC_MIXED if args.profile == "mixed" else fm.PREC_FP64)
+        for _ in range(3):
+            g.si_force()
+        g.close()
         return 0
 
     dist = None

@@ -24,7 +24,10 @@ namespace {
 
 std::string g_create_error;
 
-enum Phase { PH_AT = 0, PH_NT = 1, PH_DS = 2, PH_F = 3, PH_FK = 4 };
+// Timed phases: the reference's calc_time report (at, nt, ds, f), the main
+// force kernel alone, and the velocity-Verlet halves with their reductions.
+enum Phase { PH_AT = 0, PH_NT = 1, PH_DS = 2, PH_F = 3, PH_FK = 4, PH_DRIFT = 5, PH_KICK = 6,
+             PH_COUNT = 7 };
 
 struct TimedRange {
   int phase;
@@ -55,11 +58,19 @@ struct fibmd_ctx {
   // timers
   bool timers_on = true;
   bool kernel_timing = false;
-  double t[5] = {0, 0, 0, 0, 0};
-  long long c[5] = {0, 0, 0, 0, 0};
+  double t[PH_COUNT] = {};
+  long long c[PH_COUNT] = {};
   std::vector<TimedRange> pending;
   std::vector<cudaEvent_t> pool;
   long long spec_lt = 0;
+  // CUDA-graph step loop (spec mode)
+  bool use_graph = true;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  cudaStream_t cap2 = nullptr;
+  double4_32a* graph_frc = nullptr;  // S.frc when the graph was captured
+  int graph_nfired = -1;
+  int* d_remaining = nullptr;
   std::string err;
 };
 
@@ -262,6 +273,7 @@ static int derive_params(fibmd_ctx* ctx) {
   const double skin = std::min(rc - P.cut3 * sigmax, rclj - rlj);
   const double half = 0.5 * skin * 0.99;
   P.disp_fast2 = half * half;
+  P.disp_fastA2 = (float)(half * half * 1e20);
   // binary32 reduced units
   for (int a = 0; a < 2; a++)
     for (int b = 0; b < 2; b++) {
@@ -445,6 +457,8 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
       p->Lb[2] <= 0 || p->Ntable < 8)
     return fail(nullptr, FIBMD_EINVAL, "bad sizes (Natm %d Nsg %d Ntable %d)", p->Natm, p->Nsg,
                 p->Ntable);
+  if (p->max_sw_nbrs > 64)
+    return fail(nullptr, FIBMD_EINVAL, "max_sw_nbrs %d exceeds 64", p->max_sw_nbrs);
   if (p->precision == FIBMD_PREC_MIXED && (p->psi != 4.0 || p->qsi != 0.0))
     return fail(nullptr, FIBMD_EINVAL, "mixed precision implements psi = 4, qsi = 0 only");
   int ndev = 0;
@@ -486,15 +500,18 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   AL(S.frc, N);
   AL(S.frc_new, N);
   AL(S.xi, N);
-  AL(S.pos_build, N);
   AL(S.posq, N);
+  AL(S.posq_build, N);
   AL(S.mass, N);
+  AL(S.inv_mass, N);
   AL(S.atype, N);
   AL(S.flags, N);
   AL(S.cell_count, (size_t)ctx->P.ncell + 1);
   AL(S.cell_start, (size_t)ctx->P.ncell + 1);
   AL(S.cell_atoms, N);
+  AL(S.posq_cell, N);
   AL(S.atom_cell, N);
+  AL(S.nonempty, N);
   AL(S.scan_blocks, (size_t)nscan + 1);
   AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
   AL(S.n_sw, N);
@@ -513,6 +530,7 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   AL(S.sc, 1);
   AL(ctx->d_stage, 3 * N);
   AL(ctx->d_u64, 4);
+  AL(ctx->d_remaining, 1);
 #undef AL
   if (cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
     g_create_error = "cudaMallocHost failed";
@@ -538,9 +556,19 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   return FIBMD_OK;
 }
 
+static void drop_graph(fibmd_ctx* ctx) {
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->graph_exec = nullptr;
+  ctx->graph = nullptr;
+  ctx->graph_frc = nullptr;
+}
+
 void fibmd_gpu_destroy(fibmd_ctx* ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  drop_graph(ctx);
+  if (ctx->cap2) cudaStreamDestroy(ctx->cap2);
   flush_timers(ctx);
   for (auto e : ctx->pool) cudaEventDestroy(e);
   for (void* p : ctx->allocs) cudaFree(p);
@@ -577,8 +605,15 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
     CK(cudaMemcpyAsync(ctx->d_stage, src[k], b3, cudaMemcpyHostToDevice, ctx->stream));
     CK(launch_pack(L, N, dst[k], ctx->d_stage));
   }
+  std::vector<double> inv((size_t)N);
+  for (int i = 0; i < N; i++) {
+    if (!(mass[i] > 0.0)) return fail(ctx, FIBMD_EINVAL, "mass(%d) = %g", i + 1, mass[i]);
+    inv[i] = 1.0 / mass[i];
+  }
   CK(cudaMemcpyAsync(ctx->S.mass, mass, sizeof(double) * (size_t)N, cudaMemcpyHostToDevice,
                      ctx->stream));
+  CK(cudaMemcpyAsync(ctx->S.inv_mass, inv.data(), sizeof(double) * (size_t)N,
+                     cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->S.atype, t8.data(), (size_t)N, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(ctx->S.flags, fl.data(), sizeof(uint32_t) * (size_t)N,
                      cudaMemcpyHostToDevice, ctx->stream));
@@ -802,7 +837,7 @@ int fibmd_gpu_force(fibmd_ctx* ctx, double* F_out, double* u_out, double* Utot) 
   return check_list_status(ctx);
 }
 
-int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[4]) {
+int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[6]) {
   if (!ctx || !counts) return FIBMD_EINVAL;
   int rc = sync_scalars(ctx);
   if (rc) return rc;
@@ -810,6 +845,8 @@ int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[4]) {
   counts[1] = (long long)ctx->h_sc->counters[1];
   counts[2] = (long long)(ctx->h_sc->counters[2] / 2);
   counts[3] = (long long)ctx->h_sc->counters[3];
+  counts[4] = (long long)ctx->h_sc->rebuilds;
+  counts[5] = (long long)ctx->h_sc->heavy_count;
   return FIBMD_OK;
 }
 
@@ -841,12 +878,29 @@ int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds, double*
   return FIBMD_OK;
 }
 
+int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7, int reset) {
+  if (!ctx) return FIBMD_EINVAL;
+  cudaStreamSynchronize(ctx->stream);
+  flush_timers(ctx);
+  for (int k = 0; k < PH_COUNT; k++) {
+    if (seconds7) seconds7[k] = ctx->t[k];
+    if (counts7) counts7[k] = ctx->c[k];
+    if (reset) {
+      ctx->t[k] = 0;
+      ctx->c[k] = 0;
+    }
+  }
+  return FIBMD_OK;
+}
+
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
   if (!ctx || !key) return FIBMD_EINVAL;
   if (!std::strcmp(key, "timers")) {
     ctx->timers_on = value != 0.0;
   } else if (!std::strcmp(key, "kernel_timing")) {
     ctx->kernel_timing = value != 0.0;
+  } else if (!std::strcmp(key, "graph")) {
+    ctx->use_graph = value != 0.0;
   } else {
     return fail(ctx, FIBMD_EINVAL, "unknown option '%s'", key);
   }
@@ -873,9 +927,12 @@ static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, in
   const DevParams& P = ctx->P;
   const double Ttar = ctx->p.Ttar1;
   *time = *time + ctx->Ts;
-  if (whichctrl == 0) CK(launch_adjust_and_temp(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar));
-  if (whichctrl > 0) CK(launch_side_reduce(L, P, ctx->S));
-  CK(launch_drift(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar, whichctrl > 0));
+  {
+    PhaseTimer t(ctx, PH_DRIFT);
+    if (whichctrl == 0) CK(launch_adjust_and_temp(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar));
+    if (whichctrl > 0) CK(launch_side_reduce(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar));
+    CK(launch_drift(L, P, ctx->S, ctx->Ts, ctx->Tau, Ttar, whichctrl > 0));
+  }
   if (ctx->atlist > 0 && lt % ctx->atlist == 0) {
     PhaseTimer t(ctx, PH_AT);
     CK(launch_park(L, P, ctx->S));
@@ -902,8 +959,114 @@ static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, in
     int rcf = force_launch(ctx, false, false);
     if (rcf) return rcf;
   }
-  CK(launch_kick(L, P, ctx->S, ctx->Ts));
+  {
+    PhaseTimer t(ctx, PH_KICK);
+    CK(launch_kick(L, P, ctx->S, ctx->Ts));
+  }
   std::swap(ctx->S.frc, ctx->S.frc_new);
+  return FIBMD_OK;
+}
+
+// Captures two spec-mode MD steps (the force buffers swap back) as the body
+// of a WHILE node; in each step an IF node runs the list rebuild only when
+// the drift found an atom beyond half the skin.
+static int build_spec_graph(fibmd_ctx* ctx) {
+  drop_graph(ctx);
+  if (!ctx->cap2) CK(cudaStreamCreateWithFlags(&ctx->cap2, cudaStreamNonBlocking));
+  const DevParams& P = ctx->P;
+  const double Ttar = ctx->p.Ttar1;
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  ctx->graph = g;
+  cudaGraphConditionalHandle hw;
+  CK(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = hw;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  CK(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+
+  cudaStream_t cs = ctx->stream;
+  Launch L = launch_of(ctx);
+  Launch L2 = L;
+  L2.stream = ctx->cap2;
+  DevState Sx = ctx->S;
+  CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  auto abort_capture = [&](cudaError_t e, const char* what) {
+    cudaGraph_t tmp = nullptr;
+    cudaStreamEndCapture(cs, &tmp);
+    drop_graph(ctx);
+    return fail(ctx, FIBMD_ECUDA, "graph capture (%s): %s", what, cudaGetErrorString(e));
+  };
+#define CKC(call, what)                           \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return abort_capture(e_, what); \
+  } while (0)
+  for (int half = 0; half < 2; half++) {
+    CKC(launch_spec_drift(L, P, Sx, Ttar), "drift");
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
+    cudaGraphConditionalHandle hi;
+    CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
+    CKC(launch_set_rebuild_cond(cs, Sx.sc, hi), "cond");
+    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd), "deps");
+    cudaGraphNodeParams ip = {};
+    ip.type = cudaGraphNodeTypeConditional;
+    ip.conditional.handle = hi;
+    ip.conditional.type = cudaGraphCondTypeIf;
+    ip.conditional.size = 1;
+    cudaGraphNode_t inode;
+    CKC(cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip), "if node");
+    CKC(cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies), "update");
+    cudaGraph_t ib = ip.conditional.phGraph_out[0];
+    CKC(cudaStreamBeginCaptureToGraph(ctx->cap2, ib, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal), "if capture");
+    cudaError_t eb = launch_build_lists(L2, P, Sx, 0);
+    cudaGraph_t tmp = nullptr;
+    cudaError_t ee = cudaStreamEndCapture(ctx->cap2, &tmp);
+    if (eb != cudaSuccess) return abort_capture(eb, "rebuild");
+    if (ee != cudaSuccess) return abort_capture(ee, "if end");
+    CKC(launch_force(L, P, Sx, false, false), "force");
+    CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
+    std::swap(Sx.frc, Sx.frc_new);
+  }
+  CKC(launch_loop_ctl(cs, ctx->d_remaining, hw), "loop");
+#undef CKC
+  cudaGraph_t out = nullptr;
+  CK(cudaStreamEndCapture(cs, &out));
+  cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, g, 0);
+  if (ei != cudaSuccess) {
+    drop_graph(ctx);
+    return fail(ctx, FIBMD_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+  }
+  ctx->graph_frc = ctx->S.frc;
+  ctx->graph_nfired = P.nfired;
+  return FIBMD_OK;
+}
+
+// Runs `pairs` x 2 spec-mode steps with one graph launch.
+static int run_spec_graph(fibmd_ctx* ctx, long long pairs) {
+  if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired) {
+    int rc = build_spec_graph(ctx);
+    if (rc) return rc;
+  }
+  while (pairs > 0) {
+    const int chunk = (int)std::min<long long>(pairs, 1 << 30);
+    CK(cudaMemcpyAsync(ctx->d_remaining, &chunk, sizeof(int), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // the host value must be read before reuse
+    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+    pairs -= chunk;
+  }
   return FIBMD_OK;
 }
 
@@ -920,8 +1083,18 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->spec_ready = true;
   }
-  for (long long n = 0; n < max_steps; n++) {
-    CK(launch_spec_drift(L, P, ctx->S, Ttar));
+  long long todo = max_steps;
+  if (ctx->use_graph && todo >= 2) {
+    int rc = run_spec_graph(ctx, todo / 2);
+    if (rc) return rc;
+    *lt += 2 * (todo / 2);
+    todo -= 2 * (todo / 2);
+  }
+  for (long long n = 0; n < todo; n++) {
+    {
+      PhaseTimer t(ctx, PH_DRIFT);
+      CK(launch_spec_drift(L, P, ctx->S, Ttar));
+    }
     {
       PhaseTimer t(ctx, PH_NT);
       CK(launch_build_lists(L, P, ctx->S, 1));
@@ -931,7 +1104,10 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
       int rcf = force_launch(ctx, false, false);
       if (rcf) return rcf;
     }
-    CK(launch_spec_kick(L, P, ctx->S, Ttar, 1));
+    {
+      PhaseTimer t(ctx, PH_KICK);
+      CK(launch_spec_kick(L, P, ctx->S, Ttar, 1));
+    }
     std::swap(ctx->S.frc, ctx->S.frc_new);
     *lt = *lt + 1;
   }

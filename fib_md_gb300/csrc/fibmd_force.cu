@@ -30,55 +30,51 @@
 
 namespace fibmd {
 
-constexpr int kLegF = 9;  // ux uy uz rinv E g fx fy fz
-
-// Threads per block of the main force kernel: binary64 stages 12 legs x 9
-// doubles per thread (55 KB per 64 threads, 3 blocks per SM); binary32
-// stages floats (55 KB per 128 threads).
-template <bool MIXED>
-struct ForceBlock {
-  static constexpr int value = MIXED ? 128 : 64;
-};
-
-template <typename R, int BLOCK>
-struct LegSmem {
-  R* v;
-  int* j;
-  __device__ __forceinline__ R& at(int l, int f) {
-    return v[(l * kLegF + f) * BLOCK + threadIdx.x];
-  }
-  __device__ __forceinline__ int& idx(int l) { return j[l * BLOCK + threadIdx.x]; }
-};
-
 // 3-point Lagrange interpolation of the derivative table (itable2bd).
 // it = INT(ue/umax*(Ntable-1)) is the 0-based first stencil point.
 __device__ __forceinline__ double table_df(const DevParams& P, const double* __restrict__ tab,
                                            const double* __restrict__ tabu, double ue,
                                            int* err) {
-  int it = (int)(ue / P.umax * (double)(P.Ntable - 1));
+  const int it = (int)(ue / P.umax * (double)(P.Ntable - 1));
   if (it > P.tab_last) return 0.0;  // all three stencil entries are zero
   if (it + 1 > P.Ntable) {
     *err = 1;
     return 0.0;
   }
-  double d1 = ue - __ldg(&tabu[it]);
-  double d2 = ue - __ldg(&tabu[it + 1]);
-  double d3 = ue - __ldg(&tabu[it + 2]);
+  const double d1 = ue - __ldg(&tabu[it]);
+  const double d2 = ue - __ldg(&tabu[it + 1]);
+  const double d3 = ue - __ldg(&tabu[it + 2]);
   return 0.5 * d2 * d3 * __ldg(&tab[it]) - d1 * d3 * __ldg(&tab[it + 1]) +
          0.5 * d1 * d2 * __ldg(&tab[it + 2]);
 }
 
-// ---- main per-centre kernel ------------------------------------------------
-template <bool MIXED, bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(ForceBlock<MIXED>::value) k_force(DevParams P, DevState S) {
-  using R = typename std::conditional<MIXED, float, double>::type;
-  constexpr int BLOCK = ForceBlock<MIXED>::value;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  LegSmem<R, BLOCK> leg;
-  leg.v = reinterpret_cast<R*>(smem_raw);
-  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(R) * kMaxLegs * kLegF * BLOCK);
+// ---- binary64 per-centre kernel --------------------------------------------
+// Each thread stages up to kMaxLegs active legs (unit vector, 1/r, E, g and
+// a reaction accumulator: 9 doubles) in shared memory and evaluates every
+// unordered leg pair once: binary64 instructions are the scarce resource on
+// this GPU, so no term is computed twice.
+constexpr int kLegF64 = 9;   // ux uy uz rinv E g fx fy fz
+constexpr int kBlock64 = 64;
+constexpr int kLegF32 = 6;   // ux uy uz rinv E g
+constexpr int kBlock32 = 128;
+constexpr int kBatch = 8;    // neighbour gathers in flight per thread
 
-  const int i = blockIdx.x * BLOCK + threadIdx.x;
+template <typename R, int BLOCK, int F>
+struct LegSmem {
+  R* v;
+  int* j;
+  __device__ __forceinline__ R& at(int l, int f) { return v[(l * F + f) * BLOCK + threadIdx.x]; }
+  __device__ __forceinline__ int& idx(int l) { return j[l * BLOCK + threadIdx.x]; }
+};
+
+template <bool ENERGY, bool COUNT>
+__global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LegSmem<double, kBlock64, kLegF64> leg;
+  leg.v = reinterpret_cast<double*>(smem_raw);
+  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(double) * kMaxLegs * kLegF64 * kBlock64);
+
+  const int i = blockIdx.x * kBlock64 + threadIdx.x;
   if (i >= P.N) return;
   const int4 qi = S.posq[i];
   const int ti = qi.w & 0xff;
@@ -89,19 +85,24 @@ __global__ void __launch_bounds__(ForceBlock<MIXED>::value) k_force(DevParams P,
   const int ta = ti - 1;
 
   double fx = 0.0, fy = 0.0, fz = 0.0, ui = 0.0;
-  float mfx = 0.f, mfy = 0.f, mfz = 0.f, mui = 0.f;
-  int nl = 0;
-  int terr = 0;
+  int nl = 0, terr = 0;
   unsigned int cnt_pairs = 0, cnt_ang = 0;
 
-  for (int k = 0; k < n; k++) {
-    const int j = S.nbr_sw[(size_t)k * P.N + i];
-    const int4 qj = S.posq[j];
-    const float3 dq = qsep(qi, qj, P.qinvA);
-    const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-    if (r2f > P.pre3A2) continue;  // beyond the table support and 3-body cutoff
-    const int tb = (qj.w & 0xff) - 1;
-    if constexpr (!MIXED) {
+  for (int k0 = 0; k0 < n; k0 += kBatch) {
+    int jj[kBatch];
+    int4 qq[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) jj[u] = (k0 + u < n) ? S.nbr_sw[(size_t)(k0 + u) * P.N + i] : i;
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) qq[u] = S.posq[jj[u]];
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) {
+      if (k0 + u >= n) break;
+      const int j = jj[u];
+      const float3 dq = qsep(qi, qq[u], P.qinvA);
+      const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+      if (r2f > P.pre3A2) continue;  // beyond the table support and 3-body cutoff
+      const int tb = (qq[u].w & 0xff) - 1;
       const double4_32a pj = S.pos[j];
       const double dx = min_image(pi.x, pj.x, P.iLb[0], P.Lb[0]);
       const double dy = min_image(pi.y, pj.y, P.iLb[1], P.Lb[1]);
@@ -137,79 +138,39 @@ __global__ void __launch_bounds__(ForceBlock<MIXED>::value) k_force(DevParams P,
         }
         nl++;
       }
-    } else {
-      // binary32 in reduced units (Angstrom, eV); psi = 4, qsi = 0
-      const float rinv = rsqrtf(r2f);
-      const float r = r2f * rinv;
-      const float sg = P.sigA[ta][tb];
-      const float ue = r / sg;
-      const float cut = (float)P.cut3;
-      if (ue < cut) {
-        const float al = (float)P.al;
-        const float inv = 1.0f / (ue - al);
-        const float ex = expf(inv);
-        const float u2 = 1.0f / (ue * ue);
-        const float u4 = u2 * u2;
-        const float B = (float)P.B, A = (float)P.A;
-        // dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
-        const float dphi = A * ex * (-4.0f * B * u4 / ue - (B * u4 - 1.0f) * inv * inv);
-        const float c = -(dphi * rinv * (P.epsA[ta][tb] / sg));
-        mfx += c * dq.x;
-        mfy += c * dq.y;
-        mfz += c * dq.z;
-        if (COUNT) cnt_pairs++;
-        if (ENERGY) mui += 0.5f * P.epsA[ta][tb] * A * (B * u4 - 1.0f) * ex;
-        if (nl < kMaxLegs) {
-          const float gm = (float)P.gam;
-          leg.at(nl, 0) = dq.x * rinv;
-          leg.at(nl, 1) = dq.y * rinv;
-          leg.at(nl, 2) = dq.z * rinv;
-          leg.at(nl, 3) = rinv;
-          leg.at(nl, 4) = expf(gm * inv);
-          leg.at(nl, 5) = -gm * inv * inv / sg;
-          leg.at(nl, 6) = 0.f;
-          leg.at(nl, 7) = 0.f;
-          leg.at(nl, 8) = 0.f;
-          leg.idx(nl) = j | (tb << 30);
-        }
-        nl++;
-      }
     }
   }
 
   if (nl > kMaxLegs) {
-    // the direct kernel evaluates this centre's angle terms
-    int slot = atomicAdd(&S.sc->heavy_count, 1);
+    // the warp-per-centre kernel evaluates this centre's angle terms
+    const int slot = atomicAdd(&S.sc->heavy_count, 1);
     S.heavy_list[slot] = i;
   } else {
-    const R thrd = (R)P.thrd;
-    R cfx = 0, cfy = 0, cfz = 0, cu = 0;
+    const double thrd = P.thrd;
+    double cfx = 0, cfy = 0, cfz = 0, cu = 0;
     for (int a = 0; a < nl; a++) {
-      const R ax = leg.at(a, 0), ay = leg.at(a, 1), az = leg.at(a, 2);
-      const R ar = leg.at(a, 3), aE = leg.at(a, 4), ag = leg.at(a, 5);
+      const double ax = leg.at(a, 0), ay = leg.at(a, 1), az = leg.at(a, 2);
+      const double ar = leg.at(a, 3), aE = leg.at(a, 4), ag = leg.at(a, 5);
       const int tbA = (unsigned)leg.idx(a) >> 30;
-      R afx = 0, afy = 0, afz = 0;
+      double afx = 0, afy = 0, afz = 0, ae = 0;
       for (int b = a + 1; b < nl; b++) {
-        const R bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
-        const R br = leg.at(b, 3), bE = leg.at(b, 4), bg = leg.at(b, 5);
+        const double bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
+        const double br = leg.at(b, 3), bE = leg.at(b, 4), bg = leg.at(b, 5);
         const int tbB = (unsigned)leg.idx(b) >> 30;
-        R lp;
-        if constexpr (MIXED) lp = P.lepsA[ta][tbA][tbB];
-        else lp = P.leps[ta][tbA][tbB];
-        const R cs = ax * bx + ay * by + az * bz;
-        const R c3 = cs + thrd;
-        const R W = c3 * c3;
-        const R pref = lp * aE * bE;
-        const R s2 = (R)2 * c3;
+        const double cs = ax * bx + ay * by + az * bz;
+        const double c3 = cs + thrd;
+        const double W = c3 * c3;
+        const double pref = P.leps[ta][tbA][tbB] * aE * bE;
+        const double s2 = 2.0 * c3;
         // F_a = pref [W g_a p_a + 2(c+1/3)(p_b - c p_a)/r_a], p = unit(X_c - X_a)
-        const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
-        const R Fax = pref * (wa * ax + sa * bx);
-        const R Fay = pref * (wa * ay + sa * by);
-        const R Faz = pref * (wa * az + sa * bz);
-        const R wb = W * bg - s2 * cs * br, sb = s2 * br;
-        const R Fbx = pref * (wb * bx + sb * ax);
-        const R Fby = pref * (wb * by + sb * ay);
-        const R Fbz = pref * (wb * bz + sb * az);
+        const double wa = W * ag - s2 * cs * ar, sa = s2 * ar;
+        const double Fax = pref * (wa * ax + sa * bx);
+        const double Fay = pref * (wa * ay + sa * by);
+        const double Faz = pref * (wa * az + sa * bz);
+        const double wb = W * bg - s2 * cs * br, sb = s2 * br;
+        const double Fbx = pref * (wb * bx + sb * ax);
+        const double Fby = pref * (wb * by + sb * ay);
+        const double Fbz = pref * (wb * bz + sb * az);
         afx += Fax;
         afy += Fay;
         afz += Faz;
@@ -219,66 +180,174 @@ __global__ void __launch_bounds__(ForceBlock<MIXED>::value) k_force(DevParams P,
         cfx -= Fax + Fbx;
         cfy -= Fay + Fby;
         cfz -= Faz + Fbz;
-        if (ENERGY) cu += pref * W;
-        if (COUNT && pref != (R)0) cnt_ang++;
+        if (ENERGY) {
+          const double e = pref * W;
+          cu += e;
+          ae += e;
+          atomicAdd(&S.epot[leg.idx(b) & 0x3fffffff], e / 3.0);
+        }
+        if (COUNT && pref != 0.0) cnt_ang++;
       }
       leg.at(a, 6) += afx;
       leg.at(a, 7) += afy;
       leg.at(a, 8) += afz;
+      if (ENERGY && ae != 0.0) atomicAdd(&S.epot[leg.idx(a) & 0x3fffffff], ae / 3.0);
     }
-    // scatter leg reactions (binary64 accumulation)
-    const double conv = MIXED ? P.f_evA_to_N : 1.0;
-    for (int a = 0; a < nl; a++) {
-      const int j = leg.idx(a) & 0x3fffffff;
-      atomic_add3(S.frc_new, j, conv * (double)leg.at(a, 6), conv * (double)leg.at(a, 7),
-                  conv * (double)leg.at(a, 8));
-    }
-    if constexpr (MIXED) {
-      mfx += cfx;
-      mfy += cfy;
-      mfz += cfz;
-    } else {
-      fx += cfx;
-      fy += cfy;
-      fz += cfz;
-    }
-    if (ENERGY && nl > 1) {
-      // each angle term gives a third of its energy to each of its atoms
-      const double e3 = (MIXED ? P.e_eV_to_J : 1.0) * (double)cu / 3.0;
-      if (e3 != 0.0) {
-        ui += e3;
-        for (int a = 0; a < nl; a++) {
-          // a leg's share: sum over the terms it belongs to
-          double sh = 0.0;
-          for (int b = 0; b < nl; b++) {
-            if (b == a) continue;
-            const R cs = leg.at(a, 0) * leg.at(b, 0) + leg.at(a, 1) * leg.at(b, 1) +
-                         leg.at(a, 2) * leg.at(b, 2);
-            const R c3 = cs + thrd;
-            const int tbA = (unsigned)leg.idx(a) >> 30, tbB = (unsigned)leg.idx(b) >> 30;
-            R lp;
-            if constexpr (MIXED) lp = P.lepsA[ta][tbA][tbB];
-            else lp = P.leps[ta][tbA][tbB];
-            sh += (double)(lp * leg.at(a, 4) * leg.at(b, 4) * c3 * c3);
-          }
-          atomicAdd(&S.epot[leg.idx(a) & 0x3fffffff],
-                    (MIXED ? P.e_eV_to_J : 1.0) * sh / 3.0);
-        }
-      }
-    }
-  }
-  if constexpr (MIXED) {
-    fx += P.f_evA_to_N * (double)mfx;
-    fy += P.f_evA_to_N * (double)mfy;
-    fz += P.f_evA_to_N * (double)mfz;
-    if (ENERGY) ui += P.e_eV_to_J * (double)mui;
+    // each angle term gives a third of its energy to each of its atoms
+    if (ENERGY) ui += cu / 3.0;
+    for (int a = 0; a < nl; a++)
+      atomic_add3(S.frc_new, leg.idx(a) & 0x3fffffff, leg.at(a, 6), leg.at(a, 7), leg.at(a, 8));
+    fx += cfx;
+    fy += cfy;
+    fz += cfz;
   }
   atomic_add3(S.frc_new, i, fx, fy, fz);
   if (ENERGY && ui != 0.0) atomicAdd(&S.epot[i], ui);
   if (terr) atomicAdd(&S.sc->table_err, 1);
   if (COUNT) {
-    if (cnt_pairs) atomicAdd(&S.sc->counters[0], (unsigned long long)cnt_pairs);
-    if (cnt_ang) atomicAdd(&S.sc->counters[1], (unsigned long long)cnt_ang);
+    // one atomic per converged group of lanes
+    const unsigned m = __activemask();
+    const unsigned sp = __reduce_add_sync(m, cnt_pairs), sa = __reduce_add_sync(m, cnt_ang);
+    if ((threadIdx.x & 31) == __ffs(m) - 1) {
+      if (sp) atomicAdd(&S.sc->counters[0], (unsigned long long)sp);
+      if (sa) atomicAdd(&S.sc->counters[1], (unsigned long long)sa);
+    }
+  }
+}
+
+// ---- binary32 (mixed) per-centre kernel ------------------------------------
+// Separations come from the fixed-point shadow (binary32 with the precision
+// of the separation), arithmetic is binary32 in Angstrom/eV; per-thread
+// partial sums are binary32 over at most a few dozen terms, and every
+// cross-thread accumulation of the per-atom force is a binary64 atomic.
+// The leg pairs are evaluated as ordered pairs: each leg's reaction is summed
+// in registers over its row and scattered once, so the shared-memory stage
+// holds only 6 floats per leg (more resident warps for the gathers).
+template <bool ENERGY, bool COUNT>
+__global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState S) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  LegSmem<float, kBlock32, kLegF32> leg;
+  leg.v = reinterpret_cast<float*>(smem_raw);
+  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(float) * kMaxLegs * kLegF32 * kBlock32);
+
+  const int i = blockIdx.x * kBlock32 + threadIdx.x;
+  if (i >= P.N) return;
+  const int4 qi = S.posq[i];
+  const int ti = qi.w & 0xff;
+  if (ti >= 3 || ((qi.w >> 8) & FL_REMOVED)) return;
+  const int n = S.n_sw[i];
+  if (n == 0) return;
+  const int ta = ti - 1;
+  const float al = (float)P.al, cut = (float)P.cut3, gm = (float)P.gam;
+  const float Bc = (float)P.B, Ac = (float)P.A;
+
+  float fx = 0.f, fy = 0.f, fz = 0.f, ui = 0.f;
+  int nl = 0;
+  unsigned int cnt_pairs = 0, cnt_ang = 0;
+
+  for (int k0 = 0; k0 < n; k0 += kBatch) {
+    int jj[kBatch];
+    int4 qq[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) jj[u] = (k0 + u < n) ? S.nbr_sw[(size_t)(k0 + u) * P.N + i] : i;
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) qq[u] = S.posq[jj[u]];
+#pragma unroll
+    for (int u = 0; u < kBatch; u++) {
+      if (k0 + u >= n) break;
+      const float3 dq = qsep(qi, qq[u], P.qinvA);
+      const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+      if (r2f > P.pre3A2) continue;
+      const int tb = (qq[u].w & 0xff) - 1;
+      const float rinv = rsqrtf(r2f);
+      const float r = r2f * rinv;
+      const float sg = P.sigA[ta][tb];
+      const float ue = r / sg;
+      if (!(ue < cut)) continue;
+      const float inv = 1.0f / (ue - al);
+      const float ex = expf(inv);
+      const float u2 = 1.0f / (ue * ue);
+      const float u4 = u2 * u2;
+      // psi = 4, qsi = 0: dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
+      const float dphi = Ac * ex * (-4.0f * Bc * u4 / ue - (Bc * u4 - 1.0f) * inv * inv);
+      const float c = -(dphi * rinv * (P.epsA[ta][tb] / sg));
+      fx += c * dq.x;
+      fy += c * dq.y;
+      fz += c * dq.z;
+      if (COUNT) cnt_pairs++;
+      if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
+      const float E = expf(gm * inv);
+      // a leg whose exponential underflows in binary32 adds exactly zero
+      if (E > 0.f) {
+        if (nl < kMaxLegs) {
+          leg.at(nl, 0) = dq.x * rinv;
+          leg.at(nl, 1) = dq.y * rinv;
+          leg.at(nl, 2) = dq.z * rinv;
+          leg.at(nl, 3) = rinv;
+          leg.at(nl, 4) = E;
+          leg.at(nl, 5) = -gm * inv * inv / sg;
+          leg.idx(nl) = jj[u] | (tb << 30);
+        }
+        nl++;
+      }
+    }
+  }
+
+  const double conv = P.f_evA_to_N;
+  double ue_J = 0.0;
+  if (nl > kMaxLegs) {
+    const int slot = atomicAdd(&S.sc->heavy_count, 1);
+    S.heavy_list[slot] = i;
+  } else {
+    const float thrd = (float)P.thrd;
+    float cu = 0.f;
+    for (int a = 0; a < nl; a++) {
+      const float ax = leg.at(a, 0), ay = leg.at(a, 1), az = leg.at(a, 2);
+      const float ar = leg.at(a, 3), aE = leg.at(a, 4), ag = leg.at(a, 5);
+      const int ia = leg.idx(a);
+      const int tbA = (unsigned)ia >> 30;
+      float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+      for (int b = 0; b < nl; b++) {
+        if (b == a) continue;
+        const float bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
+        const int tbB = (unsigned)leg.idx(b) >> 30;
+        const float cs = ax * bx + ay * by + az * bz;
+        const float c3 = cs + thrd;
+        const float W = c3 * c3;
+        const float pref = P.lepsA[ta][tbA][tbB] * aE * leg.at(b, 4);
+        const float s2 = 2.0f * c3;
+        const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
+        afx += pref * (wa * ax + sa * bx);
+        afy += pref * (wa * ay + sa * by);
+        afz += pref * (wa * az + sa * bz);
+        if (ENERGY) ae += pref * W;
+        if (COUNT && b > a && pref != 0.f) cnt_ang++;
+      }
+      atomic_add3(S.frc_new, ia & 0x3fffffff, conv * (double)afx, conv * (double)afy,
+                  conv * (double)afz);
+      fx -= afx;
+      fy -= afy;
+      fz -= afz;
+      if (ENERGY) {
+        // leg a's share of its terms; the centre gets a third of each term
+        if (ae != 0.f) atomicAdd(&S.epot[ia & 0x3fffffff], P.e_eV_to_J * (double)ae / 3.0);
+        cu += ae;
+      }
+    }
+    if (ENERGY) ue_J = P.e_eV_to_J * (double)cu / 6.0;
+  }
+  atomic_add3(S.frc_new, i, conv * (double)fx, conv * (double)fy, conv * (double)fz);
+  if (ENERGY) {
+    const double e = P.e_eV_to_J * (double)ui + ue_J;
+    if (e != 0.0) atomicAdd(&S.epot[i], e);
+  }
+  if (COUNT) {
+    const unsigned m = __activemask();
+    const unsigned sp = __reduce_add_sync(m, cnt_pairs), sa = __reduce_add_sync(m, cnt_ang);
+    if ((threadIdx.x & 31) == __ffs(m) - 1) {
+      if (sp) atomicAdd(&S.sc->counters[0], (unsigned long long)sp);
+      if (sa) atomicAdd(&S.sc->counters[1], (unsigned long long)sa);
+    }
   }
 }
 
@@ -333,39 +402,83 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
   return true;
 }
 
-// Centres with more than kMaxLegs active legs: every leg pair, direct.
+// Centres with more than kMaxLegs active legs (compressed cascade regions):
+// one warp per centre. The lanes first compute every listed leg in binary64
+// and stage the active ones in shared memory, then split the leg pairs; leg
+// reactions are scattered with atomics, the centre's force is warp-reduced.
+constexpr int kHeavyWarps = 4;
+constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
+
 template <bool ENERGY>
-__global__ void k_force_heavy(DevParams P, DevState S) {
+__global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
+  __shared__ double sl[kHeavyWarps][6][kHeavyLegs];
+  __shared__ int sj[kHeavyWarps][kHeavyLegs];
+  __shared__ int snl[kHeavyWarps];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cnt = *((volatile int*)&S.sc->heavy_count);
-  for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
+  for (int h = blockIdx.x * kHeavyWarps + w; h < cnt; h += gridDim.x * kHeavyWarps) {
     const int c = S.heavy_list[h];
     const int tc = S.atype[c];
     const double4_32a pc = S.pos[c];
     const int n = S.n_sw[c];
+    if (lane == 0) snl[w] = 0;
+    __syncwarp();
+    for (int k = lane; k < n; k += 32) {
+      const int j = S.nbr_sw[(size_t)k * P.N + c];
+      const Leg64 L = make_leg(P, pc, S.pos[j], tc, S.atype[j]);
+      if (L.u < P.cut3) {
+        const int q = atomicAdd(&snl[w], 1);
+        const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
+        sl[w][0][q] = L.dx * ra;
+        sl[w][1][q] = L.dy * ra;
+        sl[w][2][q] = L.dz * ra;
+        sl[w][3][q] = ra;
+        sl[w][4][q] = exp(P.gam * ia);
+        sl[w][5][q] = -P.gam * ia * ia * L.isig;
+        sj[w][q] = j | (L.t << 30);
+      }
+    }
+    __syncwarp();
+    const int nl = snl[w];
     double fcx = 0, fcy = 0, fcz = 0, uc = 0;
-    for (int a = 0; a < n; a++) {
-      const int ja = S.nbr_sw[(size_t)a * P.N + c];
-      const Leg64 A = make_leg(P, pc, S.pos[ja], tc, S.atype[ja]);
-      if (!(A.u < P.cut3)) continue;
-      for (int b = a + 1; b < n; b++) {
-        const int jb = S.nbr_sw[(size_t)b * P.N + c];
-        const Leg64 B = make_leg(P, pc, S.pos[jb], tc, S.atype[jb]);
-        double f0[3], f1[3], f2[3], e;
-        if (!angle_term(P, tc, A, B, f0, f1, f2, &e)) continue;
-        fcx += f0[0];
-        fcy += f0[1];
-        fcz += f0[2];
-        atomic_add3(S.frc_new, ja, f1[0], f1[1], f1[2]);
-        atomic_add3(S.frc_new, jb, f2[0], f2[1], f2[2]);
+    for (int a = 0; a < nl; a++) {
+      for (int b = a + 1 + lane; b < nl; b += 32) {
+        const double ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
+        const double bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
+        const double ar = sl[w][3][a], br = sl[w][3][b];
+        const int ja = sj[w][a], jb = sj[w][b];
+        const double cs = ax * bx + ay * by + az * bz;
+        const double c3 = cs + P.thrd, W = c3 * c3, s2 = 2.0 * c3;
+        const double pref = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30] *
+                            sl[w][4][a] * sl[w][4][b];
+        const double wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
+        const double wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
+        const double Fax = pref * (wa * ax + sa * bx), Fay = pref * (wa * ay + sa * by),
+                     Faz = pref * (wa * az + sa * bz);
+        const double Fbx = pref * (wb * bx + sb * ax), Fby = pref * (wb * by + sb * ay),
+                     Fbz = pref * (wb * bz + sb * az);
+        atomic_add3(S.frc_new, ja & 0x3fffffff, Fax, Fay, Faz);
+        atomic_add3(S.frc_new, jb & 0x3fffffff, Fbx, Fby, Fbz);
+        fcx -= Fax + Fbx;
+        fcy -= Fay + Fby;
+        fcz -= Faz + Fbz;
         if (ENERGY) {
-          uc += e / 3.0;
-          atomicAdd(&S.epot[ja], e / 3.0);
-          atomicAdd(&S.epot[jb], e / 3.0);
+          const double e3 = pref * W / 3.0;
+          uc += e3;
+          atomicAdd(&S.epot[ja & 0x3fffffff], e3);
+          atomicAdd(&S.epot[jb & 0x3fffffff], e3);
         }
       }
     }
-    atomic_add3(S.frc_new, c, fcx, fcy, fcz);
-    if (ENERGY && uc != 0.0) atomicAdd(&S.epot[c], uc);
+    fcx = warp_sum(fcx);
+    fcy = warp_sum(fcy);
+    fcz = warp_sum(fcz);
+    if (ENERGY) uc = warp_sum(uc);
+    if (lane == 0) {
+      atomic_add3(S.frc_new, c, fcx, fcy, fcz);
+      if (ENERGY && uc != 0.0) atomicAdd(&S.epot[c], uc);
+    }
+    __syncwarp();
   }
 }
 
@@ -506,21 +619,21 @@ __global__ void k_force_begin(DevState S) {
 
 template <bool MIXED, bool ENERGY, bool COUNT>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
-  const size_t rsz = MIXED ? sizeof(float) : sizeof(double);
-  constexpr int BLOCK = ForceBlock<MIXED>::value;
-  const size_t smem = rsz * kMaxLegs * kLegF * BLOCK + sizeof(int) * kMaxLegs * BLOCK;
+  constexpr int BLOCK = MIXED ? kBlock32 : kBlock64;
+  const size_t smem = MIXED ? (sizeof(float) * kMaxLegs * kLegF32 + sizeof(int) * kMaxLegs) * BLOCK
+                            : (sizeof(double) * kMaxLegs * kLegF64 + sizeof(int) * kMaxLegs) * BLOCK;
+  auto kern = MIXED ? k_force_mixed<ENERGY, COUNT> : k_force_fp64<ENERGY, COUNT>;
   static bool attr_set = false;
   if (!attr_set) {
-    cudaFuncSetAttribute(k_force<MIXED, ENERGY, COUNT>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     attr_set = true;
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
-  k_force<MIXED, ENERGY, COUNT><<<(P.N + BLOCK - 1) / BLOCK, BLOCK, smem, L.stream>>>(P, S);
+  kern<<<(P.N + BLOCK - 1) / BLOCK, BLOCK, smem, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
-  k_force_heavy<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
+  k_force_heavy<ENERGY><<<side, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
   return cudaGetLastError();
 }

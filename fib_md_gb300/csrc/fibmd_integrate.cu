@@ -24,15 +24,15 @@ __device__ __forceinline__ bool ref_side_atom(const DevParams& P, double x, doub
 
 // Marks an atom displaced by at least half the list skin since the last
 // build (its angle terms may include stale-list terms, ref mode) and returns
-// the squared displacement (spec-mode rebuild trigger).
-__device__ __forceinline__ double track_displacement(const DevParams& P, const DevState& S,
-                                                     int i, double x, double y, double z) {
-  const double4_32a b = S.pos_build[i];
-  const double dx = min_image(x, b.x, P.iLb[0], P.Lb[0]);
-  const double dy = min_image(y, b.y, P.iLb[1], P.Lb[1]);
-  const double dz = min_image(z, b.z, P.iLb[2], P.Lb[2]);
-  const double d2 = dx * dx + dy * dy + dz * dz;
-  if (P.mode == FIBMD_MODE_REF && d2 >= P.disp_fast2 && !S.fast_flag[i]) {
+// the squared displacement in A^2 (spec-mode rebuild trigger). The
+// displacement is taken between fixed-point positions, whose wrapping
+// difference is the minimum image; its binary32 error (~1e-7 A) is far
+// inside the 1% margin of the threshold.
+__device__ __forceinline__ float track_displacement(const DevParams& P, const DevState& S,
+                                                    int i, const int4& q) {
+  const float3 d = qsep(q, S.posq_build[i], P.qinvA);
+  const float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
+  if (P.mode == FIBMD_MODE_REF && d2 >= P.disp_fastA2 && !S.fast_flag[i]) {
     S.fast_flag[i] = 1;
     const int slot = atomicAdd(&S.sc->fast_count, 1);
     S.fast_list[slot] = i;
@@ -40,7 +40,7 @@ __device__ __forceinline__ double track_displacement(const DevParams& P, const D
   return d2;
 }
 
-__device__ __forceinline__ void store_posq(const DevParams& P, const DevState& S, int i,
+__device__ __forceinline__ int4 store_posq(const DevParams& P, const DevState& S, int i,
                                            double x, double y, double z, uint32_t fl) {
   int4 q;
   q.x = (int)fixq(x, P.qscale[0]);
@@ -48,17 +48,19 @@ __device__ __forceinline__ void store_posq(const DevParams& P, const DevState& S
   q.z = (int)fixq(z, P.qscale[2]);
   q.w = (int)(uint8_t)S.atype[i] | (int)(fl << 8);
   S.posq[i] = q;
+  return q;
 }
 
 static int red_blocks(const DevParams& P) {
-  int nb = (P.N + kRedThreads * 4 - 1) / (kRedThreads * 4);
+  int nb = (P.N + kRedThreads - 1) / kRedThreads;
   if (nb < 1) nb = 1;
   if (nb > kMaxRedBlocks) nb = kMaxRedBlocks;
   return nb;
 }
 
 // ---- controlsidetemp: sum m v^2 and count over edge atoms (atype < 3) -----
-__global__ void __launch_bounds__(kRedThreads) k_side_reduce(DevParams P, DevState S) {
+__global__ void __launch_bounds__(kRedThreads) k_side_reduce(DevParams P, DevState S, double Ts,
+                                                             double Tau, double Ttar) {
   double v[2] = {0.0, 0.0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
     if (S.atype[i] >= 3) continue;
@@ -72,11 +74,19 @@ __global__ void __launch_bounds__(kRedThreads) k_side_reduce(DevParams P, DevSta
   if (grid_finish<2, false>(v, S.partials, &S.sc->ticket[0])) {
     S.sc->side_sum = v[0];
     S.sc->side_cnt = v[1];
+    double sf = 1.0;
+    if (v[1] > 0.0) {
+      // temp.f90:56-60, evaluated once for all edge atoms
+      const double ts = v[0] / 3. / v[1] / P.kB;
+      sf = sqrt(1. + Ts / Tau * (Ttar / ts - 1.));
+    }
+    S.sc->side_s = sf;
   }
 }
 
-cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S) {
-  k_side_reduce<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S);
+cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S,
+                               double Ts, double Tau, double Ttar) {
+  k_side_reduce<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S, Ts, Tau, Ttar);
   return cudaGetLastError();
 }
 
@@ -127,27 +137,22 @@ cudaError_t launch_temperature(const Launch& L, const DevParams& P, const DevSta
 }
 
 // ---- drift: edge thermostat, X += V Ts + F Ts^2/(2m), freeze, rebox --------
-__global__ void __launch_bounds__(256) k_drift(DevParams P, DevState S, double Ts, double Tau,
-                                               double Ttar, int side) {
+__global__ void __launch_bounds__(256) k_drift(DevParams P, DevState S, double Ts, int side) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
   double4_32a x = S.pos[i];
   double4_32a v = S.vel[i];
-  if (side && S.atype[i] < 3) {
-    const double cnt = S.sc->side_cnt;
-    if (cnt > 0.0 && ref_side_atom(P, x.x, x.y, x.z)) {
-      const double ts = S.sc->side_sum / 3. / cnt / P.kB;
-      const double s = sqrt(1. + Ts / Tau * (Ttar / ts - 1.));
-      v.x = s * v.x;
-      v.y = s * v.y;
-      v.z = s * v.z;
-    }
+  if (side && S.atype[i] < 3 && ref_side_atom(P, x.x, x.y, x.z)) {
+    const double s = S.sc->side_s;
+    v.x = s * v.x;
+    v.y = s * v.y;
+    v.z = s * v.z;
   }
   const double4_32a f = S.frc[i];
-  const double m = S.mass[i];
-  x.x = x.x + v.x * Ts + 0.5 * f.x * Ts * Ts / m;
-  x.y = x.y + v.y * Ts + 0.5 * f.y * Ts * Ts / m;
-  x.z = x.z + v.z * Ts + 0.5 * f.z * Ts * Ts / m;
+  const double c = 0.5 * Ts * Ts * S.inv_mass[i];
+  x.x = x.x + v.x * Ts + c * f.x;
+  x.y = x.y + v.y * Ts + c * f.y;
+  x.z = x.z + v.z * Ts + c * f.z;
   const uint32_t fl = S.flags[i];
   if (fl & FL_FROZEN) {
     const double4_32a xi = S.xi[i];
@@ -158,19 +163,20 @@ __global__ void __launch_bounds__(256) k_drift(DevParams P, DevState S, double T
     v.y = 0.;
     v.z = 0.;
   }
-  // rebox: MOD(X + 2 Lb, Lb); fmod is exact, as Fortran's MOD of reals
-  x.x = fmod(x.x + 2. * P.Lb[0], P.Lb[0]);
-  x.y = fmod(x.y + 2. * P.Lb[1], P.Lb[1]);
-  x.z = fmod(x.z + 2. * P.Lb[2], P.Lb[2]);
+  x.x = rebox1(x.x, P.Lb[0]);
+  x.y = rebox1(x.y, P.Lb[1]);
+  x.z = rebox1(x.z, P.Lb[2]);
   S.pos[i] = x;
   S.vel[i] = v;
-  store_posq(P, S, i, x.x, x.y, x.z, fl);
-  track_displacement(P, S, i, x.x, x.y, x.z);
+  const int4 q = store_posq(P, S, i, x.x, x.y, x.z, fl);
+  track_displacement(P, S, i, q);
 }
 
 cudaError_t launch_drift(const Launch& L, const DevParams& P, const DevState& S, double Ts,
                          double Tau, double Ttar, int side_thermo) {
-  k_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ts, Tau, Ttar, side_thermo);
+  (void)Tau;
+  (void)Ttar;
+  k_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ts, side_thermo);
   return cudaGetLastError();
 }
 
@@ -199,8 +205,8 @@ __global__ void __launch_bounds__(256) k_park(DevParams P, DevState S) {
   S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
   if (moved) {
     S.pos[i] = x;
-    store_posq(P, S, i, x.x, x.y, x.z, S.flags[i]);
-    track_displacement(P, S, i, x.x, x.y, x.z);
+    const int4 q = store_posq(P, S, i, x.x, x.y, x.z, S.flags[i]);
+    track_displacement(P, S, i, q);
   }
 }
 
@@ -216,10 +222,10 @@ __global__ void __launch_bounds__(256) k_kick(DevParams P, DevState S, double Ts
   double4_32a v = S.vel[i];
   const double4_32a f = S.frc[i];
   const double4_32a g = S.frc_new[i];
-  const double m = S.mass[i];
-  v.x = v.x + 0.5 * (f.x + g.x) * Ts / m;
-  v.y = v.y + 0.5 * (f.y + g.y) * Ts / m;
-  v.z = v.z + 0.5 * (f.z + g.z) * Ts / m;
+  const double c = 0.5 * Ts * S.inv_mass[i];
+  v.x = v.x + c * (f.x + g.x);
+  v.y = v.y + c * (f.y + g.y);
+  v.z = v.z + c * (f.z + g.z);
   S.vel[i] = v;
 }
 
@@ -254,8 +260,7 @@ cudaError_t launch_ke_max(const Launch& L, const DevParams& P, const DevState& S
 __global__ void k_track_all(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
-  const double4_32a x = S.pos[i];
-  track_displacement(P, S, i, x.x, x.y, x.z);
+  track_displacement(P, S, i, S.posq[i]);
 }
 
 cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S) {
@@ -314,7 +319,7 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z, and the rebuild trigger at half the list skin.
-__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, double Ttar) {
+__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const double dt = ((volatile DevScalars*)S.sc)->dt;
   bool trig = false;
@@ -324,20 +329,16 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, dou
       double4_32a x = S.pos[i];
       double4_32a v = S.vel[i];
       if (fl & FL_THERMO) {
-        const double cnt = S.sc->thermo_cnt;
-        const double T = cnt > 0.0 ? S.sc->thermo_sum / 3. / cnt / P.kB : 0.0;
-        if (T > 0.0) {
-          const double s = sqrt(1. + dt / P.tau_spec * (Ttar / T - 1.));
-          v.x *= s;
-          v.y *= s;
-          v.z *= s;
-        }
+        const double s = S.sc->thermo_s;
+        v.x *= s;
+        v.y *= s;
+        v.z *= s;
       }
       const double4_32a f = S.frc[i];
-      const double m = S.mass[i];
-      x.x = x.x + v.x * dt + 0.5 * f.x * dt * dt / m;
-      x.y = x.y + v.y * dt + 0.5 * f.y * dt * dt / m;
-      x.z = x.z + v.z * dt + 0.5 * f.z * dt * dt / m;
+      const double c = 0.5 * dt * dt * S.inv_mass[i];
+      x.x = x.x + v.x * dt + c * f.x;
+      x.y = x.y + v.y * dt + c * f.y;
+      x.z = x.z + v.z * dt + c * f.z;
       if (fl & FL_FROZEN) {
         const double4_32a xi = S.xi[i];
         x.x = xi.x;
@@ -345,9 +346,11 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, dou
         x.z = xi.z;
         v.x = v.y = v.z = 0.0;
       }
-      x.x = fmod(x.x + 2. * P.Lb[0], P.Lb[0]);
-      x.y = fmod(x.y + 2. * P.Lb[1], P.Lb[1]);
-      x.z = fmod(x.z + 2. * P.Lb[2], P.Lb[2]);
+      // spec mode has no bit-compatibility constraint with the reference's
+      // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped
+      x.x = x.x < 0.0 ? x.x + P.Lb[0] : (x.x >= P.Lb[0] ? x.x - P.Lb[0] : x.x);
+      x.y = x.y < 0.0 ? x.y + P.Lb[1] : (x.y >= P.Lb[1] ? x.y - P.Lb[1] : x.y);
+      x.z = x.z < 0.0 ? x.z + P.Lb[2] : (x.z >= P.Lb[2] ? x.z - P.Lb[2] : x.z);
       if (P.remove_z > 0.0 && x.z > P.remove_z && S.atype[i] < 3) {
         fl |= FL_REMOVED;
         S.flags[i] = fl;
@@ -357,8 +360,8 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, dou
       }
       S.pos[i] = x;
       S.vel[i] = v;
-      store_posq(P, S, i, x.x, x.y, x.z, fl);
-      if (track_displacement(P, S, i, x.x, x.y, x.z) >= P.disp_fast2) trig = true;
+      const int4 q = store_posq(P, S, i, x.x, x.y, x.z, fl);
+      if (track_displacement(P, S, i, q) >= P.disp_fastA2) trig = true;
     }
   }
   if (__syncthreads_or(trig) && threadIdx.x == 0) S.sc->need_rebuild = 1;
@@ -366,79 +369,80 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S, dou
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
                               double Ttar) {
-  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, Ttar);
+  (void)Ttar;
+  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S);
   return cudaGetLastError();
 }
 
 // Kick (apply != 0) followed by the reductions the next step needs: the
 // largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
-// thermostat layer's sum m v^2 and count. The last block also advances the
-// device time by the step just taken and installs the next dt.
-__global__ void __launch_bounds__(kRedThreads) k_spec_kick(DevParams P, DevState S, int apply) {
+// thermostat layer's sum m v^2 and count. Warps reduce in registers and add
+// to device accumulators (the max through the bit order of non-negative
+// doubles); k_spec_finalize then derives dt and the Berendsen factor.
+__global__ void __launch_bounds__(256) k_spec_kick(DevParams P, DevState S, int apply) {
   const double dt = ((volatile DevScalars*)S.sc)->dt;
-  double sums[2] = {0.0, 0.0};
-  double vmax2[1] = {0.0};
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < P.N; i += gridDim.x * blockDim.x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double v2 = 0.0, ts = 0.0, tc = 0.0;
+  if (i < P.N) {
     const uint32_t fl = S.flags[i];
-    if (fl & FL_REMOVED) continue;
-    double4_32a v = S.vel[i];
-    if (apply) {
-      const double4_32a f = S.frc[i];
-      const double4_32a g = S.frc_new[i];
-      const double m = S.mass[i];
-      v.x = v.x + 0.5 * (f.x + g.x) * dt / m;
-      v.y = v.y + 0.5 * (f.y + g.y) * dt / m;
-      v.z = v.z + 0.5 * (f.z + g.z) * dt / m;
-      S.vel[i] = v;
+    if (!(fl & FL_REMOVED)) {
+      double4_32a v = S.vel[i];
+      if (apply) {
+        const double4_32a f = S.frc[i];
+        const double4_32a g = S.frc_new[i];
+        const double c = 0.5 * dt * S.inv_mass[i];
+        v.x = v.x + c * (f.x + g.x);
+        v.y = v.y + c * (f.y + g.y);
+        v.z = v.z + c * (f.z + g.z);
+        S.vel[i] = v;
+      }
+      v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+      if ((fl & FL_THERMO) && S.atype[i] < 3) {
+        ts = S.mass[i] * v2;
+        tc = 1.0;
+      }
     }
-    const double v2 = v.x * v.x + v.y * v.y + v.z * v.z;
-    vmax2[0] = fmax(vmax2[0], v2);
-    if ((fl & FL_THERMO) && S.atype[i] < 3) {
-      sums[0] += S.mass[i] * v2;
-      sums[1] += 1.0;
+  }
+  v2 = warp_max(v2);
+  ts = warp_sum(ts);
+  tc = warp_sum(tc);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&S.sc->acc_vmax2_bits, (unsigned long long)__double_as_longlong(v2));
+    if (tc > 0.0) {
+      atomicAdd(&S.sc->acc_tsum, ts);
+      atomicAdd(&S.sc->acc_tcnt, tc);
     }
   }
-  vmax2[0] = block_max(vmax2[0]);
-  block_sum<2>(sums);
-  double all[3] = {sums[0], sums[1], vmax2[0]};
-  // grid_finish sums; the max travels separately through its own partials
-  __shared__ bool last;
-  if (threadIdx.x == 0) {
-    S.partials[0 * kMaxRedBlocks + blockIdx.x] = all[0];
-    S.partials[1 * kMaxRedBlocks + blockIdx.x] = all[1];
-    S.partials[2 * kMaxRedBlocks + blockIdx.x] = all[2];
-    __threadfence();
-    last = atomicAdd(&S.sc->ticket[5], 1u) == gridDim.x - 1;
+}
+
+__global__ void k_spec_finalize(DevParams P, DevState S, int apply, double Ttar) {
+  DevScalars* sc = S.sc;
+  const double mx = __longlong_as_double((long long)sc->acc_vmax2_bits);
+  const double tsum = sc->acc_tsum, tcnt = sc->acc_tcnt;
+  sc->acc_vmax2_bits = 0ull;
+  sc->acc_tsum = 0.0;
+  sc->acc_tcnt = 0.0;
+  sc->thermo_sum = tsum;
+  sc->thermo_cnt = tcnt;
+  sc->vmax2 = mx;
+  if (apply) sc->time += sc->dt;
+  const double vm = sqrt(mx);
+  double nd = P.dt_max;
+  if (vm > 0.0 && P.dx_max / vm < nd) nd = P.dx_max / vm;
+  sc->dt = nd;
+  // Berendsen factor of the thermostat layer for the next step
+  double sf = 1.0;
+  if (tcnt > 0.0) {
+    const double T = tsum / 3. / tcnt / P.kB;
+    if (T > 0.0) sf = sqrt(1. + nd / P.tau_spec * (Ttar / T - 1.));
   }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  double acc[2] = {0.0, 0.0};
-  double mx = 0.0;
-  for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-    acc[0] += ((volatile double*)S.partials)[b];
-    acc[1] += ((volatile double*)S.partials)[kMaxRedBlocks + b];
-    mx = fmax(mx, ((volatile double*)S.partials)[2 * kMaxRedBlocks + b]);
-  }
-  block_sum<2>(acc);
-  mx = block_max(mx);
-  if (threadIdx.x == 0) {
-    S.sc->thermo_sum = acc[0];
-    S.sc->thermo_cnt = acc[1];
-    S.sc->vmax2 = mx;
-    if (apply) S.sc->time += dt;
-    const double vm = sqrt(mx);
-    double nd = P.dt_max;
-    if (vm > 0.0 && P.dx_max / vm < nd) nd = P.dx_max / vm;
-    S.sc->dt = nd;
-    S.sc->ticket[5] = 0u;
-  }
+  sc->thermo_s = sf;
 }
 
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply) {
-  (void)Ttar;
-  k_spec_kick<<<red_blocks(P), kRedThreads, 0, L.stream>>>(P, S, apply);
+  k_spec_kick<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, apply);
+  k_spec_finalize<<<1, 1, 0, L.stream>>>(P, S, apply, Ttar);
   return cudaGetLastError();
 }
 

@@ -2,14 +2,15 @@
 // kernels of the FIB_MD GB300 backend.
 //
 // HBM layout (one context, N atoms, 0-based index = Fortran index - 1):
-//   pos, vel, frc, frc_new, xi, pos_build : double4_32a[N]  (x, y, z, unused)
+//   pos, vel, frc, frc_new, xi : double4_32a[N]  (x, y, z, unused)
 //   posq      : int4[N]   fixed-point positions, x = round(x/Lb * 2^32) mod
 //               2^32, w = atype | flags << 8. Differences of two fixed-point
 //               coordinates wrap modulo 2^32, which is the minimum image, and
 //               convert to binary32 with the precision of the separation
 //               itself (not of the absolute coordinate).
 //   mass      : double[N];  atype : int8[N];  flags : uint32[N]
-//   cells     : cell_start[ncell+1], cell_atoms[N] (counting sort by cell)
+//   cells     : cell_start[ncell+1], cell_atoms[N] and posq_cell[N] (counting
+//               sort by cell; posq_cell streams a cell's candidates)
 //   nbr_sw    : int[max_sw * N], slot-major (nbr_sw[k*N + i]) so a warp of
 //               consecutive centres reads one coalesced row per slot
 //   mol_pairs : int2[cap] full Moliere pair list (both orders)
@@ -58,6 +59,7 @@ struct DevParams {
   double umax;
   // stale-list bookkeeping
   double disp_fast2;  // squared displacement (m^2) that marks an atom fast
+  float disp_fastA2;  // the same in A^2
   // mixed precision, reduced units (A, eV)
   float epsA[2][2], sigA[2][2], lepsA[2][2][2];
   float molKA[3][3];       // ie0*Zi*Zj*ec*ec in eV*A
@@ -80,6 +82,8 @@ struct DevParams {
 struct DevScalars {
   double side_sum;     // controlsidetemp: sum m v^2 over edge atoms
   double side_cnt;     //                  number of edge atoms
+  double side_s;       //                  its Berendsen factor (1 if none)
+  double thermo_s;     // spec: Berendsen factor of the thermostat layer
   double temp;         // temperature() of the current velocities
   double ke_max;       // calc_atm: max 0.5 m v^2 / ec
   double vmax2;        // spec: max |v|^2
@@ -99,6 +103,11 @@ struct DevScalars {
   int nan_flag;
   int need_rebuild;
   int removed_count;
+  int nonempty_count;
+  unsigned long long rebuilds;  // list builds since creation
+  // spec-mode kick accumulators (zeroed by the finalizer after use)
+  unsigned long long acc_vmax2_bits;  // max |v|^2 as the bits of a double >= 0
+  double acc_tsum, acc_tcnt;
   unsigned int ticket[8];
   unsigned long long counters[4];
 };
@@ -110,16 +119,19 @@ struct DevState {
   double4_32a* frc;      // F (previous step)
   double4_32a* frc_new;  // Fp (this step)
   double4_32a* xi;
-  double4_32a* pos_build;
   int4* posq;
+  int4* posq_build;  // fixed-point positions at the last list build
   double* mass;
+  double* inv_mass;
   int8_t* atype;
   uint32_t* flags;
   // cells
   int* cell_count;
   int* cell_start;
   int* cell_atoms;
+  int4* posq_cell;   // posq in cell order (filled with cell_atoms)
   int* atom_cell;
+  int* nonempty;     // cells holding at least one atom (build order)
   int* scan_blocks;
   // lists
   int* nbr_sw;
@@ -158,6 +170,22 @@ __device__ __forceinline__ double min_image(double xi, double xj, double iLb,
                                             double Lb) {
   double d = xi - xj;
   return d - round(d * iLb) * Lb;
+}
+
+// The reference's rebox, MOD(x + 2 Lb, Lb). Fortran's MOD of reals is
+// exact (fmod); for a = x + 2Lb in [Lb, 3Lb) the subtraction of Lb or 2Lb
+// is exact too (Sterbenz), so this returns fmod's bits at a fraction of its
+// binary64 instructions and falls back to fmod outside that range.
+__device__ __forceinline__ double rebox1(double x, double L) {
+  const double a = x + 2.0 * L;
+  const double L2 = 2.0 * L;
+  if (a >= L2) {
+    const double r = a - L2;
+    if (r < L) return r;
+  } else if (a >= L) {
+    return a - L;
+  }
+  return fmod(a, L);
 }
 
 __device__ __forceinline__ unsigned int fixq(double x, double qscale) {
@@ -286,7 +314,8 @@ cudaError_t launch_count_triplets(const Launch& L, const DevParams& P, const Dev
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
                          bool energy, bool count);
 // fibmd_integrate.cu
-cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S);
+cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S,
+                               double Ts, double Tau, double Ttar);
 cudaError_t launch_adjust_and_temp(const Launch& L, const DevParams& P, const DevState& S,
                                    double Ts, double Tau, double Ttar);
 cudaError_t launch_drift(const Launch& L, const DevParams& P, const DevState& S, double Ts,
@@ -303,5 +332,9 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
                               double Ttar);
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
+// fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
+cudaError_t launch_set_rebuild_cond(cudaStream_t s, DevScalars* sc,
+                                    cudaGraphConditionalHandle h);
+cudaError_t launch_loop_ctl(cudaStream_t s, int* remaining, cudaGraphConditionalHandle h);
 
 }  // namespace fibmd

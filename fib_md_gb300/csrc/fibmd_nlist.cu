@@ -48,27 +48,47 @@ __global__ void k_build_begin(DevParams P, DevState S, int from_flag) {
     S.sc->overflow_mol = 0;
     S.sc->cell_oob = 0;
     S.sc->disp_max2 = 0.0;
+    S.sc->nonempty_count = 0;
   }
 }
 
 // atomcell (nlist.f90:28-30): Icell = INT((X - FLOOR(X*iLb)*Lb)/h) + 1.
+// The cell along an axis is floor(x nc / Lb), which the fixed-point shadow
+// q = round(x 2^32 / Lb) gives as (q nc) >> 32 with integer arithmetic. The
+// two agree except within ~nc 2^-33 of a cell boundary; there (fraction
+// within 1e-6 of a boundary) the reference's binary64 formula decides, so
+// the cell of every atom is the reference's.
+__device__ __forceinline__ int ref_cell(const DevParams& P, double x, int d) {
+  const double fl = floor(__dmul_rn(x, P.iLb[d]));
+  const double t = __ddiv_rn(__dsub_rn(x, __dmul_rn(fl, P.Lb[d])), P.hcell[d]);
+  return (int)t;
+}
+
 __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
-  if (S.flags[i] & FL_REMOVED) {
+  const int4 q = S.posq[i];
+  if ((q.w >> 8) & FL_REMOVED) {
     S.atom_cell[i] = -1;
+    S.n_sw[i] = 0;
+    S.posq_build[i] = q;
+    S.fast_flag[i] = 0;
     return;
   }
-  double4_32a p = S.pos[i];
-  double x[3] = {p.x, p.y, p.z};
+  const unsigned qq[3] = {(unsigned)q.x, (unsigned)q.y, (unsigned)q.z};
+  constexpr unsigned kGuard = 4295u;  // 1e-6 of a cell, in units of 2^-32
   int ic[3];
   bool oob = false;
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    double fl = floor(__dmul_rn(x[d], P.iLb[d]));
-    double t = __ddiv_rn(__dsub_rn(x[d], __dmul_rn(fl, P.Lb[d])), P.hcell[d]);
-    int c = (int)t;  // 0-based (the reference adds 1)
+    const unsigned long long t = (unsigned long long)qq[d] * (unsigned long long)P.nc[d];
+    int c = (int)(t >> 32);
+    const unsigned frac = (unsigned)t;
+    if (frac < kGuard || frac > 0xffffffffu - kGuard) {
+      const double4_32a p = S.pos[i];
+      c = ref_cell(P, d == 0 ? p.x : d == 1 ? p.y : p.z, d);
+    }
     if (c < 0 || c >= P.nc[d]) {
       oob = true;
       c = c < 0 ? 0 : P.nc[d] - 1;
@@ -76,9 +96,9 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
     ic[d] = c;
   }
   if (oob) atomicAdd(&S.sc->cell_oob, 1);
-  int cell = ic[0] + P.nc[0] * (ic[1] + P.nc[1] * ic[2]);
+  const int cell = ic[0] + P.nc[0] * (ic[1] + P.nc[1] * ic[2]);
   S.atom_cell[i] = cell;
-  atomicAdd(&S.cell_count[cell], 1);
+  if (atomicAdd(&S.cell_count[cell], 1) == 0) S.nonempty[atomicAdd(&S.sc->nonempty_count, 1)] = cell;
 }
 
 // Exclusive scan of cell_count (ncell+1 entries) into cell_start.
@@ -163,104 +183,146 @@ __global__ void k_scan_add(DevParams P, DevState S, int from_flag) {
 
 __global__ void k_cell_fill(DevParams P, DevState S, int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
-  int c = S.atom_cell[i];
+  const int c = S.atom_cell[i];
   if (c < 0) return;
-  int slot = S.cell_start[c] + atomicAdd(&S.cell_count[c], 1);
+  const int slot = S.cell_start[c] + atomicAdd(&S.cell_count[c], 1);
   S.cell_atoms[slot] = i;
-}
-
-// Order each cell's members by atom index so list order (and so the force
-// summation order) does not depend on atomic scheduling.
-__global__ void k_cell_order(DevParams P, DevState S, int from_flag) {
-  if (rebuild_skipped(S, from_flag)) return;
-  int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= P.ncell) return;
-  int b = S.cell_start[c], e = S.cell_start[c + 1];
-  for (int a = b + 1; a < e; a++) {
-    int v = S.cell_atoms[a];
-    int q = a - 1;
-    while (q >= b && S.cell_atoms[q] > v) {
-      S.cell_atoms[q + 1] = S.cell_atoms[q];
-      q--;
-    }
-    S.cell_atoms[q + 1] = v;
-  }
+  S.posq_cell[slot] = S.posq[i];
 }
 
 // ---- pair lists (si_nlistG pair loop, si.f90:130-189) ---------------------
-__global__ void __launch_bounds__(128) k_build_pairs(DevParams P, DevState S, int from_flag) {
-  if (rebuild_skipped(S, from_flag)) return;
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.N) return;
-  int ci = S.atom_cell[i];
-  S.pos_build[i] = S.pos[i];
-  S.fast_flag[i] = 0;
-  if (ci < 0) {
-    S.n_sw[i] = 0;
-    return;
+// One warp per non-empty cell. The warp stages the candidates of the
+// 27-cell stencil (9 rows of three x-adjacent cells, each row one
+// contiguous range of the cell-sorted arrays when it does not wrap) in
+// shared memory with coalesced loads, then tests every home atom of the
+// cell against them, 32 candidates at a time; accepted SW neighbours are
+// compacted into the home atom's list slots with a ballot and prefix count.
+constexpr int kBuildWarps = 4;
+constexpr int kCand = 256;   // staged candidates per warp (flushed when full)
+constexpr int kHome = 64;    // home atoms handled per pass over the stencil
+
+struct BuildStage {
+  int4 q[kBuildWarps][kCand];
+  int j[kBuildWarps][kCand];
+  int n[kBuildWarps][kHome];
+};
+
+__device__ __forceinline__ bool pair_in_list(const DevParams& P, const DevState& S, int i,
+                                             const int4& qi, int j, const int4& qj, bool* sw) {
+  const int ti = qi.w & 0xff, tj = qj.w & 0xff;
+  *sw = (ti > tj ? ti : tj) < 3;
+  if (j == i) return false;
+  const float3 d = qsep(qi, qj, P.qinvA);
+  const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
+  if (r2f > (*sw ? P.pre_sw2A : P.pre_mol2A)) return false;
+  if (r2f < (*sw ? P.acc_sw2A : P.acc_mol2A)) return true;
+  // within 1e-4 of the radius: the reference's binary64 test decides
+  const double4_32a pi = S.pos[i], pj = S.pos[j];
+  const double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
+  const double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
+  const double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
+  const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
+  return r2 < (*sw ? P.rv2 : P.rv2lj);
+}
+
+// Tests home atoms [h0, h1) against the K staged candidates.
+__device__ __forceinline__ void test_staged(const DevParams& P, const DevState& S,
+                                            BuildStage& st, int w, int lane, int h0, int h1,
+                                            int K) {
+  for (int h = h0; h < h1; h++) {
+    const int i = S.cell_atoms[h];
+    const int4 qi = S.posq_cell[h];
+    int n = st.n[w][h - h0];
+    for (int k0 = 0; k0 < K; k0 += 32) {
+      const int k = k0 + lane;
+      bool sw = true, in = false;
+      int j = -1;
+      if (k < K) {
+        j = st.j[w][k];
+        in = pair_in_list(P, S, i, qi, j, st.q[w][k], &sw);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, in && sw);
+      if (in && sw) {
+        const int slot = n + __popc(m & ((1u << lane) - 1u));
+        if (slot < P.max_sw) S.nbr_sw[(size_t)slot * P.N + i] = j;
+      } else if (in) {
+        const int slot = atomicAdd(&S.sc->mol_count, 1);
+        if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
+      }
+      n += __popc(m);
+    }
+    if (lane == 0) st.n[w][h - h0] = n;
   }
-  const int4 qi = S.posq[i];
-  const double4_32a pi = S.pos[i];
-  const int ti = (int)S.atype[i];
-  int cx = ci % P.nc[0];
-  int cy = (ci / P.nc[0]) % P.nc[1];
-  int cz = ci / (P.nc[0] * P.nc[1]);
-  int n = 0;
-  for (int dz = -1; dz <= 1; dz++) {
-    int z = cz + dz;
-    if (P.nc[2] > 2) z = (z + P.nc[2]) % P.nc[2];
-    else if (z < 0 || z >= P.nc[2]) continue;
-    for (int dy = -1; dy <= 1; dy++) {
-      int y = cy + dy;
-      if (P.nc[1] > 2) y = (y + P.nc[1]) % P.nc[1];
-      else if (y < 0 || y >= P.nc[1]) continue;
-      for (int dx = -1; dx <= 1; dx++) {
-        int x = cx + dx;
-        if (P.nc[0] > 2) x = (x + P.nc[0]) % P.nc[0];
-        else if (x < 0 || x >= P.nc[0]) continue;
-        int c2 = x + P.nc[0] * (y + P.nc[1] * z);
-        int b = S.cell_start[c2], e = S.cell_start[c2 + 1];
-        for (int p = b; p < e; p++) {
-          int j = S.cell_atoms[p];
-          if (j == i) continue;
-          int4 qj = S.posq[j];
-          int tj = qj.w & 0xff;
-          float3 d = qsep(qi, qj, P.qinvA);
-          float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
-          bool sw = (ti > tj ? ti : tj) < 3;
-          float pre = sw ? P.pre_sw2A : P.pre_mol2A;
-          if (r2f > pre) continue;
-          bool in;
-          if (r2f < (sw ? P.acc_sw2A : P.acc_mol2A)) {
-            in = true;
-          } else {
-            double4_32a pj = S.pos[j];
-            double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
-            double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
-            double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
-            double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)),
-                                  __dmul_rn(zz, zz));
-            in = r2 < (sw ? P.rv2 : P.rv2lj);
-          }
-          if (!in) continue;
-          if (sw) {
-            if (n < P.max_sw) S.nbr_sw[(size_t)n * P.N + i] = j;
-            n++;
-          } else {
-            int slot = atomicAdd(&S.sc->mol_count, 1);
-            if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
-          }
-        }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(32 * kBuildWarps) k_build_cells(DevParams P, DevState S,
+                                                                  int from_flag) {
+  if (rebuild_skipped(S, from_flag)) return;
+  __shared__ BuildStage st;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ncells = ((volatile DevScalars*)S.sc)->nonempty_count;
+  const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
+  // lane s < 27 owns stencil cell (dx, dy, dz) = (s%3, s/3%3, s/9) - 1
+  const int sdx = lane % 3 - 1, sdy = (lane / 3) % 3 - 1, sdz = lane / 9 - 1;
+  for (int wc = blockIdx.x * kBuildWarps + w; wc < ncells; wc += gridDim.x * kBuildWarps) {
+    const int c = S.nonempty[wc];
+    const int hb = S.cell_start[c], he = S.cell_start[c + 1];
+    const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+    // this lane's stencil cell and its atom range (periodic wrap only on
+    // axes with more than two cells, as the reference's ghost layers)
+    int b = 0, e = 0;
+    if (lane < 27) {
+      int x = cx + sdx, y = cy + sdy, z = cz + sdz;
+      bool ok = true;
+      if (nx > 2) x = (x + nx) % nx; else ok &= (x >= 0 && x < nx);
+      if (ny > 2) y = (y + ny) % ny; else ok &= (y >= 0 && y < ny);
+      if (nz > 2) z = (z + nz) % nz; else ok &= (z >= 0 && z < nz);
+      if (ok) {
+        const int cc = x + nx * (y + ny * z);
+        b = S.cell_start[cc];
+        e = S.cell_start[cc + 1];
       }
     }
+    const int cnt = e - b;
+    int off = cnt;  // inclusive warp scan of the counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, off, o);
+      if (lane >= o) off += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, off, 31);
+    off -= cnt;  // exclusive
+    for (int h0 = hb; h0 < he; h0 += kHome) {
+      const int h1 = min(he, h0 + kHome);
+      for (int h = h0 + lane; h < h1; h += 32) st.n[w][h - h0] = 0;
+      // stage the candidates in chunks of kCand; each lane copies its cell
+      for (int base = 0; base < total; base += kCand) {
+        __syncwarp();
+        const int lo = max(off, base), hi = min(off + cnt, base + kCand);
+        for (int k = lo; k < hi; k++) {
+          st.q[w][k - base] = S.posq_cell[b + (k - off)];
+          st.j[w][k - base] = S.cell_atoms[b + (k - off)];
+        }
+        __syncwarp();
+        test_staged(P, S, st, w, lane, h0, h1, min(kCand, total - base));
+      }
+      for (int h = h0 + lane; h < h1; h += 32) {
+        const int i = S.cell_atoms[h];
+        int n = st.n[w][h - h0];
+        if (n > P.max_sw) {
+          atomicAdd(&S.sc->overflow_sw, 1);
+          n = P.max_sw;
+        }
+        S.n_sw[i] = n;
+        S.posq_build[i] = S.posq_cell[h];
+        S.fast_flag[i] = 0;
+      }
+      __syncwarp();
+    }
   }
-  if (n > P.max_sw) {
-    atomicAdd(&S.sc->overflow_sw, 1);
-    n = P.max_sw;
-  }
-  S.n_sw[i] = n;
 }
 
 __global__ void k_build_end(DevParams P, DevState S, int from_flag) {
@@ -268,6 +330,7 @@ __global__ void k_build_end(DevParams P, DevState S, int from_flag) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     if (S.sc->mol_count > P.mol_cap) S.sc->overflow_mol = S.sc->mol_count;
     S.sc->need_rebuild = 0;
+    S.sc->rebuilds++;
   }
 }
 
@@ -283,8 +346,8 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
   k_scan_top<<<1, kScanBlock, 0, L.stream>>>(P, S, nscan, from_flag);
   k_scan_add<<<nscan, kScanBlock, 0, L.stream>>>(P, S, from_flag);
   k_cell_fill<<<nb_atoms, 256, 0, L.stream>>>(P, S, from_flag);
-  k_cell_order<<<(P.ncell + 255) / 256, 256, 0, L.stream>>>(P, S, from_flag);
-  k_build_pairs<<<(P.N + 127) / 128, 128, 0, L.stream>>>(P, S, from_flag);
+  const int side = L.sms > 0 ? L.sms : 152;
+  k_build_cells<<<side * 16, 32 * kBuildWarps, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);
   return cudaGetLastError();
 }

@@ -264,7 +264,7 @@ class FibMD:
         return U, u
 
     def work_counters(self):
-        c = (C.c_longlong * 4)()
+        c = (C.c_longlong * 6)()
         self._check(self.lib.fibmd_gpu_work_counters(self.h, c), "work_counters")
         return list(c)
 
@@ -298,6 +298,14 @@ class FibMD:
         self._check(self.lib.fibmd_gpu_kernel_time(self.h, C.byref(t), C.byref(n), int(reset)),
                     "kernel_time")
         return t.value, n.value
+
+    PHASES = ("at", "nt", "ds", "f", "force_kernel", "drift", "kick")
+
+    def phase_times(self, reset: bool = False) -> dict:
+        t = (C.c_double * 7)()
+        n = (C.c_longlong * 7)()
+        self._check(self.lib.fibmd_gpu_phase_times(self.h, t, n, int(reset)), "phase_times")
+        return {k: (t[i], n[i]) for i, k in enumerate(self.PHASES)}
 
     @property
     def stream_ptr(self) -> int:

@@ -247,9 +247,18 @@ int fibmd_gpu_regime(fibmd_ctx* ctx, double* Ts, int* tic);
 int fibmd_gpu_timers(fibmd_ctx* ctx, double* at, double* nt, double* ds,
                      double* f, long long* counts4, int reset);
 
-/* Options: "timers" (phase timers of fibmd_gpu_timers, default 1) and
+/* Device time (s) and call counts per phase since the last reset, from
+   CUDA events on the context's stream: [0] parking (at), [1] neighbour
+   lists (nt), [2] calc_atm (ds), [3] force phase (f), [4] main force kernel
+   (with "kernel_timing"), [5] thermostat + drift, [6] kick. */
+int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
+                          int reset);
+
+/* Options: "timers" (phase timers of fibmd_gpu_timers, default 1),
    "kernel_timing" (CUDA events around every launch of the main force
-   kernel, default 0). */
+   kernel, default 0) and "graph" (spec mode runs step pairs as one CUDA
+   graph launch with device-side rebuild decisions, default 1; phase and
+   kernel timers see only the steps run outside the graph). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
 
 /* Total device time (s) and number of launches of the main force kernel
@@ -262,10 +271,13 @@ int fibmd_gpu_kernel_time(fibmd_ctx* ctx, double* force_kernel_s,
    diagnostic for reporting the force kernel against its arithmetic pipe. */
 int fibmd_gpu_pipe_peaks(double* fp64_tflops, double* fp32_tflops);
 
-/* Counters of the last force evaluation: active SW pairs (i<j with a
-   non-zero table entry), non-zero 3-body angle terms, Moliere pairs
-   evaluated, and stale-list angle terms added by the correction pass. */
-int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[4]);
+/* Work counters: [0] active SW pairs (i<j with a non-zero table entry),
+   [1] non-zero 3-body angle terms, [2] Moliere pairs evaluated and [3]
+   stale-list angle terms added by the correction pass, all of the last
+   fibmd_gpu_force call; [4] neighbour-list builds since creation; [5]
+   centres of the last force evaluation with more active legs than the
+   per-thread stage holds (evaluated by the warp-per-centre path). */
+int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[6]);
 
 /* CUDA stream the context orders its work on (cudaStream_t as void*). */
 void* fibmd_gpu_stream(fibmd_ctx* ctx);
