@@ -20,9 +20,19 @@
 
 using namespace fibmd;
 
+namespace fibmd {
+// Message of the last failure that had no context (create, the
+// allocation-free entry point); a fixed buffer so reporting allocates nothing.
+char g_noctx_error[512] = "";
+
+void set_noctx_error(const char* msg) {
+  std::snprintf(g_noctx_error, sizeof g_noctx_error, "%s", msg);
+}
+}  // namespace fibmd
+
 namespace {
 
-std::string g_create_error;
+
 
 // Timed phases: the reference's calc_time report (at, nt, ds, f), the main
 // force kernel alone, and the velocity-Verlet halves with their reductions.
@@ -82,7 +92,7 @@ static int fail(fibmd_ctx* ctx, int code, const char* fmt, ...) {
   vsnprintf(buf, sizeof buf, fmt, ap);
   va_end(ap);
   if (ctx) ctx->err = buf;
-  else g_create_error = buf;
+  else set_noctx_error(buf);
   return code;
 }
 
@@ -156,12 +166,14 @@ struct PhaseTimer {
 };
 
 // ---- parameter derivation --------------------------------------------------------
-// mktables, src/si.f90:575-597, in the reference's operation order.
-static void build_table(const fibmd_params& p, std::vector<double>& tab,
-                        std::vector<double>& tabu, double* umax_out, int* last_nz) {
+namespace fibmd {
+
+// mktables, src/si.f90:575-597, in the reference's operation order, into
+// caller buffers of Ntable + 2 entries.
+void build_ref_table(const fibmd_params& p, double* tab, double* tabu, double* umax_out,
+                     int* last_nz) {
   const int Nt = p.Ntable;
-  tab.assign((size_t)Nt + 2, 0.0);
-  tabu.assign((size_t)Nt + 2, 0.0);
+  for (int i = 0; i < Nt + 2; i++) tab[i] = tabu[i] = 0.0;
   const double umax = 2.5 * p.listfac * p.al;
   const double du = umax / (double)(Nt - 1);
   int last = 0;
@@ -182,13 +194,12 @@ static void build_table(const fibmd_params& p, std::vector<double>& tab,
   *last_nz = last;
 }
 
-static int derive_params(fibmd_ctx* ctx) {
-  const fibmd_params& p = ctx->p;
-  DevParams& P = ctx->P;
+int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_last, DevParams& P,
+                      char* err, int errlen) {
   std::memset(&P, 0, sizeof P);
   P.N = p.Natm;
   P.Nsg = p.Nsg;
-  P.nfired = p.Nsg + ctx->impact;
+  P.nfired = p.Nsg + impact;
   P.mode = p.mode;
   P.precision = p.precision;
   P.max_sw = p.max_sw_nbrs > 0 ? p.max_sw_nbrs : 48;
@@ -208,7 +219,10 @@ static int derive_params(fibmd_ctx* ctx) {
     P.qinvA[d] = (float)(p.Lb[d] * 1.0e10 / 4294967296.0);
     ncell *= P.nc[d];
   }
-  if (ncell > (1ll << 30)) return fail(ctx, FIBMD_EINVAL, "cell grid too large (%lld)", ncell);
+  if (ncell > (1ll << 30)) {
+    std::snprintf(err, (size_t)errlen, "cell grid too large (%lld)", ncell);
+    return FIBMD_EINVAL;
+  }
   P.ncell = (int)ncell;
   P.rv2 = rc * rc;
   P.rv2lj = rclj * rclj;
@@ -263,10 +277,13 @@ static int derive_params(fibmd_ctx* ctx) {
   P.amol = p.alpha_mol;
   P.bmol = p.beta_mol;
   P.gmol = p.gamma_mol;
-  // 2-body table
-  build_table(p, ctx->tab, ctx->tabu, &P.umax, &P.tab_last);
+  // 2-body table (built separately by build_ref_table)
+  P.umax = umax;
+  P.tab_last = tab_last;
   P.Ntable = p.Ntable;
-  const double usup = std::max(P.cut3, ctx->tabu[(size_t)P.tab_last + 1]);
+  // abscissa after the last non-zero entry: u(k+1) = umax*k/(Ntable-1)
+  const double u_next = umax * (double)(tab_last + 1) / (double)(p.Ntable - 1);
+  const double usup = std::max(P.cut3, u_next);
   const double rsupA = usup * sigmax * 1e10 * (1 + 1e-4);
   P.pre3A2 = (float)(rsupA * rsupA);
   // fast atoms: displaced by at least half the smaller list skin
@@ -312,6 +329,21 @@ static int derive_params(fibmd_ctx* ctx) {
   // Moliere full-list capacity: at least the reference's MLlj = 1500*Nlj
   long long mlj = 1500ll * (p.Nlj > 0 ? p.Nlj : 1);
   P.mol_cap = p.max_mol_pairs > 0 ? p.max_mol_pairs : (int)std::max<long long>(mlj, 1 << 16);
+  return FIBMD_OK;
+}
+
+}  // namespace fibmd
+
+static int derive_params(fibmd_ctx* ctx) {
+  const fibmd_params& p = ctx->p;
+  ctx->tab.assign((size_t)p.Ntable + 2, 0.0);
+  ctx->tabu.assign((size_t)p.Ntable + 2, 0.0);
+  double umax = 0.0;
+  int last = 0;
+  build_ref_table(p, ctx->tab.data(), ctx->tabu.data(), &umax, &last);
+  char err[256] = "";
+  const int rc = derive_dev_params(p, ctx->impact, umax, last, ctx->P, err, sizeof err);
+  if (rc) return fail(ctx, rc, "%s", err);
   return FIBMD_OK;
 }
 
@@ -441,8 +473,7 @@ int fibmd_gpu_params_default(fibmd_params* p) {
 
 int fibmd_gpu_last_error(const fibmd_ctx* ctx, char* buf, int len) {
   if (!buf || len <= 0) return FIBMD_EINVAL;
-  const std::string& s = ctx ? ctx->err : g_create_error;
-  std::snprintf(buf, (size_t)len, "%s", s.c_str());
+  std::snprintf(buf, (size_t)len, "%s", ctx ? ctx->err.c_str() : g_noctx_error);
   return FIBMD_OK;
 }
 
@@ -470,14 +501,14 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   ctx->p = *p;
   int rc = derive_params(ctx);
   if (rc) {
-    g_create_error = ctx->err;
+    set_noctx_error(ctx->err.c_str());
     delete ctx;
     return rc;
   }
   cudaGetDevice(&ctx->dev);
   cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->dev);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    g_create_error = "cudaStreamCreate failed";
+    set_noctx_error("cudaStreamCreate failed");
     delete ctx;
     return FIBMD_ECUDA;
   }
@@ -490,7 +521,7 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   do {                                   \
     int r_ = dalloc(ctx, &(ptr), (n));   \
     if (r_) {                            \
-      g_create_error = ctx->err;         \
+      set_noctx_error(ctx->err.c_str());         \
       fibmd_gpu_destroy(ctx);            \
       return r_;                         \
     }                                    \
@@ -533,7 +564,7 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   AL(ctx->d_remaining, 1);
 #undef AL
   if (cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
-    g_create_error = "cudaMallocHost failed";
+    set_noctx_error("cudaMallocHost failed");
     fibmd_gpu_destroy(ctx);
     return FIBMD_ENOMEM;
   }
@@ -547,7 +578,7 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   cudaMemsetAsync(S.frc, 0, sizeof(double4_32a) * N, ctx->stream);
   cudaMemsetAsync(S.flags, 0, sizeof(uint32_t) * N, ctx->stream);
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) {
-    g_create_error = "initialisation copies failed";
+    set_noctx_error("initialisation copies failed");
     fibmd_gpu_destroy(ctx);
     return FIBMD_ECUDA;
   }

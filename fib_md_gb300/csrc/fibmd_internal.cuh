@@ -296,6 +296,16 @@ __device__ __forceinline__ bool grid_finish(double (&v)[NV], double* partials,
   return threadIdx.x == 0;
 }
 
+// ---- host-side parameter derivation (fibmd_capi.cu) ------------------------
+// Records the message fibmd_gpu_last_error(NULL, ...) returns (no heap use).
+void set_noctx_error(const char* msg);
+// mktables into caller buffers of Ntable + 2 entries.
+void build_ref_table(const fibmd_params& p, double* tab, double* tabu, double* umax,
+                     int* last_nz);
+// init_nlist/setupSiGe/setupMol constants for the kernels; allocates nothing.
+int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_last,
+                      DevParams& P, char* err, int errlen);
+
 // ---- launchers (defined in the .cu files) --------------------------------
 struct Launch {
   cudaStream_t stream;
