@@ -111,6 +111,7 @@ SIGNATURES = {
     "fibmd_gpu_kernel_time": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_phase_times": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),
+    "fibmd_gpu_force_noalloc": (_I, [C.POINTER(Params), _VP, _VP, _I, _VP, _VP]),
     # fibmd_host.h
     "fibmd_host_rng_seed": (None, [C.POINTER(Rng), _I]),
     "fibmd_host_ran1": (_D, [C.POINTER(Rng)]),

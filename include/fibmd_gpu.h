@@ -282,6 +282,32 @@ int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[6]);
 /* CUDA stream the context orders its work on (cudaStream_t as void*). */
 void* fibmd_gpu_stream(fibmd_ctx* ctx);
 
+/* Force of one configuration with no device allocation. This entry point
+   has no counterpart in the reference. It is for hosts that cannot ask the
+   driver for device memory when they need a force: hosts whose device
+   memory is handed out by a pool manager or an embedding runtime that
+   forbids driver allocations after start-up, and drivers that must keep a
+   fixed device footprint on a shared GPU. It computes si_force in binary64
+   with the reference's semantics (lists built from X, table SW 2-body,
+   Moliere for fired ions, SW 3-body) and writes F.
+   X_dev, F_dev: device (Natm,3) column-major; atype_dev: device (Natm) with
+   values 1..3; impact: atoms with index > Nsg+impact are unfired ions;
+   stream: a cudaStream_t (NULL for the default stream); returns after
+   synchronising it.
+   All scratch memory (3.9 MB: cells, lists, shadows, scalars, the 2-body
+   table) is one fixed device array inside the library, held by every device
+   that loads it until the process exits. Limits: Natm <= 8192, at most
+   65536 cells in the reference's cell grid, Ntable <= 12000,
+   max_sw_nbrs <= 48, max_mol_pairs <= 65536, precision FP64; beyond them
+   the call returns FIBMD_EINVAL and fibmd_gpu_last_error(NULL, ...) says
+   which limit. The first call on a device looks up the array's device
+   address and uploads the 2-body table: make that first call before any
+   stream capture. Every call shares the array; calls that overlap on the
+   GPU (other streams or host threads) race, so serialise them. */
+int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_dev,
+                            const int* atype_dev, int impact, double* F_dev,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif
