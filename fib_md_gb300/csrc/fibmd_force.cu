@@ -409,24 +409,47 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
 constexpr int kHeavyWarps = 4;
 constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
-template <bool ENERGY>
+template <bool MIXED, bool ENERGY>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
-  __shared__ double sl[kHeavyWarps][6][kHeavyLegs];
+  // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
+  using R = typename std::conditional<MIXED, float, double>::type;
+  __shared__ R sl[kHeavyWarps][6][kHeavyLegs];
   __shared__ int sj[kHeavyWarps][kHeavyLegs];
   __shared__ int snl[kHeavyWarps];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cnt = *((volatile int*)&S.sc->heavy_count);
+  const double conv = MIXED ? P.f_evA_to_N : 1.0;
+  const double econv = MIXED ? P.e_eV_to_J : 1.0;
   for (int h = blockIdx.x * kHeavyWarps + w; h < cnt; h += gridDim.x * kHeavyWarps) {
     const int c = S.heavy_list[h];
     const int tc = S.atype[c];
-    const double4_32a pc = S.pos[c];
     const int n = S.n_sw[c];
     if (lane == 0) snl[w] = 0;
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
       const int j = S.nbr_sw[(size_t)k * P.N + c];
-      const Leg64 L = make_leg(P, pc, S.pos[j], tc, S.atype[j]);
-      if (L.u < P.cut3) {
+      const int tj = S.atype[j];
+      if constexpr (MIXED) {
+        const float3 dq = qsep(S.posq[c], S.posq[j], P.qinvA);
+        const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+        const float rinv = rsqrtf(r2);
+        const float sg = P.sigA[tc - 1][tj - 1];
+        const float u = r2 * rinv / sg;
+        if (!(u < (float)P.cut3)) continue;
+        const float ia = 1.0f / (u - (float)P.al);
+        const float E = expf((float)P.gam * ia);
+        if (!(E > 0.f)) continue;
+        const int q = atomicAdd(&snl[w], 1);
+        sl[w][0][q] = dq.x * rinv;
+        sl[w][1][q] = dq.y * rinv;
+        sl[w][2][q] = dq.z * rinv;
+        sl[w][3][q] = rinv;
+        sl[w][4][q] = E;
+        sl[w][5][q] = -(float)P.gam * ia * ia / sg;
+        sj[w][q] = j | ((tj - 1) << 30);
+      } else {
+        const Leg64 L = make_leg(P, S.pos[c], S.pos[j], tc, tj);
+        if (!(L.u < P.cut3)) continue;
         const int q = atomicAdd(&snl[w], 1);
         const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
         sl[w][0][q] = L.dx * ra;
@@ -441,29 +464,34 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     __syncwarp();
     const int nl = snl[w];
     double fcx = 0, fcy = 0, fcz = 0, uc = 0;
+    const R thrd = (R)P.thrd;
     for (int a = 0; a < nl; a++) {
       for (int b = a + 1 + lane; b < nl; b += 32) {
-        const double ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
-        const double bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
-        const double ar = sl[w][3][a], br = sl[w][3][b];
+        const R ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
+        const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
+        const R ar = sl[w][3][a], br = sl[w][3][b];
         const int ja = sj[w][a], jb = sj[w][b];
-        const double cs = ax * bx + ay * by + az * bz;
-        const double c3 = cs + P.thrd, W = c3 * c3, s2 = 2.0 * c3;
-        const double pref = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30] *
-                            sl[w][4][a] * sl[w][4][b];
-        const double wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
-        const double wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
-        const double Fax = pref * (wa * ax + sa * bx), Fay = pref * (wa * ay + sa * by),
-                     Faz = pref * (wa * az + sa * bz);
-        const double Fbx = pref * (wb * bx + sb * ax), Fby = pref * (wb * by + sb * ay),
-                     Fbz = pref * (wb * bz + sb * az);
+        const R cs = ax * bx + ay * by + az * bz;
+        const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
+        R lp;
+        if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+        else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+        const R pref = lp * sl[w][4][a] * sl[w][4][b];
+        const R wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
+        const R wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
+        const double Fax = conv * (double)(pref * (wa * ax + sa * bx));
+        const double Fay = conv * (double)(pref * (wa * ay + sa * by));
+        const double Faz = conv * (double)(pref * (wa * az + sa * bz));
+        const double Fbx = conv * (double)(pref * (wb * bx + sb * ax));
+        const double Fby = conv * (double)(pref * (wb * by + sb * ay));
+        const double Fbz = conv * (double)(pref * (wb * bz + sb * az));
         atomic_add3(S.frc_new, ja & 0x3fffffff, Fax, Fay, Faz);
         atomic_add3(S.frc_new, jb & 0x3fffffff, Fbx, Fby, Fbz);
         fcx -= Fax + Fbx;
         fcy -= Fay + Fby;
         fcz -= Faz + Fbz;
         if (ENERGY) {
-          const double e3 = pref * W / 3.0;
+          const double e3 = econv * (double)(pref * W) / 3.0;
           uc += e3;
           atomicAdd(&S.epot[ja & 0x3fffffff], e3);
           atomicAdd(&S.epot[jb & 0x3fffffff], e3);
@@ -633,7 +661,7 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
-  k_force_heavy<ENERGY><<<side, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
+  k_force_heavy<MIXED, ENERGY><<<side, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
   return cudaGetLastError();
 }

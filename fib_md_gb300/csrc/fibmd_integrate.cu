@@ -403,12 +403,23 @@ __global__ void __launch_bounds__(256) k_spec_kick(DevParams P, DevState S, int 
       }
     }
   }
-  v2 = warp_max(v2);
-  ts = warp_sum(ts);
-  tc = warp_sum(tc);
+  // max through the bit order of non-negative doubles (integer shuffles,
+  // no binary64 instructions)
+  unsigned long long vb = (unsigned long long)__double_as_longlong(v2);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long t = __shfl_xor_sync(0xffffffffu, vb, o);
+    vb = t > vb ? t : vb;
+  }
+  // only warps holding thermostat atoms sum
+  const bool thermo = __any_sync(0xffffffffu, tc > 0.0);
+  if (thermo) {
+    ts = warp_sum(ts);
+    tc = warp_sum(tc);
+  }
   if ((threadIdx.x & 31) == 0) {
-    atomicMax(&S.sc->acc_vmax2_bits, (unsigned long long)__double_as_longlong(v2));
-    if (tc > 0.0) {
+    atomicMax(&S.sc->acc_vmax2_bits, vb);
+    if (thermo) {
       atomicAdd(&S.sc->acc_tsum, ts);
       atomicAdd(&S.sc->acc_tcnt, tc);
     }

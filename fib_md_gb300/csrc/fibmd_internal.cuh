@@ -188,8 +188,11 @@ __device__ __forceinline__ double rebox1(double x, double L) {
   return fmod(a, L);
 }
 
+// round(x * qscale) mod 2^32 with one binary64 FMA: adding 1.5 * 2^52 puts
+// the nearest integer (ties to even) into the low mantissa bits, valid for
+// |x * qscale| < 2^51.
 __device__ __forceinline__ unsigned int fixq(double x, double qscale) {
-  return (unsigned int)(long long)__double2ll_rn(x * qscale);
+  return (unsigned int)__double_as_longlong(fma(x, qscale, 6755399441055744.0));
 }
 
 // binary32 separation (Angstrom) of two fixed-point positions.
