@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--list-skin", type=float, default=0.0,
+                    help="spec-mode list skin in Angstrom (0: the reference's list radii)")
+    ap.add_argument("--no-graph", action="store_true",
+                    help="run the step loop launch by launch (for a profiler's launch list)")
     ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
                     help="set up the workload, evaluate the force 3 times, exit (for ncu)")
     return ap.parse_args()
@@ -60,7 +64,7 @@ def parse():
 
 # ---------------------------------------------------------------------------
 # workload
-def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0):
+def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A=0.0):
     import fib_md_gb300 as fm
 
     p = fm.params_default()
@@ -92,6 +96,7 @@ def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0):
     p.Ttar1 = 300.0
     p.tau_spec = 1.0e-13
     p.remove_z = surf + 15e-10 + 20e-10  # sputtered atoms well above the surface leave
+    p.list_skin = list_skin_A * 1e-10
     return dict(params=p, X=X, V=V, Xi=s.Xi.copy(order="F"), mass=s.mass.copy(),
                 atype=s.atype.copy(), xsides=np.zeros(N, dtype=np.int32), tags=tags)
 
@@ -196,7 +201,7 @@ def bench_ours(args, rank, world, dist):
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     cells = tuple(int(x) for x in args.cells.split(","))
-    w = make_workload(cells)
+    w = make_workload(cells, list_skin_A=args.list_skin)
     N = w["params"].Natm
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     fp64_peak, fp32_peak = fm.md.pipe_peaks()
@@ -209,6 +214,7 @@ def bench_ours(args, rank, world, dist):
     # ---- mixed precision (the headline); the step loop runs as CUDA graphs
     g = make_ctx(w, fm.PREC_MIXED)
     g.set_option("timers", 0)
+    g.set_option("graph", 0 if args.no_graph else 1)
     stream = torch.cuda.ExternalStream(g.stream_ptr)
     run_device(g, torch, stream, args.warmup, args.md_steps, flush)
     barrier()
@@ -235,7 +241,7 @@ def bench_ours(args, rank, world, dist):
     run_device(g, torch, stream, 1, min(args.md_steps, 200), flush)
     fk_total, fk_n = g.kernel_time(reset=True)
     g.set_option("kernel_timing", 0)
-    g.set_option("graph", 1)
+    g.set_option("graph", 0 if args.no_graph else 1)
     g.si_force()
     counts = g.work_counters()
     flops = flops_per_force(counts)
@@ -339,6 +345,8 @@ def bench_ours(args, rank, world, dist):
                         f"({N - 1} Si + 1 Ga), 5 keV Ga at 7 deg, variable dt, "
                         f"{args.md_steps} MD steps per bench step",
             "atoms": N, "md_steps_per_step": args.md_steps, "mode": "spec",
+            "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
+            "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
             "parallelism": f"replicas x{world}", "l2": "flushed between timed steps",
         },
         "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
@@ -436,7 +444,7 @@ def main():
     if args.profile:
         import fib_md_gb300 as fm
 
-        w = make_workload(cells)
+        w = make_workload(cells, list_skin_A=args.list_skin)
         g = make_ctx(w, fm.PREC_MIXED if args.profile == "mixed" else fm.PREC_FP64)
         for _ in range(3):
             g.si_force()

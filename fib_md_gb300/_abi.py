@@ -49,7 +49,7 @@ class Params(C.Structure):
         ("outz", _D * 4), ("atomz", _D * 2), ("ionz", _D), ("knockz", _D),
         ("sidewidth", _D), ("dti", _D),
         ("dt_max", _D), ("dx_max", _D), ("tau_spec", _D), ("remove_z", _D),
-        ("mixed_mol_fp64_r", _D),
+        ("mixed_mol_fp64_r", _D), ("list_skin", _D),
         ("max_sw_nbrs", _I), ("max_mol_pairs", _I), ("reserved", _I * 8),
     ]
 

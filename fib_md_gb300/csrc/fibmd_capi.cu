@@ -205,9 +205,14 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   P.max_sw = p.max_sw_nbrs > 0 ? p.max_sw_nbrs : 48;
   const double sigmax = p.sigmaGe > p.sigmaSi ? p.sigmaGe : p.sigmaSi;
   // init_nlist, si.f90:56-61
-  const double rc = p.listfac * p.al * sigmax;
+  double rc = p.listfac * p.al * sigmax;
   const double rlj = 2.5 * sigmax;
-  const double rclj = p.listfac * rlj;
+  double rclj = p.listfac * rlj;
+  const bool spec = p.mode == FIBMD_MODE_SPEC;
+  if (spec && p.list_skin > 0.0) {
+    rc = 0.999 * p.al * sigmax + p.list_skin;
+    rclj = rlj + p.list_skin;
+  }
   long long ncell = 1;
   for (int d = 0; d < 3; d++) {
     P.Lb[d] = p.Lb[d];
@@ -215,10 +220,27 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
     const int n = (int)(p.Lb[d] / rc);
     P.nc[d] = n > 1 ? n : 1;
     P.hcell[d] = p.Lb[d] / (double)P.nc[d];  // chainlist's HMf = Lb/REAL(N)
+    P.wrap[d] = P.nc[d] > 2;                  // ghost layers only when Nc > 2
     P.qscale[d] = 4294967296.0 / p.Lb[d];
     P.qinvA[d] = (float)(p.Lb[d] * 1.0e10 / 4294967296.0);
-    ncell *= P.nc[d];
   }
+  P.mol_reach = 1;
+  if (spec) {
+    // atoms above remove_z are removed, so the grid need not cover the
+    // vacuum above it; pairs never straddle z = 0 (no wrap in z)
+    if (p.remove_z > 0.0 && p.remove_z + rc < p.Lb[2]) {
+      const double zext = p.remove_z + rc;
+      const int n = (int)(zext / (rc * (1.0 + 1e-6)));
+      P.nc[2] = n > 1 ? n : 1;
+      P.hcell[2] = zext / (double)P.nc[2];
+      P.inv_hz = 1.0 / P.hcell[2];
+      P.zcompact = 1;
+      P.wrap[2] = 0;
+    }
+    const double hmin = std::min(P.hcell[0], std::min(P.hcell[1], P.hcell[2]));
+    P.mol_reach = (int)std::ceil(rclj / hmin);
+  }
+  for (int d = 0; d < 3; d++) ncell *= P.nc[d];
   if (ncell > (1ll << 30)) {
     std::snprintf(err, (size_t)errlen, "cell grid too large (%lld)", ncell);
     return FIBMD_EINVAL;
@@ -468,6 +490,7 @@ int fibmd_gpu_params_default(fibmd_params* p) {
   p->tau_spec = 1.0e-13;
   p->remove_z = -1.0;
   p->mixed_mol_fp64_r = 1.0e-10;
+  p->list_skin = 0.0;
   return FIBMD_OK;
 }
 

@@ -346,12 +346,17 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
         x.z = xi.z;
         v.x = v.y = v.z = 0.0;
       }
+      // removal looks at the unwrapped height, so an atom leaving through
+      // the bottom of a periodic box is not taken for a sputtered one
+      const bool removed = P.remove_z > 0.0 && x.z > P.remove_z && S.atype[i] < 3;
       // spec mode has no bit-compatibility constraint with the reference's
-      // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped
+      // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped; with the
+      // cell grid cut at remove_z, z is an open axis and is not wrapped
       x.x = x.x < 0.0 ? x.x + P.Lb[0] : (x.x >= P.Lb[0] ? x.x - P.Lb[0] : x.x);
       x.y = x.y < 0.0 ? x.y + P.Lb[1] : (x.y >= P.Lb[1] ? x.y - P.Lb[1] : x.y);
-      x.z = x.z < 0.0 ? x.z + P.Lb[2] : (x.z >= P.Lb[2] ? x.z - P.Lb[2] : x.z);
-      if (P.remove_z > 0.0 && x.z > P.remove_z && S.atype[i] < 3) {
+      if (!P.zcompact)
+        x.z = x.z < 0.0 ? x.z + P.Lb[2] : (x.z >= P.Lb[2] ? x.z - P.Lb[2] : x.z);
+      if (removed) {
         fl |= FL_REMOVED;
         S.flags[i] = fl;
         v.x = v.y = v.z = 0.0;
@@ -376,10 +381,13 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 
 // Kick (apply != 0) followed by the reductions the next step needs: the
 // largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
-// thermostat layer's sum m v^2 and count. Warps reduce in registers and add
-// to device accumulators (the max through the bit order of non-negative
-// doubles); k_spec_finalize then derives dt and the Berendsen factor.
-__global__ void __launch_bounds__(256) k_spec_kick(DevParams P, DevState S, int apply) {
+// thermostat layer's sum m v^2 and count. Each block writes its partials
+// (the max through the bit order of non-negative doubles, integer shuffles);
+// k_spec_finalize reduces them in block order and derives dt and the
+// Berendsen factor. No atomics, so the result does not depend on timing.
+constexpr int kKickThreads = 256;
+
+__global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply) {
   const double dt = ((volatile DevScalars*)S.sc)->dt;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double v2 = 0.0, ts = 0.0, tc = 0.0;
@@ -403,36 +411,54 @@ __global__ void __launch_bounds__(256) k_spec_kick(DevParams P, DevState S, int 
       }
     }
   }
-  // max through the bit order of non-negative doubles (integer shuffles,
-  // no binary64 instructions)
   unsigned long long vb = (unsigned long long)__double_as_longlong(v2);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long t = __shfl_xor_sync(0xffffffffu, vb, o);
     vb = t > vb ? t : vb;
   }
-  // only warps holding thermostat atoms sum
   const bool thermo = __any_sync(0xffffffffu, tc > 0.0);
   if (thermo) {
     ts = warp_sum(ts);
     tc = warp_sum(tc);
   }
-  if ((threadIdx.x & 31) == 0) {
-    atomicMax(&S.sc->acc_vmax2_bits, vb);
-    if (thermo) {
-      atomicAdd(&S.sc->acc_tsum, ts);
-      atomicAdd(&S.sc->acc_tcnt, tc);
+  __shared__ unsigned long long smax[kKickThreads / 32];
+  __shared__ double ssum[kKickThreads / 32], scnt[kKickThreads / 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (lane == 0) {
+    smax[w] = vb;
+    ssum[w] = thermo ? ts : 0.0;
+    scnt[w] = thermo ? tc : 0.0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = 0ull;
+    double a = 0.0, b = 0.0;
+    for (int q = 0; q < kKickThreads / 32; q++) {
+      m = smax[q] > m ? smax[q] : m;
+      a += ssum[q];
+      b += scnt[q];
     }
+    S.partials[blockIdx.x] = __longlong_as_double((long long)m);
+    S.partials[kMaxRedBlocks + blockIdx.x] = a;
+    S.partials[2 * kMaxRedBlocks + blockIdx.x] = b;
   }
 }
 
-__global__ void k_spec_finalize(DevParams P, DevState S, int apply, double Ttar) {
+__global__ void __launch_bounds__(256) k_spec_finalize(DevParams P, DevState S, int apply,
+                                                       double Ttar, int nblocks) {
+  double v[2] = {0.0, 0.0};
+  double mx = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+    mx = fmax(mx, S.partials[b]);
+    v[0] += S.partials[kMaxRedBlocks + b];
+    v[1] += S.partials[2 * kMaxRedBlocks + b];
+  }
+  mx = block_max(mx);
+  block_sum<2>(v);
+  if (threadIdx.x != 0) return;
   DevScalars* sc = S.sc;
-  const double mx = __longlong_as_double((long long)sc->acc_vmax2_bits);
-  const double tsum = sc->acc_tsum, tcnt = sc->acc_tcnt;
-  sc->acc_vmax2_bits = 0ull;
-  sc->acc_tsum = 0.0;
-  sc->acc_tcnt = 0.0;
+  const double tsum = v[0], tcnt = v[1];
   sc->thermo_sum = tsum;
   sc->thermo_cnt = tcnt;
   sc->vmax2 = mx;
@@ -452,8 +478,10 @@ __global__ void k_spec_finalize(DevParams P, DevState S, int apply, double Ttar)
 
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply) {
-  k_spec_kick<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, apply);
-  k_spec_finalize<<<1, 1, 0, L.stream>>>(P, S, apply, Ttar);
+  const int nb = (P.N + kKickThreads - 1) / kKickThreads;
+  if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
+  k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply);
+  k_spec_finalize<<<1, 256, 0, L.stream>>>(P, S, apply, Ttar, nb);
   return cudaGetLastError();
 }
 

@@ -25,7 +25,7 @@ namespace fibmd {
 
 constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
-constexpr int kMaxRedBlocks = 4096;
+constexpr int kMaxRedBlocks = 16384;  // row stride of the reduction partials
 
 enum : uint32_t {
   FL_FROZEN = 1u,   // xsides > 0 (ref) / FIBMD_TAG_FROZEN (spec)
@@ -42,6 +42,11 @@ struct DevParams {
   int Ntable, tab_last;  // tab_last: last 0-based index with a non-zero entry
   int nc[3];
   int ncell;
+  int wrap[3];      // periodic cell stencil per axis (the reference: Nc > 2)
+  int zcompact;     // spec mode: cell grid in z covers [0, zext) only
+  double inv_hz;    //            1 / cell height in z
+  int mol_reach;    // cells scanned for Moliere pairs (1: the reference's
+                    // 27-cell stencil; spec mode: enough for the radius)
   double Lb[3], iLb[3], hcell[3];
   double qscale[3];      // 2^32 / Lb
   float qinvA[3];        // Lb / 2^32 in Angstrom
@@ -105,9 +110,6 @@ struct DevScalars {
   int removed_count;
   int nonempty_count;
   unsigned long long rebuilds;  // list builds since creation
-  // spec-mode kick accumulators (zeroed by the finalizer after use)
-  unsigned long long acc_vmax2_bits;  // max |v|^2 as the bits of a double >= 0
-  double acc_tsum, acc_tcnt;
   unsigned int ticket[8];
   unsigned long long counters[4];
 };

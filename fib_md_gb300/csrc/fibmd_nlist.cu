@@ -85,7 +85,14 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
     const unsigned long long t = (unsigned long long)qq[d] * (unsigned long long)P.nc[d];
     int c = (int)(t >> 32);
     const unsigned frac = (unsigned)t;
-    if (frac < kGuard || frac > 0xffffffffu - kGuard) {
+    if (d == 2 && P.zcompact) {
+      // spec mode with an open z axis: the grid covers [0, remove_z + rc);
+      // an atom above it (an ion: other atoms there are removed) joins the
+      // top layer and an atom below z = 0 the bottom one, which hold every
+      // atom within rc of it
+      const double zc = S.pos[i].z * P.inv_hz;
+      c = zc < 0.0 ? 0 : (zc >= (double)P.nc[2] ? P.nc[2] - 1 : (int)zc);
+    } else if (frac < kGuard || frac > 0xffffffffu - kGuard) {
       const double4_32a p = S.pos[i];
       c = ref_cell(P, d == 0 ? p.x : d == 1 ? p.y : p.z, d);
     }
@@ -214,6 +221,7 @@ __device__ __forceinline__ bool pair_in_list(const DevParams& P, const DevState&
   const int ti = qi.w & 0xff, tj = qj.w & 0xff;
   *sw = (ti > tj ? ti : tj) < 3;
   if (j == i) return false;
+  if (!*sw && P.mol_reach > 1) return false;  // k_build_ion_pairs lists these
   const float3 d = qsep(qi, qj, P.qinvA);
   const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
   if (r2f > (*sw ? P.pre_sw2A : P.pre_mol2A)) return false;
@@ -277,9 +285,9 @@ __global__ void __launch_bounds__(32 * kBuildWarps) k_build_cells(DevParams P, D
     if (lane < 27) {
       int x = cx + sdx, y = cy + sdy, z = cz + sdz;
       bool ok = true;
-      if (nx > 2) x = (x + nx) % nx; else ok &= (x >= 0 && x < nx);
-      if (ny > 2) y = (y + ny) % ny; else ok &= (y >= 0 && y < ny);
-      if (nz > 2) z = (z + nz) % nz; else ok &= (z >= 0 && z < nz);
+      if (P.wrap[0]) x = (x + nx) % nx; else ok &= (x >= 0 && x < nx);
+      if (P.wrap[1]) y = (y + ny) % ny; else ok &= (y >= 0 && y < ny);
+      if (P.wrap[2]) z = (z + nz) % nz; else ok &= (z >= 0 && z < nz);
       if (ok) {
         const int cc = x + nx * (y + ny * z);
         b = S.cell_start[cc];
@@ -325,6 +333,64 @@ __global__ void __launch_bounds__(32 * kBuildWarps) k_build_cells(DevParams P, D
   }
 }
 
+// Spec mode: every pair with an ion inside the Moliere list radius. One
+// warp per ion scans the cells within mol_reach (the radius exceeds the
+// cell width, which the reference's 27-cell stencil does not cover). The
+// ion stores an ion-atom pair in both orders; an ion-ion pair is stored
+// once by each of its two ions.
+__global__ void __launch_bounds__(128) k_build_ion_pairs(DevParams P, DevState S,
+                                                         int from_flag) {
+  if (rebuild_skipped(S, from_flag)) return;
+  const int lane = threadIdx.x & 31;
+  const int nion = P.N - P.Nsg;
+  const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
+  const int R = P.mol_reach, W = 2 * R + 1;
+  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nion;
+       k += (gridDim.x * blockDim.x) >> 5) {
+    const int i = P.Nsg + k;
+    const int4 qi = S.posq[i];
+    const int ci = S.atom_cell[i];
+    if ((qi.w & 0xff) != 3 || ci < 0) continue;
+    const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
+    for (int s = lane; s < W * W * W; s += 32) {
+      int x = cx + s % W - R, y = cy + (s / W) % W - R, z = cz + s / (W * W) - R;
+      // a stencil wider than an axis would visit a cell twice: skip repeats
+      if (P.wrap[0]) { if (W > nx && (s % W) >= nx) continue; x = ((x % nx) + nx) % nx; }
+      else if (x < 0 || x >= nx) continue;
+      if (P.wrap[1]) { if (W > ny && ((s / W) % W) >= ny) continue; y = ((y % ny) + ny) % ny; }
+      else if (y < 0 || y >= ny) continue;
+      if (P.wrap[2]) { if (W > nz && (s / (W * W)) >= nz) continue; z = ((z % nz) + nz) % nz; }
+      else if (z < 0 || z >= nz) continue;
+      const int c = x + nx * (y + ny * z);
+      const int b = S.cell_start[c], e = S.cell_start[c + 1];
+      for (int p = b; p < e; p++) {
+        const int j = S.cell_atoms[p];
+        if (j == i) continue;
+        const int4 qj = S.posq_cell[p];
+        const bool ion_j = (qj.w & 0xff) == 3;
+        const float3 d = qsep(qi, qj, P.qinvA);
+        const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
+        if (r2f > P.pre_mol2A) continue;
+        bool in = r2f < P.acc_mol2A;
+        if (!in) {
+          const double4_32a pi = S.pos[i], pj = S.pos[j];
+          const double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
+          const double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
+          const double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
+          const double r2 =
+              __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
+          in = r2 < P.rv2lj;
+        }
+        if (!in) continue;
+        const int nw = ion_j ? 1 : 2;
+        const int slot = atomicAdd(&S.sc->mol_count, nw);
+        if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
+        if (!ion_j && slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
+      }
+    }
+  }
+}
+
 __global__ void k_build_end(DevParams P, DevState S, int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   if (threadIdx.x == 0 && blockIdx.x == 0) {
@@ -348,6 +414,8 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
   k_cell_fill<<<nb_atoms, 256, 0, L.stream>>>(P, S, from_flag);
   const int side = L.sms > 0 ? L.sms : 152;
   k_build_cells<<<side * 16, 32 * kBuildWarps, 0, L.stream>>>(P, S, from_flag);
+  if (P.mol_reach > 1 && P.N > P.Nsg)
+    k_build_ion_pairs<<<(P.N - P.Nsg + 3) / 4, 128, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);
   return cudaGetLastError();
 }

@@ -13,7 +13,7 @@
 //
 // Limits: at most kNaAtoms atoms, kNaCells cells of the reference's cell
 // grid, Ntable <= kNaTable, max_sw_nbrs <= kNaMaxSw, kNaMolPairs Moliere list
-// entries. The array (3.9 MB) stays resident on every device that loads the
+// entries. The array (4.2 MB) stays resident on every device that loads the
 // library until the process exits. Every call shares it and finds the
 // previous call's contents there; calls that overlap on the GPU race.
 #include <cuda_runtime.h>

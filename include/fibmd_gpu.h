@@ -131,6 +131,15 @@ typedef struct fibmd_params {
   /* mixed precision */
   double mixed_mol_fp64_r;   /* Moliere pairs closer than this (m) stay fp64  */
 
+  /* spec mode: list radius = interaction cutoff + list_skin (m) for the SW
+     list (cutoff 0.999*a*sigma) and the Moliere list (2.5*sigma); <= 0
+     keeps the reference's radii (listfac 1.1). Spec mode always finds every
+     Moliere pair (the reference's 27-cell stencil misses those beyond one
+     cell). With remove_z > 0 (and remove_z + list radius < Lb(3)) spec mode
+     treats z as an open axis: positions are not wrapped in z and the cell
+     grid covers [0, remove_z + list radius) only. */
+  double list_skin;
+
   /* capacities; 0 = defaults */
   int max_sw_nbrs;           /* SW list slots per atom, default 48            */
   int max_mol_pairs;         /* full Moliere list entries, default
@@ -294,7 +303,7 @@ void* fibmd_gpu_stream(fibmd_ctx* ctx);
    values 1..3; impact: atoms with index > Nsg+impact are unfired ions;
    stream: a cudaStream_t (NULL for the default stream); returns after
    synchronising it.
-   All scratch memory (3.9 MB: cells, lists, shadows, scalars, the 2-body
+   All scratch memory (4.2 MB: cells, lists, shadows, scalars, the 2-body
    table) is one fixed device array inside the library, held by every device
    that loads it until the process exits. Limits: Natm <= 8192, at most
    65536 cells in the reference's cell grid, Ntable <= 12000,

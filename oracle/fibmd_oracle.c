@@ -99,6 +99,7 @@ void orc_params_default(fibmd_params* p) {
   p->tau_spec = 1.0e-13;
   p->remove_z = -1.0;
   p->mixed_mol_fp64_r = 1.0e-10;
+  p->list_skin = 0.0;
 }
 
 /* ---- set-up: setupSiGe / setupMol (prms.f90:433-480), init_nlist

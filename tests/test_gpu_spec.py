@@ -83,3 +83,101 @@ def test_nve_energy_conservation(gpu_lib, precision):
     drift_eV_per_atom = abs(E1 - E0) / s.params.ec / nsg
     assert t > 0.5e-12  # dt at its 1 fs cap for thermal speeds
     assert drift_eV_per_atom < 2e-4, drift_eV_per_atom
+
+
+def _pairs_within(X, Lb, r, sel):
+    """Every pair closer than r by the minimum image in x and y (z open),
+    with at least one atom in sel, as get_pairs reports it: (i, j), i < j,
+    1-based, sorted."""
+    out = []
+    for i in range(X.shape[0]):
+        d = X[i + 1:] - X[i]
+        d[:, :2] -= Lb[:2] * np.rint(d[:, :2] / Lb[:2])
+        r2 = np.einsum("ij,ij->i", d, d)
+        js = i + 1 + np.nonzero(r2 < r * r)[0]
+        js = js[sel[i] | sel[js]]
+        out.append(np.stack([np.full(js.size, i), js], axis=1))
+    P = np.concatenate(out).astype(np.int32) + 1
+    return P[np.lexsort((P[:, 1], P[:, 0]))]
+
+
+def _spec_params(s, skin_A, remove_above_A):
+    p = s.params.copy()
+    p.mode = 1
+    p.list_skin = skin_A * 1e-10
+    nsg = p.Nsg
+    p.remove_z = float(s.X[:nsg, 2].max()) + remove_above_A * 1e-10
+    return p
+
+
+@pytest.mark.parametrize("ion_dz_A", [1.2, 9.0])
+def test_spec_lists_complete(gpu_lib, ion_dz_A):
+    """Spec mode (list skin 0.3 A, cell grid cut at remove_z): the SW list
+    holds every Si/Ge pair within 0.999*a*sigma + skin and the Moliere list
+    every ion pair within 2.5*sigma + skin, beyond the 27-cell stencil."""
+    import fib_md_gb300 as fm
+
+    s, X, V = _spec_system(nc=(6, 6, 4), seed=11)
+    rs = np.random.default_rng(3)
+    nsg = s.params.Nsg
+    X[:nsg] += rs.normal(scale=0.1e-10, size=(nsg, 3))
+    top = np.argmax(X[:nsg, 2])
+    X[nsg] = X[top] + np.array([0.5e-10, -0.3e-10, ion_dz_A * 1e-10])
+    Lb = np.array(s.params.Lb[:])
+    X[:, :2] = np.mod(X[:, :2] + 2 * Lb[:2], Lb[:2])  # some atoms sit below z = 0
+    assert (X[:, 2] < 0).any()
+    p = _spec_params(s, 0.3, 12.0)
+    g = fm.FibMD(p)
+    g.upload(X, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+    g.set_impact(1)
+    g.si_nlist()
+    sig = max(p.sigmaSi, p.sigmaGe)
+    rc = 0.999 * p.al * sig + p.list_skin
+    rclj = 2.5 * sig + p.list_skin
+    ion = s.atype == 3
+    nsg = p.Nsg
+    sw = _pairs_within(X[:nsg], Lb, rc, np.ones(nsg, dtype=bool))
+    assert np.array_equal(g.get_pairs(0), sw)
+    mol = _pairs_within(X, Lb, rclj, ion)
+    assert np.array_equal(g.get_pairs(1), mol)
+    if ion_dz_A < 3.0:
+        assert len(mol) > 0
+        # pairs farther than one cell apart, which a 27-cell scan can miss
+        d = X[mol[:, 1] - 1] - X[mol[:, 0] - 1]
+        d -= Lb * np.rint(d / Lb)
+        assert (np.abs(d).max(axis=1) > rc).any()
+
+
+def test_spec_compact_grid_trajectory(gpu_lib):
+    """The z-limited cell grid gives the same lists, hence the same motion,
+    as the full periodic grid. Only the order of the force sums differs, and
+    with it, at a threshold crossing, the step of a skin-triggered rebuild
+    (which changes no force: both lists are complete)."""
+    import fib_md_gb300 as fm
+
+    s, X, V = _spec_system(nc=(6, 6, 4), seed=13, ion_eV=500.0)
+    runs = []
+    for compact in (True, False):
+        p = _spec_params(s, 0.3, 12.0)
+        if not compact:
+            p.remove_z = -1.0  # no removal height: periodic z, full grid
+        g = fm.FibMD(p)
+        g.upload(X, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+        g.set_tags(np.zeros(p.Natm, dtype=np.uint32))
+        g.set_impact(1)
+        g.si_nlist()
+        g.si_force()
+        lt, t, _, _ = g.steps(2, 150, 0, 0.0, 300.0)
+        Xg, Vg, _ = g.download()
+        g.si_nlist()
+        runs.append((lt, t, Xg, g.work_counters(), g.get_pairs(0), g.get_pairs(1)))
+    (la, ta, Xa, ca, swa, ma), (lb, tb, Xb, cb, swb, mb) = runs
+    # the periodic run wraps atoms that cross z = 0, the open-z run does not
+    Lb = np.array(s.params.Lb[:])
+    d = Xa - Xb
+    d -= Lb * np.rint(d / Lb)
+    dmax = np.abs(d).max()
+    assert la == lb == 150 and abs(ta - tb) <= 1e-12 * tb
+    assert dmax < 1e-18, dmax
+    assert ca[4] > 10 and abs(ca[4] - cb[4]) <= 3, (ca[4], cb[4])
+    assert np.array_equal(swa, swb) and np.array_equal(ma, mb) and len(ma) > 0
