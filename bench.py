@@ -57,8 +57,9 @@ def parse():
                     help="spec-mode list skin in Angstrom (0: the reference's list radii)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the step loop launch by launch (for a profiler's launch list)")
-    ap.add_argument("--profile", choices=["mixed", "fp64"], default=None,
-                    help="set up the workload, evaluate the force 3 times, exit (for ncu)")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "build"], default=None,
+                    help="set up the workload, evaluate the force 3 times (mixed, fp64) "
+                         "or rebuild the lists 5 times (build), exit (for ncu)")
     return ap.parse_args()
 
 
@@ -445,9 +446,12 @@ def main():
         import fib_md_gb300 as fm
 
         w = make_workload(cells, list_skin_A=args.list_skin)
-        g = make_ctx(w, fm.PREC_MIXED if args.profile == "mixed" else fm.PREC_FP64)
-        for _ in range(3):
-            g.si_force()
+        g = make_ctx(w, fm.PREC_FP64 if args.profile == "fp64" else fm.PREC_MIXED)
+        for _ in range(5 if args.profile == "build" else 3):
+            if args.profile == "build":
+                g.si_nlist()
+            else:
+                g.si_force()
         g.close()
         return 0
 

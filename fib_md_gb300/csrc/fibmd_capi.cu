@@ -565,7 +565,6 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   AL(S.cell_atoms, N);
   AL(S.posq_cell, N);
   AL(S.atom_cell, N);
-  AL(S.nonempty, N);
   AL(S.scan_blocks, (size_t)nscan + 1);
   AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
   AL(S.n_sw, N);

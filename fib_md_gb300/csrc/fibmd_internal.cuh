@@ -108,7 +108,6 @@ struct DevScalars {
   int nan_flag;
   int need_rebuild;
   int removed_count;
-  int nonempty_count;
   unsigned long long rebuilds;  // list builds since creation
   unsigned int ticket[8];
   unsigned long long counters[4];
@@ -133,7 +132,6 @@ struct DevState {
   int* cell_atoms;
   int4* posq_cell;   // posq in cell order (filled with cell_atoms)
   int* atom_cell;
-  int* nonempty;     // cells holding at least one atom (build order)
   int* scan_blocks;
   // lists
   int* nbr_sw;

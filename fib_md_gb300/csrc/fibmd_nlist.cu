@@ -48,7 +48,6 @@ __global__ void k_build_begin(DevParams P, DevState S, int from_flag) {
     S.sc->overflow_mol = 0;
     S.sc->cell_oob = 0;
     S.sc->disp_max2 = 0.0;
-    S.sc->nonempty_count = 0;
   }
 }
 
@@ -105,7 +104,7 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
   if (oob) atomicAdd(&S.sc->cell_oob, 1);
   const int cell = ic[0] + P.nc[0] * (ic[1] + P.nc[1] * ic[2]);
   S.atom_cell[i] = cell;
-  if (atomicAdd(&S.cell_count[cell], 1) == 0) S.nonempty[atomicAdd(&S.sc->nonempty_count, 1)] = cell;
+  atomicAdd(&S.cell_count[cell], 1);
 }
 
 // Exclusive scan of cell_count (ncell+1 entries) into cell_start.
@@ -196,192 +195,174 @@ __global__ void k_cell_fill(DevParams P, DevState S, int from_flag) {
   if (c < 0) return;
   const int slot = S.cell_start[c] + atomicAdd(&S.cell_count[c], 1);
   S.cell_atoms[slot] = i;
-  S.posq_cell[slot] = S.posq[i];
+  int4 q = S.posq[i];
+  // spec mode lists ion pairs in a scan of its own: half a box away in x,
+  // an ion never passes the SW distance test of the per-atom scan
+  if (P.mol_reach > 1 && (q.w & 0xff) == 3) q.x = (int)((unsigned)q.x + 0x80000000u);
+  S.posq_cell[slot] = q;
 }
 
 // ---- pair lists (si_nlistG pair loop, si.f90:130-189) ---------------------
-// One warp per non-empty cell. The warp stages the candidates of the
-// 27-cell stencil (9 rows of three x-adjacent cells, each row one
-// contiguous range of the cell-sorted arrays when it does not wrap) in
-// shared memory with coalesced loads, then tests every home atom of the
-// cell against them, 32 candidates at a time; accepted SW neighbours are
-// compacted into the home atom's list slots with a ballot and prefix count.
-constexpr int kBuildWarps = 4;
-constexpr int kCand = 256;   // staged candidates per warp (flushed when full)
-constexpr int kHome = 64;    // home atoms handled per pass over the stencil
-
-struct BuildStage {
-  int4 q[kBuildWarps][kCand];
-  int j[kBuildWarps][kCand];
-  int n[kBuildWarps][kHome];
-};
-
-__device__ __forceinline__ bool pair_in_list(const DevParams& P, const DevState& S, int i,
-                                             const int4& qi, int j, const int4& qj, bool* sw) {
-  const int ti = qi.w & 0xff, tj = qj.w & 0xff;
-  *sw = (ti > tj ? ti : tj) < 3;
-  if (j == i) return false;
-  if (!*sw && P.mol_reach > 1) return false;  // k_build_ion_pairs lists these
-  const float3 d = qsep(qi, qj, P.qinvA);
-  const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
-  if (r2f > (*sw ? P.pre_sw2A : P.pre_mol2A)) return false;
-  if (r2f < (*sw ? P.acc_sw2A : P.acc_mol2A)) return true;
-  // within 1e-4 of the radius: the reference's binary64 test decides
+// Exact list membership of a candidate already inside the FP32 prefilter
+// band: the reference's binary64 minimum-image distance decides.
+__device__ __forceinline__ bool exact_in(const DevParams& P, const DevState& S, int i, int j,
+                                         double rv2) {
   const double4_32a pi = S.pos[i], pj = S.pos[j];
   const double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
   const double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
   const double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
-  return r2 < (*sw ? P.rv2 : P.rv2lj);
+  return r2 < rv2;
 }
 
-// Tests home atoms [h0, h1) against the K staged candidates.
-__device__ __forceinline__ void test_staged(const DevParams& P, const DevState& S,
-                                            BuildStage& st, int w, int lane, int h0, int h1,
-                                            int K) {
-  for (int h = h0; h < h1; h++) {
-    const int i = S.cell_atoms[h];
-    const int4 qi = S.posq_cell[h];
-    int n = st.n[w][h - h0];
-    for (int k0 = 0; k0 < K; k0 += 32) {
-      const int k = k0 + lane;
-      bool sw = true, in = false;
-      int j = -1;
-      if (k < K) {
-        j = st.j[w][k];
-        in = pair_in_list(P, S, i, qi, j, st.q[w][k], &sw);
-      }
-      const unsigned m = __ballot_sync(0xffffffffu, in && sw);
-      if (in && sw) {
-        const int slot = n + __popc(m & ((1u << lane) - 1u));
-        if (slot < P.max_sw) S.nbr_sw[(size_t)slot * P.N + i] = j;
-      } else if (in) {
-        const int slot = atomicAdd(&S.sc->mol_count, 1);
-        if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
-      }
-      n += __popc(m);
-    }
-    if (lane == 0) st.n[w][h - h0] = n;
-  }
-  __syncwarp();
-}
+// One thread per binned atom, in cell order. The lanes of a warp hold the
+// atoms of a few x-adjacent cells, so they walk nearly the same nine
+// stencil rows, and their candidate loads hit the same cached lines. A row
+// of three x-adjacent cells is one run of the cell-sorted arrays (two runs
+// where it wraps in x). Candidates are tested in binary32 on the
+// fixed-point separations; within 1e-4 of a radius the reference's
+// binary64 test decides. Accepted SW neighbours are kept (as cell-order
+// slots) in shared memory and written to the list after the scan, one list
+// slot of all lanes at a time. A pair with an ion goes to the Moliere pair
+// list; with WIDE (spec mode) the ion scan below lists those instead and
+// ions are skipped here.
+constexpr int kBuildThreads = 128;
+constexpr int kBuildBuf = 24;  // buffered neighbours per atom
 
-__global__ void __launch_bounds__(32 * kBuildWarps) k_build_cells(DevParams P, DevState S,
-                                                                  int from_flag) {
+template <bool WIDE>
+__global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, DevState S,
+                                                               int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  __shared__ BuildStage st;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ncells = ((volatile DevScalars*)S.sc)->nonempty_count;
-  const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
-  // lane s < 27 owns stencil cell (dx, dy, dz) = (s%3, s/3%3, s/9) - 1
-  const int sdx = lane % 3 - 1, sdy = (lane / 3) % 3 - 1, sdz = lane / 9 - 1;
-  for (int wc = blockIdx.x * kBuildWarps + w; wc < ncells; wc += gridDim.x * kBuildWarps) {
-    const int c = S.nonempty[wc];
-    const int hb = S.cell_start[c], he = S.cell_start[c + 1];
+  __shared__ int buf[kBuildBuf][kBuildThreads];
+  const int t = threadIdx.x;
+  const int h = blockIdx.x * kBuildThreads + t;
+  if (h >= S.cell_start[P.ncell]) return;
+  const int i = S.cell_atoms[h];
+  const int4 qi = S.posq_cell[h];
+  const int ti = qi.w & 0xff;
+  int* const nbr = S.nbr_sw + i;
+  const size_t stride = (size_t)P.N;
+  int n = 0;
+  if (!(WIDE && ti == 3)) {
+    const int c = S.atom_cell[i];
+    const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
-    // this lane's stencil cell and its atom range (periodic wrap only on
-    // axes with more than two cells, as the reference's ghost layers)
-    int b = 0, e = 0;
-    if (lane < 27) {
-      int x = cx + sdx, y = cy + sdy, z = cz + sdz;
-      bool ok = true;
-      if (P.wrap[0]) x = (x + nx) % nx; else ok &= (x >= 0 && x < nx);
-      if (P.wrap[1]) y = (y + ny) % ny; else ok &= (y >= 0 && y < ny);
-      if (P.wrap[2]) z = (z + nz) % nz; else ok &= (z >= 0 && z < nz);
-      if (ok) {
-        const int cc = x + nx * (y + ny * z);
-        b = S.cell_start[cc];
-        e = S.cell_start[cc + 1];
+    // inclusive x ranges of the stencil row (periodic only with > 2 cells)
+    int xa0, xa1, xb0 = 0, xb1 = -1;
+    if (P.wrap[0]) {
+      if (cx == 0) {
+        xa0 = 0; xa1 = 1; xb0 = xb1 = nx - 1;
+      } else if (cx == nx - 1) {
+        xa0 = nx - 2; xa1 = nx - 1; xb0 = xb1 = 0;
+      } else {
+        xa0 = cx - 1; xa1 = cx + 1;
       }
+    } else {
+      xa0 = max(cx - 1, 0);
+      xa1 = min(cx + 1, nx - 1);
     }
-    const int cnt = e - b;
-    int off = cnt;  // inclusive warp scan of the counts
+    const float thr_sw = P.pre_sw2A;
+    // binary32 bound of any listed pair of this atom
+    const float thr = WIDE ? P.pre_sw2A : fmaxf(P.pre_sw2A, P.pre_mol2A);
+    const int4* __restrict__ qc = S.posq_cell;
+    for (int dz = -1; dz <= 1; dz++) {
+      int z = cz + dz;
+      if (P.wrap[2]) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+      else if (z < 0 || z >= nz) continue;
+      for (int dy = -1; dy <= 1; dy++) {
+        int y = cy + dy;
+        if (P.wrap[1]) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+        else if (y < 0 || y >= ny) continue;
+        const int row = nx * (y + ny * z);
+        for (int part = 0; part < 2; part++) {
+          const int x0 = part ? xb0 : xa0, x1 = part ? xb1 : xa1;
+          if (x1 < x0) break;
+          const int b = S.cell_start[row + x0], e = S.cell_start[row + x1 + 1];
+          // two candidates per pass, their loads in flight together; the
+          // common case (outside the prefilter sphere) is the first test
+          for (int p0 = b; p0 < e; p0 += 2) {
+            const int4 q0 = __ldg(&qc[p0]);
+            const int4 q1 = p0 + 1 < e ? __ldg(&qc[p0 + 1]) : q0;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int t = __shfl_up_sync(0xffffffffu, off, o);
-      if (lane >= o) off += t;
-    }
-    const int total = __shfl_sync(0xffffffffu, off, 31);
-    off -= cnt;  // exclusive
-    for (int h0 = hb; h0 < he; h0 += kHome) {
-      const int h1 = min(he, h0 + kHome);
-      for (int h = h0 + lane; h < h1; h += 32) st.n[w][h - h0] = 0;
-      // stage the candidates in chunks of kCand; each lane copies its cell
-      for (int base = 0; base < total; base += kCand) {
-        __syncwarp();
-        const int lo = max(off, base), hi = min(off + cnt, base + kCand);
-        for (int k = lo; k < hi; k++) {
-          st.q[w][k - base] = S.posq_cell[b + (k - off)];
-          st.j[w][k - base] = S.cell_atoms[b + (k - off)];
+            for (int u = 0; u < 2; u++) {
+              const int p = p0 + u;
+              if (p >= e) break;
+              const int4 qj = u ? q1 : q0;
+              const float3 d = qsep(qi, qj, P.qinvA);
+              const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+              if (r2f > thr || p == h) continue;
+              bool sw = true;
+              if (!WIDE) {
+                const int tj = qj.w & 0xff;
+                sw = (ti > tj ? ti : tj) < 3;
+                if (sw && r2f > thr_sw) continue;
+              }
+              if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) &&
+                  !exact_in(P, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
+                continue;
+              if (sw) {
+                if (n < kBuildBuf) buf[n][t] = p;
+                else if (n < P.max_sw) nbr[(size_t)n * stride] = __ldg(&S.cell_atoms[p]);
+                n++;
+              } else {
+                const int slot = atomicAdd(&S.sc->mol_count, 1);
+                if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, __ldg(&S.cell_atoms[p]));
+              }
+            }
+          }
         }
-        __syncwarp();
-        test_staged(P, S, st, w, lane, h0, h1, min(kCand, total - base));
       }
-      for (int h = h0 + lane; h < h1; h += 32) {
-        const int i = S.cell_atoms[h];
-        int n = st.n[w][h - h0];
-        if (n > P.max_sw) {
-          atomicAdd(&S.sc->overflow_sw, 1);
-          n = P.max_sw;
-        }
-        S.n_sw[i] = n;
-        S.posq_build[i] = S.posq_cell[h];
-        S.fast_flag[i] = 0;
-      }
-      __syncwarp();
     }
   }
+  if (n > P.max_sw) {
+    atomicAdd(&S.sc->overflow_sw, 1);
+    n = P.max_sw;
+  }
+  const int nb = min(n, kBuildBuf);
+  for (int k = 0; k < nb; k++) nbr[(size_t)k * stride] = S.cell_atoms[buf[k][t]];
+  S.n_sw[i] = n;
+  S.posq_build[i] = (WIDE && ti == 3) ? S.posq[i] : qi;
+  S.fast_flag[i] = 0;
 }
 
 // Spec mode: every pair with an ion inside the Moliere list radius. One
-// warp per ion scans the cells within mol_reach (the radius exceeds the
-// cell width, which the reference's 27-cell stencil does not cover). The
-// ion stores an ion-atom pair in both orders; an ion-ion pair is stored
-// once by each of its two ions.
+// block per ion; its threads share out the cells within mol_reach (the
+// radius exceeds the cell width, which the reference's 27-cell stencil
+// does not cover). The ion stores an ion-atom pair in both orders; an
+// ion-ion pair is stored once by each of its two ions.
 __global__ void __launch_bounds__(128) k_build_ion_pairs(DevParams P, DevState S,
                                                          int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  const int lane = threadIdx.x & 31;
   const int nion = P.N - P.Nsg;
   const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
   const int R = P.mol_reach, W = 2 * R + 1;
-  for (int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < nion;
-       k += (gridDim.x * blockDim.x) >> 5) {
+  for (int k = blockIdx.x; k < nion; k += gridDim.x) {
     const int i = P.Nsg + k;
     const int4 qi = S.posq[i];
     const int ci = S.atom_cell[i];
     if ((qi.w & 0xff) != 3 || ci < 0) continue;
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
-    for (int s = lane; s < W * W * W; s += 32) {
-      int x = cx + s % W - R, y = cy + (s / W) % W - R, z = cz + s / (W * W) - R;
-      // a stencil wider than an axis would visit a cell twice: skip repeats
-      if (P.wrap[0]) { if (W > nx && (s % W) >= nx) continue; x = ((x % nx) + nx) % nx; }
+    for (int s = threadIdx.x; s < W * W * W; s += blockDim.x) {
+      const int ox = s % W, oy = (s / W) % W, oz = s / (W * W);
+      int x = cx + ox - R, y = cy + oy - R, z = cz + oz - R;
+      // a stencil wider than a periodic axis would visit a cell twice
+      if (P.wrap[0]) { if (ox >= nx) continue; x = ((x % nx) + nx) % nx; }
       else if (x < 0 || x >= nx) continue;
-      if (P.wrap[1]) { if (W > ny && ((s / W) % W) >= ny) continue; y = ((y % ny) + ny) % ny; }
+      if (P.wrap[1]) { if (oy >= ny) continue; y = ((y % ny) + ny) % ny; }
       else if (y < 0 || y >= ny) continue;
-      if (P.wrap[2]) { if (W > nz && (s / (W * W)) >= nz) continue; z = ((z % nz) + nz) % nz; }
+      if (P.wrap[2]) { if (oz >= nz) continue; z = ((z % nz) + nz) % nz; }
       else if (z < 0 || z >= nz) continue;
       const int c = x + nx * (y + ny * z);
       const int b = S.cell_start[c], e = S.cell_start[c + 1];
       for (int p = b; p < e; p++) {
         const int j = S.cell_atoms[p];
         if (j == i) continue;
-        const int4 qj = S.posq_cell[p];
-        const bool ion_j = (qj.w & 0xff) == 3;
+        const int4 qj = S.posq[j];  // posq_cell holds ions shifted
         const float3 d = qsep(qi, qj, P.qinvA);
         const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
         if (r2f > P.pre_mol2A) continue;
-        bool in = r2f < P.acc_mol2A;
-        if (!in) {
-          const double4_32a pi = S.pos[i], pj = S.pos[j];
-          const double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
-          const double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
-          const double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
-          const double r2 =
-              __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
-          in = r2 < P.rv2lj;
-        }
-        if (!in) continue;
+        if (r2f >= P.acc_mol2A && !exact_in(P, S, i, j, P.rv2lj)) continue;
+        const bool ion_j = (qj.w & 0xff) == 3;
         const int nw = ion_j ? 1 : 2;
         const int slot = atomicAdd(&S.sc->mol_count, nw);
         if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
@@ -412,10 +393,13 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
   k_scan_top<<<1, kScanBlock, 0, L.stream>>>(P, S, nscan, from_flag);
   k_scan_add<<<nscan, kScanBlock, 0, L.stream>>>(P, S, from_flag);
   k_cell_fill<<<nb_atoms, 256, 0, L.stream>>>(P, S, from_flag);
-  const int side = L.sms > 0 ? L.sms : 152;
-  k_build_cells<<<side * 16, 32 * kBuildWarps, 0, L.stream>>>(P, S, from_flag);
+  const int nb_build = (P.N + kBuildThreads - 1) / kBuildThreads;
+  if (P.mol_reach > 1)
+    k_build_atoms<true><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
+  else
+    k_build_atoms<false><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
   if (P.mol_reach > 1 && P.N > P.Nsg)
-    k_build_ion_pairs<<<(P.N - P.Nsg + 3) / 4, 128, 0, L.stream>>>(P, S, from_flag);
+    k_build_ion_pairs<<<min(P.N - P.Nsg, 4096), 128, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);
   return cudaGetLastError();
 }

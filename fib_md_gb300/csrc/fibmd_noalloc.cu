@@ -38,7 +38,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // byte offsets of the sub-arrays inside the scratch array
 struct Layout {
   size_t pos, frc_new, posq, posq_build, posq_cell, atype, flags, cell_count, cell_start,
-      cell_atoms, atom_cell, nonempty, scan_blocks, nbr_sw, n_sw, mol_pairs, fast_flag,
+      cell_atoms, atom_cell, scan_blocks, nbr_sw, n_sw, mol_pairs, fast_flag,
       fast_list, heavy_list, tab, tabu, partials, sc, total;
 };
 
@@ -57,7 +57,6 @@ constexpr Layout make_layout() {
   L.cell_start = o; o += align256(sizeof(int) * C);
   L.cell_atoms = o; o += align256(sizeof(int) * N);
   L.atom_cell = o; o += align256(sizeof(int) * N);
-  L.nonempty = o; o += align256(sizeof(int) * N);
   L.scan_blocks = o; o += align256(sizeof(int) * (C / 1024 + 2));
   L.nbr_sw = o; o += align256(sizeof(int) * (size_t)kNaMaxSw * N);
   L.n_sw = o; o += align256(sizeof(int) * N);
@@ -215,7 +214,6 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
   S.cell_start = reinterpret_cast<int*>(b + kLayout.cell_start);
   S.cell_atoms = reinterpret_cast<int*>(b + kLayout.cell_atoms);
   S.atom_cell = reinterpret_cast<int*>(b + kLayout.atom_cell);
-  S.nonempty = reinterpret_cast<int*>(b + kLayout.nonempty);
   S.scan_blocks = reinterpret_cast<int*>(b + kLayout.scan_blocks);
   S.nbr_sw = reinterpret_cast<int*>(b + kLayout.nbr_sw);
   S.n_sw = reinterpret_cast<int*>(b + kLayout.n_sw);
