@@ -8,11 +8,12 @@ from . import _abi
 from ._abi import (MODE_REF, MODE_SPEC, PREC_FP64, PREC_MIXED, STOP_DONE, STOP_DUMP,
                    STOP_MAXSTEPS, STOP_REGIME, TAG_FROZEN, TAG_REMOVED, TAG_THERMO, Params,
                    Siga)
-from .md import (FibMD, FibmdError, Ran1, System, crystal_system, knock, params_default,
-                 pureepi, read_siga)
+from .md import (FibMD, FibMDBatch, FibmdError, Ran1, SpecSlab, System, crystal_system, knock,
+                 params_default, pureepi, read_siga, spec_slab)
 
 __all__ = [
-    "FibMD", "FibmdError", "Params", "Siga", "Ran1", "System", "crystal_system", "knock",
+    "FibMD", "FibMDBatch", "FibmdError", "Params", "Siga", "Ran1", "SpecSlab", "System",
+    "crystal_system", "knock", "spec_slab",
     "params_default", "pureepi", "read_siga", "MODE_REF", "MODE_SPEC", "PREC_FP64",
     "PREC_MIXED", "TAG_FROZEN", "TAG_THERMO", "TAG_REMOVED", "STOP_MAXSTEPS", "STOP_DUMP",
     "STOP_DONE", "STOP_REGIME",

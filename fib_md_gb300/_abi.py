@@ -59,6 +59,13 @@ class Params(C.Structure):
         return q
 
 
+class Replica(C.Structure):
+    """Mirror of `fibmd_replica`: one replica of a batched ensemble."""
+
+    _fields_ = [("natm", _I), ("nsg", _I), ("Lb", _D * 3), ("remove_z", _D),
+                ("reserved", _I * 4)]
+
+
 class Siga(C.Structure):
     """Mirror of `fibmd_siga` (fibmd_host.h)."""
 
@@ -112,6 +119,9 @@ SIGNATURES = {
     "fibmd_gpu_phase_times": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),
     "fibmd_gpu_force_noalloc": (_I, [C.POINTER(Params), _VP, _VP, _I, _VP, _VP]),
+    "fibmd_gpu_batch_create": (_I, [C.POINTER(Params), _I, C.POINTER(Replica), C.POINTER(_VP)]),
+    "fibmd_gpu_batch_layout": (_I, [_VP, _IP, _IP]),
+    "fibmd_gpu_batch_scalars": (_I, [_VP, _DP, _DP, _IP]),
     # fibmd_host.h
     "fibmd_host_rng_seed": (None, [C.POINTER(Rng), _I]),
     "fibmd_host_ran1": (_D, [C.POINTER(Rng)]),

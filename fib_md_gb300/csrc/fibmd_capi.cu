@@ -81,6 +81,10 @@ struct fibmd_ctx {
   double4_32a* graph_frc = nullptr;  // S.frc when the graph was captured
   int graph_nfired = -1;
   int* d_remaining = nullptr;
+  // replicas: one for a single system, several for a batched ensemble
+  Geo geo0;                 // the single system's geometry
+  std::vector<Geo> geo;     // per replica (uploaded to S.geo)
+  std::vector<int> rep_of;  // replica of each atom, -1 for padding slots
   std::string err;
 };
 
@@ -194,58 +198,98 @@ void build_ref_table(const fibmd_params& p, double* tab, double* tabu, double* u
   *last_nz = last;
 }
 
-int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_last, DevParams& P,
-                      char* err, int errlen) {
-  std::memset(&P, 0, sizeof P);
-  P.N = p.Natm;
-  P.Nsg = p.Nsg;
-  P.nfired = p.Nsg + impact;
-  P.mode = p.mode;
-  P.precision = p.precision;
-  P.max_sw = p.max_sw_nbrs > 0 ? p.max_sw_nbrs : 48;
+// List radii (m): the reference's listfac * a * sigma and listfac * 2.5 sigma
+// (init_nlist, si.f90:56-61), or in spec mode with a list skin, cutoff + skin.
+static void list_radii(const fibmd_params& p, double* rc, double* rclj) {
   const double sigmax = p.sigmaGe > p.sigmaSi ? p.sigmaGe : p.sigmaSi;
-  // init_nlist, si.f90:56-61
-  double rc = p.listfac * p.al * sigmax;
-  const double rlj = 2.5 * sigmax;
-  double rclj = p.listfac * rlj;
+  *rc = p.listfac * p.al * sigmax;
+  *rclj = p.listfac * 2.5 * sigmax;
+  if (p.mode == FIBMD_MODE_SPEC && p.list_skin > 0.0) {
+    *rc = 0.999 * p.al * sigmax + p.list_skin;
+    *rclj = 2.5 * sigmax + p.list_skin;
+  }
+}
+
+int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& G, char* err,
+               int errlen) {
+  std::memset(&G, 0, sizeof G);
+  double rc, rclj;
+  list_radii(p, &rc, &rclj);
   const bool spec = p.mode == FIBMD_MODE_SPEC;
-  if (spec && p.list_skin > 0.0) {
-    rc = 0.999 * p.al * sigmax + p.list_skin;
-    rclj = rlj + p.list_skin;
-  }
-  long long ncell = 1;
   for (int d = 0; d < 3; d++) {
-    P.Lb[d] = p.Lb[d];
-    P.iLb[d] = 1. / p.Lb[d];
-    const int n = (int)(p.Lb[d] / rc);
-    P.nc[d] = n > 1 ? n : 1;
-    P.hcell[d] = p.Lb[d] / (double)P.nc[d];  // chainlist's HMf = Lb/REAL(N)
-    P.wrap[d] = P.nc[d] > 2;                  // ghost layers only when Nc > 2
-    P.qscale[d] = 4294967296.0 / p.Lb[d];
-    P.qinvA[d] = (float)(p.Lb[d] * 1.0e10 / 4294967296.0);
+    if (!(Lb[d] > 0.0)) {
+      std::snprintf(err, (size_t)errlen, "box length %d is %g", d + 1, Lb[d]);
+      return FIBMD_EINVAL;
+    }
+    G.Lb[d] = Lb[d];
+    G.iLb[d] = 1. / Lb[d];
+    const int n = (int)(Lb[d] / rc);
+    G.nc[d] = n > 1 ? n : 1;
+    G.hcell[d] = Lb[d] / (double)G.nc[d];  // chainlist's HMf = Lb/REAL(N)
+    G.wrap[d] = G.nc[d] > 2;                // ghost layers only when Nc > 2
+    G.qscale[d] = 4294967296.0 / Lb[d];
+    G.qinvA[d] = (float)(Lb[d] * 1.0e10 / 4294967296.0);
   }
-  P.mol_reach = 1;
+  G.remove_z = remove_z;
+  G.mol_reach = 1;
   if (spec) {
     // atoms above remove_z are removed, so the grid need not cover the
     // vacuum above it; pairs never straddle z = 0 (no wrap in z)
-    if (p.remove_z > 0.0 && p.remove_z + rc < p.Lb[2]) {
-      const double zext = p.remove_z + rc;
+    if (remove_z > 0.0 && remove_z + rc < Lb[2]) {
+      const double zext = remove_z + rc;
       const int n = (int)(zext / (rc * (1.0 + 1e-6)));
-      P.nc[2] = n > 1 ? n : 1;
-      P.hcell[2] = zext / (double)P.nc[2];
-      P.inv_hz = 1.0 / P.hcell[2];
-      P.zcompact = 1;
-      P.wrap[2] = 0;
+      G.nc[2] = n > 1 ? n : 1;
+      G.hcell[2] = zext / (double)G.nc[2];
+      G.inv_hz = 1.0 / G.hcell[2];
+      G.zcompact = 1;
+      G.wrap[2] = 0;
     }
-    const double hmin = std::min(P.hcell[0], std::min(P.hcell[1], P.hcell[2]));
-    P.mol_reach = (int)std::ceil(rclj / hmin);
+    const double hmin = std::min(G.hcell[0], std::min(G.hcell[1], G.hcell[2]));
+    G.mol_reach = (int)std::ceil(rclj / hmin);
   }
-  for (int d = 0; d < 3; d++) ncell *= P.nc[d];
+  const long long ncell = (long long)G.nc[0] * G.nc[1] * G.nc[2];
   if (ncell > (1ll << 30)) {
     std::snprintf(err, (size_t)errlen, "cell grid too large (%lld)", ncell);
     return FIBMD_EINVAL;
   }
-  P.ncell = (int)ncell;
+  G.ncell = (int)ncell;
+  return FIBMD_OK;
+}
+
+int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_last, DevParams& P,
+                      Geo& G, char* err, int errlen) {
+  std::memset(&P, 0, sizeof P);
+  P.N = p.Natm;
+  P.Nsg = p.Nsg;
+  P.nfired = p.Nsg + impact;
+  P.nrep = 1;
+  P.nion = p.Natm - p.Nsg;
+  P.mode = p.mode;
+  P.precision = p.precision;
+  P.max_sw = p.max_sw_nbrs > 0 ? p.max_sw_nbrs : 48;
+  const double sigmax = p.sigmaGe > p.sigmaSi ? p.sigmaGe : p.sigmaSi;
+  double rc, rclj;
+  list_radii(p, &rc, &rclj);
+  const double rlj = 2.5 * sigmax;
+  int rcg = derive_geo(p, p.Lb, p.remove_z, G, err, errlen);
+  if (rcg) return rcg;
+  G.atom_begin = 0;
+  G.atom_end = p.Natm;
+  G.blk_begin = 0;
+  G.blk_end = (p.Natm + kKickThreads - 1) / kKickThreads;
+  for (int d = 0; d < 3; d++) {
+    P.Lb[d] = G.Lb[d];
+    P.iLb[d] = G.iLb[d];
+    P.nc[d] = G.nc[d];
+    P.hcell[d] = G.hcell[d];
+    P.wrap[d] = G.wrap[d];
+    P.qscale[d] = G.qscale[d];
+    P.qinvA[d] = G.qinvA[d];
+  }
+  P.zcompact = G.zcompact;
+  P.inv_hz = G.inv_hz;
+  P.mol_reach = G.mol_reach;
+  P.ncell = G.ncell;
   P.rv2 = rc * rc;
   P.rv2lj = rclj * rclj;
   P.rlj2 = rlj * rlj;
@@ -364,7 +408,7 @@ static int derive_params(fibmd_ctx* ctx) {
   int last = 0;
   build_ref_table(p, ctx->tab.data(), ctx->tabu.data(), &umax, &last);
   char err[256] = "";
-  const int rc = derive_dev_params(p, ctx->impact, umax, last, ctx->P, err, sizeof err);
+  const int rc = derive_dev_params(p, ctx->impact, umax, last, ctx->P, ctx->geo0, err, sizeof err);
   if (rc) return fail(ctx, rc, "%s", err);
   return FIBMD_OK;
 }
@@ -500,6 +544,8 @@ int fibmd_gpu_last_error(const fibmd_ctx* ctx, char* buf, int len) {
   return FIBMD_OK;
 }
 
+static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx** out);
+
 int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   fibmd_ctx* ctx = nullptr;
   if (!p || !out) return fail(nullptr, FIBMD_EINVAL, "null argument");
@@ -528,6 +574,16 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
     delete ctx;
     return rc;
   }
+  ctx->geo.assign(1, ctx->geo0);
+  ctx->rep_of.assign((size_t)p->Natm, 0);
+  std::vector<int> ions;
+  for (int i = p->Nsg; i < p->Natm; i++) ions.push_back(i);
+  return finish_create(ctx, ions, out);
+}
+
+// Allocates and initialises the device state of a context whose P, geo and
+// rep_of are set; deletes the context on failure.
+static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx** out) {
   cudaGetDevice(&ctx->dev);
   cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, ctx->dev);
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -535,7 +591,8 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
     delete ctx;
     return FIBMD_ECUDA;
   }
-  const size_t N = (size_t)p->Natm;
+  const size_t N = (size_t)ctx->P.N;
+  const size_t R = ctx->geo.size();
   DevState& S = ctx->S;
   std::memset(&S, 0, sizeof S);
   S.N = (int)N;
@@ -580,7 +637,13 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   S.tabu = tabu;
   AL(S.epot, N);
   AL(S.partials, 3 * (size_t)kMaxRedBlocks);
-  AL(S.sc, 1);
+  AL(S.sc, R);
+  Geo* geo = nullptr;
+  int* ion_list = nullptr;
+  AL(geo, R);
+  AL(ion_list, ions.size());
+  S.geo = geo;
+  S.ion_list = ion_list;
   AL(ctx->d_stage, 3 * N);
   AL(ctx->d_u64, 4);
   AL(ctx->d_remaining, 1);
@@ -594,7 +657,11 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
                   cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(tabu, ctx->tabu.data(), sizeof(double) * ctx->tabu.size(),
                   cudaMemcpyHostToDevice, ctx->stream);
-  cudaMemsetAsync(S.sc, 0, sizeof(DevScalars), ctx->stream);
+  cudaMemcpyAsync(geo, ctx->geo.data(), sizeof(Geo) * R, cudaMemcpyHostToDevice, ctx->stream);
+  if (!ions.empty())
+    cudaMemcpyAsync(ion_list, ions.data(), sizeof(int) * ions.size(), cudaMemcpyHostToDevice,
+                    ctx->stream);
+  cudaMemsetAsync(S.sc, 0, sizeof(DevScalars) * R, ctx->stream);
   cudaMemsetAsync(S.fast_flag, 0, N, ctx->stream);
   cudaMemsetAsync(S.n_sw, 0, sizeof(int) * N, ctx->stream);
   cudaMemsetAsync(S.frc, 0, sizeof(double4_32a) * N, ctx->stream);
@@ -606,6 +673,114 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   }
   set_regime(ctx, 1);
   *out = ctx;
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica* reps,
+                           fibmd_ctx** out) {
+  if (!p || !reps || !out || nrep < 1) return fail(nullptr, FIBMD_EINVAL, "batch: bad arguments");
+  *out = nullptr;
+  if (p->abi_version != FIBMD_ABI_VERSION)
+    return fail(nullptr, FIBMD_EINVAL, "abi_version %d, library has %d", p->abi_version,
+                FIBMD_ABI_VERSION);
+  if (p->mode != FIBMD_MODE_SPEC) return fail(nullptr, FIBMD_EINVAL, "batch needs spec mode");
+  if (nrep > 65535) return fail(nullptr, FIBMD_EINVAL, "batch: %d replicas (max 65535)", nrep);
+  if (p->max_sw_nbrs > 64)
+    return fail(nullptr, FIBMD_EINVAL, "max_sw_nbrs %d exceeds 64", p->max_sw_nbrs);
+  if (p->precision == FIBMD_PREC_MIXED && (p->psi != 4.0 || p->qsi != 0.0))
+    return fail(nullptr, FIBMD_EINVAL, "mixed precision implements psi = 4, qsi = 0 only");
+  long long off = 0, nion = 0;
+  std::vector<long long> begin((size_t)nrep);
+  for (int r = 0; r < nrep; r++) {
+    const fibmd_replica& q = reps[r];
+    if (q.natm < 1 || q.nsg < 0 || q.nsg > q.natm)
+      return fail(nullptr, FIBMD_EINVAL, "replica %d: natm %d nsg %d", r, q.natm, q.nsg);
+    begin[r] = off;
+    off += q.natm;
+    off = (off + kKickThreads - 1) / kKickThreads * kKickThreads;
+    nion += q.natm - q.nsg;
+  }
+  if (off > (1ll << 30)) return fail(nullptr, FIBMD_EINVAL, "batch: %lld atoms", off);
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0)
+    return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
+
+  fibmd_ctx* ctx = new fibmd_ctx();
+  fibmd_params q = *p;
+  q.Natm = (int)off;
+  q.Nsg = (int)off;  // every ion is fired; ions are found through the ion list
+  q.Nlj = (int)nion;
+  for (int d = 0; d < 3; d++) q.Lb[d] = reps[0].Lb[d];
+  q.remove_z = reps[0].remove_z;
+  ctx->p = q;
+  int rc = derive_params(ctx);
+  if (rc) {
+    set_noctx_error(ctx->err.c_str());
+    delete ctx;
+    return rc;
+  }
+  ctx->geo.resize((size_t)nrep);
+  ctx->rep_of.assign((size_t)off, -1);
+  std::vector<int> ions;
+  long long cells = 0;
+  int reach = 1;
+  for (int r = 0; r < nrep; r++) {
+    char err[256] = "";
+    Geo& G = ctx->geo[(size_t)r];
+    rc = derive_geo(q, reps[r].Lb, reps[r].remove_z, G, err, sizeof err);
+    if (rc) {
+      set_noctx_error(err);
+      delete ctx;
+      return rc;
+    }
+    G.cell_off = (int)cells;
+    cells += G.ncell;
+    G.atom_begin = (int)begin[r];
+    G.atom_end = (int)(begin[r] + reps[r].natm);
+    G.blk_begin = G.atom_begin / kKickThreads;
+    G.blk_end = (G.atom_end + kKickThreads - 1) / kKickThreads;
+    reach = std::max(reach, G.mol_reach);
+    for (int i = G.atom_begin; i < G.atom_end; i++) ctx->rep_of[(size_t)i] = r;
+    for (int i = G.atom_begin + reps[r].nsg; i < G.atom_end; i++) ions.push_back(i);
+  }
+  if (cells > (1ll << 30) || off / kKickThreads > kMaxRedBlocks) {
+    set_noctx_error("batch: too many cells or atoms");
+    delete ctx;
+    return FIBMD_EINVAL;
+  }
+  DevParams& P = ctx->P;
+  P.nrep = nrep;
+  P.nion = (int)ions.size();
+  P.nfired = (int)off;
+  P.ncell = (int)cells;
+  P.mol_reach = reach;
+  return finish_create(ctx, ions, out);
+}
+
+int fibmd_gpu_batch_layout(fibmd_ctx* ctx, int* nrep, int* offsets) {
+  if (!ctx) return FIBMD_EINVAL;
+  const int R = (int)ctx->geo.size();
+  if (nrep) *nrep = R;
+  if (offsets) {
+    for (int r = 0; r < R; r++) offsets[r] = ctx->geo[(size_t)r].atom_begin;
+    offsets[R] = ctx->P.N;
+  }
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_batch_scalars(fibmd_ctx* ctx, double* time, double* dt, int* removed) {
+  if (!ctx) return FIBMD_EINVAL;
+  const size_t R = ctx->geo.size();
+  std::vector<DevScalars> h(R);
+  CK(cudaMemcpyAsync(h.data(), ctx->S.sc, sizeof(DevScalars) * R, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (size_t r = 0; r < R; r++) {
+    if (time) time[r] = h[r].time;
+    if (dt) dt[r] = h[r].dt;
+    if (removed) removed[r] = h[r].removed_count;
+  }
   return FIBMD_OK;
 }
 
@@ -632,6 +807,22 @@ void fibmd_gpu_destroy(fibmd_ctx* ctx) {
 
 void* fibmd_gpu_stream(fibmd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
+// Per-atom flags word: the tag bits and the atom's replica in bits 16..31;
+// padding slots of a batch are removed atoms of the replica before them.
+static uint32_t replica_flags(const fibmd_ctx* ctx, int i, uint32_t tag) {
+  int r = ctx->rep_of[(size_t)i];
+  if (r < 0) {
+    r = 0;
+    for (int k = i; k >= 0; k--)
+      if (ctx->rep_of[(size_t)k] >= 0) {
+        r = ctx->rep_of[(size_t)k];
+        break;
+      }
+    tag = FL_REMOVED;
+  }
+  return (tag & 0xffu) | ((uint32_t)r << 16);
+}
+
 int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const double* F,
                      const double* Xi, const double* mass, const int* atype,
                      const int* xsides) {
@@ -646,7 +837,7 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
     if (atype[i] < 1 || atype[i] > 3)
       return fail(ctx, FIBMD_EINVAL, "atype(%d) = %d is not 1, 2 or 3", i + 1, atype[i]);
     t8[i] = (int8_t)atype[i];
-    fl[i] = xsides[i] > 0 ? FL_FROZEN : 0u;
+    fl[i] = replica_flags(ctx, i, xsides[i] > 0 ? FL_FROZEN : 0u);
   }
   const double* src[4] = {X, V, F, Xi};
   double4_32a* dst[4] = {ctx->S.pos, ctx->S.vel, ctx->S.frc, ctx->S.xi};
@@ -681,8 +872,11 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
 int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags) {
   if (!ctx || !tags) return FIBMD_EINVAL;
   const int N = ctx->P.N;
-  CK(cudaMemcpyAsync(ctx->S.flags, tags, sizeof(uint32_t) * (size_t)N, cudaMemcpyHostToDevice,
-                     ctx->stream));
+  std::vector<uint32_t> fl((size_t)N);
+  for (int i = 0; i < N; i++) fl[i] = replica_flags(ctx, i, tags[i] & 0xffu);
+  CK(cudaMemcpyAsync(ctx->S.flags, fl.data(), sizeof(uint32_t) * (size_t)N,
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   CK(launch_update_posq(launch_of(ctx), ctx->P, ctx->S));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->spec_ready = false;
@@ -1129,9 +1323,10 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
   const DevParams& P = ctx->P;
   const double Ttar = ctx->p.Ttar1;
   if (!ctx->spec_ready) {
-    double t0 = *time;
-    CK(cudaMemcpyAsync(&ctx->S.sc->time, &t0, sizeof(double), cudaMemcpyHostToDevice,
-                       ctx->stream));
+    const double t0 = *time;
+    for (int r = 0; r < P.nrep; r++)
+      CK(cudaMemcpyAsync(&ctx->S.sc[r].time, &t0, sizeof(double), cudaMemcpyHostToDevice,
+                         ctx->stream));
     CK(launch_spec_kick(L, P, ctx->S, Ttar, 0));
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->spec_ready = true;

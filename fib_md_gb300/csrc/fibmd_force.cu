@@ -83,6 +83,9 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
   if (n == 0) return;
   const double4_32a pi = S.pos[i];
   const int ta = ti - 1;
+  const Geo& G = S.geo[rep_of_w(qi.w)];
+  const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
+  const double Lb[3] = {G.Lb[0], G.Lb[1], G.Lb[2]}, iLb[3] = {G.iLb[0], G.iLb[1], G.iLb[2]};
 
   double fx = 0.0, fy = 0.0, fz = 0.0, ui = 0.0;
   int nl = 0, terr = 0;
@@ -99,14 +102,14 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
     for (int u = 0; u < kBatch; u++) {
       if (k0 + u >= n) break;
       const int j = jj[u];
-      const float3 dq = qsep(qi, qq[u], P.qinvA);
+      const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
       if (r2f > P.pre3A2) continue;  // beyond the table support and 3-body cutoff
       const int tb = (qq[u].w & 0xff) - 1;
       const double4_32a pj = S.pos[j];
-      const double dx = min_image(pi.x, pj.x, P.iLb[0], P.Lb[0]);
-      const double dy = min_image(pi.y, pj.y, P.iLb[1], P.Lb[1]);
-      const double dz = min_image(pi.z, pj.z, P.iLb[2], P.Lb[2]);
+      const double dx = min_image(pi.x, pj.x, iLb[0], Lb[0]);
+      const double dy = min_image(pi.y, pj.y, iLb[1], Lb[1]);
+      const double dz = min_image(pi.z, pj.z, iLb[2], Lb[2]);
       const double r2 = dx * dx + dy * dy + dz * dz;
       const double r = sqrt(r2);
       const double rinv = 1.0 / r;
@@ -238,6 +241,8 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
   const int n = S.n_sw[i];
   if (n == 0) return;
   const int ta = ti - 1;
+  const Geo& G = S.geo[rep_of_w(qi.w)];
+  const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
   const float al = (float)P.al, cut = (float)P.cut3, gm = (float)P.gam;
   const float Bc = (float)P.B, Ac = (float)P.A;
 
@@ -255,7 +260,7 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
 #pragma unroll
     for (int u = 0; u < kBatch; u++) {
       if (k0 + u >= n) break;
-      const float3 dq = qsep(qi, qq[u], P.qinvA);
+      const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
       if (r2f > P.pre3A2) continue;
       const int tb = (qq[u].w & 0xff) - 1;
@@ -360,12 +365,13 @@ struct Leg64 {
   int t;
 };
 
-__device__ __forceinline__ Leg64 make_leg(const DevParams& P, const double4_32a& pc,
-                                          const double4_32a& pl, int tc, int tl) {
+__device__ __forceinline__ Leg64 make_leg(const DevParams& P, const Geo& G,
+                                          const double4_32a& pc, const double4_32a& pl,
+                                          int tc, int tl) {
   Leg64 L;
-  L.dx = min_image(pc.x, pl.x, P.iLb[0], P.Lb[0]);
-  L.dy = min_image(pc.y, pl.y, P.iLb[1], P.Lb[1]);
-  L.dz = min_image(pc.z, pl.z, P.iLb[2], P.Lb[2]);
+  L.dx = min_image(pc.x, pl.x, G.iLb[0], G.Lb[0]);
+  L.dy = min_image(pc.y, pl.y, G.iLb[1], G.Lb[1]);
+  L.dz = min_image(pc.z, pl.z, G.iLb[2], G.Lb[2]);
   L.r = sqrt(L.dx * L.dx + L.dy * L.dy + L.dz * L.dz);
   L.isig = P.isig[tc - 1][tl - 1];
   L.u = L.r * L.isig;
@@ -424,13 +430,14 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     const int c = S.heavy_list[h];
     const int tc = S.atype[c];
     const int n = S.n_sw[c];
+    const Geo& G = S.geo[rep_of_flags(S.flags[c])];
     if (lane == 0) snl[w] = 0;
     __syncwarp();
     for (int k = lane; k < n; k += 32) {
       const int j = S.nbr_sw[(size_t)k * P.N + c];
       const int tj = S.atype[j];
       if constexpr (MIXED) {
-        const float3 dq = qsep(S.posq[c], S.posq[j], P.qinvA);
+        const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
         const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
         const float rinv = rsqrtf(r2);
         const float sg = P.sigA[tc - 1][tj - 1];
@@ -448,7 +455,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
         sl[w][5][q] = -(float)P.gam * ia * ia / sg;
         sj[w][q] = j | ((tj - 1) << 30);
       } else {
-        const Leg64 L = make_leg(P, S.pos[c], S.pos[j], tc, tj);
+        const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);
         if (!(L.u < P.cut3)) continue;
         const int q = atomicAdd(&snl[w], 1);
         const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
@@ -531,6 +538,7 @@ __global__ void k_force_stale(DevParams P, DevState S) {
     const double4_32a pf = S.pos[f];
     const int4 qf = S.posq[f];
     const int nf = S.n_sw[f];
+    const Geo& G = S.geo[rep_of_w(qf.w)];
     unsigned int terms = 0;
     for (int ia = 0; ia < nf; ia++) {
       const int a = S.nbr_sw[(size_t)ia * P.N + f];
@@ -539,7 +547,7 @@ __global__ void k_force_stale(DevParams P, DevState S) {
         const int x = S.nbr_sw[(size_t)ix * P.N + a];
         if (x == f) continue;
         const int4 qx = S.posq[x];
-        const float3 dq = qsep(qf, qx, P.qinvA);
+        const float3 dq = qsep(qf, qx, G.qinvA);
         if (dq.x * dq.x + dq.y * dq.y + dq.z * dq.z > P.pre3A2) continue;
         if (S.fast_flag[x] && x < f) continue;  // the pair is handled from x
         if (in_list(P, S, f, x)) continue;
@@ -548,8 +556,8 @@ __global__ void k_force_stale(DevParams P, DevState S) {
         double f0[3], f1[3], f2[3], e;
         // centre f, legs a and x
         {
-          const Leg64 A = make_leg(P, pf, pa, tf, ta);
-          const Leg64 X = make_leg(P, pf, px, tf, tx);
+          const Leg64 A = make_leg(P, G, pf, pa, tf, ta);
+          const Leg64 X = make_leg(P, G, pf, px, tf, tx);
           if (angle_term(P, tf, A, X, f0, f1, f2, &e)) {
             atomic_add3(S.frc_new, f, f0[0], f0[1], f0[2]);
             atomic_add3(S.frc_new, a, f1[0], f1[1], f1[2]);
@@ -564,8 +572,8 @@ __global__ void k_force_stale(DevParams P, DevState S) {
         }
         // centre x, legs a and f
         {
-          const Leg64 A = make_leg(P, px, pa, tx, ta);
-          const Leg64 Fl = make_leg(P, px, pf, tx, tf);
+          const Leg64 A = make_leg(P, G, px, pa, tx, ta);
+          const Leg64 Fl = make_leg(P, G, px, pf, tx, tf);
           if (angle_term(P, tx, A, Fl, f0, f1, f2, &e)) {
             atomic_add3(S.frc_new, x, f0[0], f0[1], f0[2]);
             atomic_add3(S.frc_new, a, f1[0], f1[1], f1[2]);
@@ -599,9 +607,10 @@ __global__ void k_force_moliere(DevParams P, DevState S) {
     if (!ENERGY && !fired) continue;
     const int ti = S.atype[i] - 1, tj = S.atype[j] - 1;
     const double4_32a pi = S.pos[i], pj = S.pos[j];
-    const double dx = min_image(pi.x, pj.x, P.iLb[0], P.Lb[0]);
-    const double dy = min_image(pi.y, pj.y, P.iLb[1], P.Lb[1]);
-    const double dz = min_image(pi.z, pj.z, P.iLb[2], P.Lb[2]);
+    const Geo& G = S.geo[rep_of_flags(S.flags[i])];
+    const double dx = min_image(pi.x, pj.x, G.iLb[0], G.Lb[0]);
+    const double dy = min_image(pi.y, pj.y, G.iLb[1], G.Lb[1]);
+    const double dz = min_image(pi.z, pj.z, G.iLb[2], G.Lb[2]);
     const double r2 = dx * dx + dy * dy + dz * dz;
     if (!(r2 < P.rlj2)) continue;
     if (fired) npair++;

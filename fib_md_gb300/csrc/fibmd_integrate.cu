@@ -28,9 +28,9 @@ __device__ __forceinline__ bool ref_side_atom(const DevParams& P, double x, doub
 // displacement is taken between fixed-point positions, whose wrapping
 // difference is the minimum image; its binary32 error (~1e-7 A) is far
 // inside the 1% margin of the threshold.
-__device__ __forceinline__ float track_displacement(const DevParams& P, const DevState& S,
-                                                    int i, const int4& q) {
-  const float3 d = qsep(q, S.posq_build[i], P.qinvA);
+__device__ __forceinline__ float track_displacement(const DevParams& P, const Geo& G,
+                                                    const DevState& S, int i, const int4& q) {
+  const float3 d = qsep(q, S.posq_build[i], G.qinvA);
   const float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
   if (P.mode == FIBMD_MODE_REF && d2 >= P.disp_fastA2 && !S.fast_flag[i]) {
     S.fast_flag[i] = 1;
@@ -40,13 +40,13 @@ __device__ __forceinline__ float track_displacement(const DevParams& P, const De
   return d2;
 }
 
-__device__ __forceinline__ int4 store_posq(const DevParams& P, const DevState& S, int i,
-                                           double x, double y, double z, uint32_t fl) {
+__device__ __forceinline__ int4 store_posq(const Geo& G, const DevState& S, int i, double x,
+                                           double y, double z, uint32_t fl) {
   int4 q;
-  q.x = (int)fixq(x, P.qscale[0]);
-  q.y = (int)fixq(y, P.qscale[1]);
-  q.z = (int)fixq(z, P.qscale[2]);
-  q.w = (int)(uint8_t)S.atype[i] | (int)(fl << 8);
+  q.x = (int)fixq(x, G.qscale[0]);
+  q.y = (int)fixq(y, G.qscale[1]);
+  q.z = (int)fixq(z, G.qscale[2]);
+  q.w = posq_w(S.atype[i], fl);
   S.posq[i] = q;
   return q;
 }
@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(256) k_drift(DevParams P, DevState S, double T
   x.z = rebox1(x.z, P.Lb[2]);
   S.pos[i] = x;
   S.vel[i] = v;
-  const int4 q = store_posq(P, S, i, x.x, x.y, x.z, fl);
-  track_displacement(P, S, i, q);
+  const Geo& G = S.geo[0];
+  const int4 q = store_posq(G, S, i, x.x, x.y, x.z, fl);
+  track_displacement(P, G, S, i, q);
 }
 
 cudaError_t launch_drift(const Launch& L, const DevParams& P, const DevState& S, double Ts,
@@ -205,8 +206,9 @@ __global__ void __launch_bounds__(256) k_park(DevParams P, DevState S) {
   S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
   if (moved) {
     S.pos[i] = x;
-    const int4 q = store_posq(P, S, i, x.x, x.y, x.z, S.flags[i]);
-    track_displacement(P, S, i, q);
+    const Geo& G = S.geo[0];
+    const int4 q = store_posq(G, S, i, x.x, x.y, x.z, S.flags[i]);
+    track_displacement(P, G, S, i, q);
   }
 }
 
@@ -260,7 +262,8 @@ cudaError_t launch_ke_max(const Launch& L, const DevParams& P, const DevState& S
 __global__ void k_track_all(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
-  track_displacement(P, S, i, S.posq[i]);
+  const int4 q = S.posq[i];
+  track_displacement(P, S.geo[rep_of_w(q.w)], S, i, q);
 }
 
 cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S) {
@@ -321,15 +324,18 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // remove_z, and the rebuild trigger at half the list skin.
 __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const double dt = ((volatile DevScalars*)S.sc)->dt;
   bool trig = false;
   if (i < P.N) {
     uint32_t fl = S.flags[i];
     if (!(fl & FL_REMOVED)) {
+      const int r = rep_of_flags(fl);
+      const Geo& G = S.geo[r];
+      DevScalars* R = S.sc + r;
+      const double dt = ((volatile DevScalars*)R)->dt;
       double4_32a x = S.pos[i];
       double4_32a v = S.vel[i];
       if (fl & FL_THERMO) {
-        const double s = S.sc->thermo_s;
+        const double s = R->thermo_s;
         v.x *= s;
         v.y *= s;
         v.z *= s;
@@ -348,25 +354,25 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
       }
       // removal looks at the unwrapped height, so an atom leaving through
       // the bottom of a periodic box is not taken for a sputtered one
-      const bool removed = P.remove_z > 0.0 && x.z > P.remove_z && S.atype[i] < 3;
+      const bool removed = G.remove_z > 0.0 && x.z > G.remove_z && S.atype[i] < 3;
       // spec mode has no bit-compatibility constraint with the reference's
       // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped; with the
       // cell grid cut at remove_z, z is an open axis and is not wrapped
-      x.x = x.x < 0.0 ? x.x + P.Lb[0] : (x.x >= P.Lb[0] ? x.x - P.Lb[0] : x.x);
-      x.y = x.y < 0.0 ? x.y + P.Lb[1] : (x.y >= P.Lb[1] ? x.y - P.Lb[1] : x.y);
-      if (!P.zcompact)
-        x.z = x.z < 0.0 ? x.z + P.Lb[2] : (x.z >= P.Lb[2] ? x.z - P.Lb[2] : x.z);
+      x.x = x.x < 0.0 ? x.x + G.Lb[0] : (x.x >= G.Lb[0] ? x.x - G.Lb[0] : x.x);
+      x.y = x.y < 0.0 ? x.y + G.Lb[1] : (x.y >= G.Lb[1] ? x.y - G.Lb[1] : x.y);
+      if (!G.zcompact)
+        x.z = x.z < 0.0 ? x.z + G.Lb[2] : (x.z >= G.Lb[2] ? x.z - G.Lb[2] : x.z);
       if (removed) {
         fl |= FL_REMOVED;
         S.flags[i] = fl;
         v.x = v.y = v.z = 0.0;
         trig = true;
-        atomicAdd(&S.sc->removed_count, 1);
+        atomicAdd(&R->removed_count, 1);
       }
       S.pos[i] = x;
       S.vel[i] = v;
-      const int4 q = store_posq(P, S, i, x.x, x.y, x.z, fl);
-      if (track_displacement(P, S, i, q) >= P.disp_fastA2) trig = true;
+      const int4 q = store_posq(G, S, i, x.x, x.y, x.z, fl);
+      if (track_displacement(P, G, S, i, q) >= P.disp_fastA2) trig = true;
     }
   }
   if (__syncthreads_or(trig) && threadIdx.x == 0) S.sc->need_rebuild = 1;
@@ -385,15 +391,15 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 // (the max through the bit order of non-negative doubles, integer shuffles);
 // k_spec_finalize reduces them in block order and derives dt and the
 // Berendsen factor. No atomics, so the result does not depend on timing.
-constexpr int kKickThreads = 256;
-
 __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply) {
-  const double dt = ((volatile DevScalars*)S.sc)->dt;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double v2 = 0.0, ts = 0.0, tc = 0.0;
   if (i < P.N) {
     const uint32_t fl = S.flags[i];
     if (!(fl & FL_REMOVED)) {
+      // a kick block lies inside one replica (replicas start at multiples
+      // of the block size)
+      const double dt = ((volatile DevScalars*)(S.sc + rep_of_flags(fl)))->dt;
       double4_32a v = S.vel[i];
       if (apply) {
         const double4_32a f = S.frc[i];
@@ -445,11 +451,13 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
   }
 }
 
+// One block per replica, over the replica's kick blocks.
 __global__ void __launch_bounds__(256) k_spec_finalize(DevParams P, DevState S, int apply,
-                                                       double Ttar, int nblocks) {
+                                                       double Ttar) {
+  const Geo& G = S.geo[blockIdx.x];
   double v[2] = {0.0, 0.0};
   double mx = 0.0;
-  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) {
+  for (int b = G.blk_begin + threadIdx.x; b < G.blk_end; b += blockDim.x) {
     mx = fmax(mx, S.partials[b]);
     v[0] += S.partials[kMaxRedBlocks + b];
     v[1] += S.partials[2 * kMaxRedBlocks + b];
@@ -457,7 +465,7 @@ __global__ void __launch_bounds__(256) k_spec_finalize(DevParams P, DevState S, 
   mx = block_max(mx);
   block_sum<2>(v);
   if (threadIdx.x != 0) return;
-  DevScalars* sc = S.sc;
+  DevScalars* sc = S.sc + blockIdx.x;
   const double tsum = v[0], tcnt = v[1];
   sc->thermo_sum = tsum;
   sc->thermo_cnt = tcnt;
@@ -481,7 +489,7 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
   k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply);
-  k_spec_finalize<<<1, 256, 0, L.stream>>>(P, S, apply, Ttar, nb);
+  k_spec_finalize<<<P.nrep, 256, 0, L.stream>>>(P, S, apply, Ttar);
   return cudaGetLastError();
 }
 

@@ -4,7 +4,9 @@
 // HBM layout (one context, N atoms, 0-based index = Fortran index - 1):
 //   pos, vel, frc, frc_new, xi : double4_32a[N]  (x, y, z, unused)
 //   posq      : int4[N]   fixed-point positions, x = round(x/Lb * 2^32) mod
-//               2^32, w = atype | flags << 8. Differences of two fixed-point
+//               2^32, w = atype | (flags & 0xff) << 8 | replica << 16
+//               (flags bits 16..31 hold the atom's replica, 0 for a single
+//               system). Differences of two fixed-point
 //               coordinates wrap modulo 2^32, which is the minimum image, and
 //               convert to binary32 with the precision of the separation
 //               itself (not of the absolute coordinate).
@@ -26,6 +28,7 @@ namespace fibmd {
 constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
 constexpr int kMaxRedBlocks = 16384;  // row stride of the reduction partials
+constexpr int kKickThreads = 256;  // spec kick block; replicas start at multiples
 
 enum : uint32_t {
   FL_FROZEN = 1u,   // xsides > 0 (ref) / FIBMD_TAG_FROZEN (spec)
@@ -33,9 +36,36 @@ enum : uint32_t {
   FL_REMOVED = 4u,  // spec-mode sputtered and removed
 };
 
+// Box and cell geometry of one replica. A context holds one system
+// (replica 0) or a batch of independent replicas, each with its own box,
+// cell grid (a slice of the context's cells) and atom range; kernels that
+// handle atoms of any replica read their geometry here.
+struct Geo {
+  double Lb[3], iLb[3], hcell[3];
+  double qscale[3];   // 2^32 / Lb
+  double inv_hz;      // 1 / cell height in z (open z axis)
+  double remove_z;    // spec mode: atoms above are removed (<= 0: never)
+  float qinvA[3];     // Lb / 2^32 in Angstrom
+  int nc[3];
+  int wrap[3];        // periodic cell stencil per axis (the reference: Nc > 2)
+  int zcompact;       // spec mode: open z axis, cell grid over [0, zext)
+  int mol_reach;      // cells scanned for Moliere pairs (spec mode)
+  int cell_off, ncell;      // this replica's cells in the context's grid
+  int atom_begin, atom_end;  // its atoms
+  int blk_begin, blk_end;    // its kick blocks (kKickThreads atoms each)
+};
+
+__device__ __forceinline__ int rep_of_w(int w) { return (int)((unsigned)w >> 16); }
+__device__ __forceinline__ int rep_of_flags(uint32_t fl) { return (int)(fl >> 16); }
+__device__ __forceinline__ int posq_w(int8_t type, uint32_t fl) {
+  return (int)(uint8_t)type | (int)((fl & 0xffu) << 8) | (int)(fl & 0xffff0000u);
+}
+
 // Derived constants handed to every kernel by value.
 struct DevParams {
   int N, Nsg, nfired;  // atoms with index >= nfired are unfired ions
+  int nrep;            // replicas (1: a single system)
+  int nion;            // ions (entries of DevState::ion_list)
   int mode, precision;
   int max_sw;
   int mol_cap;
@@ -148,7 +178,10 @@ struct DevState {
   double* epot;
   // reductions
   double* partials;
-  DevScalars* sc;
+  DevScalars* sc;    // one per replica; context-wide fields live in sc[0]
+  // replicas
+  const Geo* geo;    // nrep entries
+  const int* ion_list;  // the ions (atype 3), ascending
 };
 
 // ---- small device helpers ------------------------------------------------
@@ -305,9 +338,14 @@ void set_noctx_error(const char* msg);
 // mktables into caller buffers of Ntable + 2 entries.
 void build_ref_table(const fibmd_params& p, double* tab, double* tabu, double* umax,
                      int* last_nz);
-// init_nlist/setupSiGe/setupMol constants for the kernels; allocates nothing.
+// Box and cell geometry of one replica with box Lb and removal height
+// remove_z (the list radii and mode come from p); allocates nothing.
+int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& G, char* err,
+               int errlen);
+// init_nlist/setupSiGe/setupMol constants for the kernels, and the
+// geometry G of the single system p describes; allocates nothing.
 int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_last,
-                      DevParams& P, char* err, int errlen);
+                      DevParams& P, Geo& G, char* err, int errlen);
 
 // ---- launchers (defined in the .cu files) --------------------------------
 struct Launch {

@@ -18,11 +18,13 @@ __global__ void k_update_posq(DevParams P, DevState S) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
   double4_32a p = S.pos[i];
+  const uint32_t fl = S.flags[i];
+  const Geo& G = S.geo[rep_of_flags(fl)];
   int4 q;
-  q.x = (int)fixq(p.x, P.qscale[0]);
-  q.y = (int)fixq(p.y, P.qscale[1]);
-  q.z = (int)fixq(p.z, P.qscale[2]);
-  q.w = (int)(uint8_t)S.atype[i] | (int)(S.flags[i] << 8);
+  q.x = (int)fixq(p.x, G.qscale[0]);
+  q.y = (int)fixq(p.y, G.qscale[1]);
+  q.z = (int)fixq(p.z, G.qscale[2]);
+  q.w = posq_w(S.atype[i], fl);
   S.posq[i] = q;
 }
 
@@ -57,9 +59,9 @@ __global__ void k_build_begin(DevParams P, DevState S, int from_flag) {
 // two agree except within ~nc 2^-33 of a cell boundary; there (fraction
 // within 1e-6 of a boundary) the reference's binary64 formula decides, so
 // the cell of every atom is the reference's.
-__device__ __forceinline__ int ref_cell(const DevParams& P, double x, int d) {
-  const double fl = floor(__dmul_rn(x, P.iLb[d]));
-  const double t = __ddiv_rn(__dsub_rn(x, __dmul_rn(fl, P.Lb[d])), P.hcell[d]);
+__device__ __forceinline__ int ref_cell(const Geo& G, double x, int d) {
+  const double fl = floor(__dmul_rn(x, G.iLb[d]));
+  const double t = __ddiv_rn(__dsub_rn(x, __dmul_rn(fl, G.Lb[d])), G.hcell[d]);
   return (int)t;
 }
 
@@ -75,34 +77,35 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
     S.fast_flag[i] = 0;
     return;
   }
+  const Geo& G = S.geo[rep_of_w(q.w)];
   const unsigned qq[3] = {(unsigned)q.x, (unsigned)q.y, (unsigned)q.z};
   constexpr unsigned kGuard = 4295u;  // 1e-6 of a cell, in units of 2^-32
   int ic[3];
   bool oob = false;
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    const unsigned long long t = (unsigned long long)qq[d] * (unsigned long long)P.nc[d];
+    const unsigned long long t = (unsigned long long)qq[d] * (unsigned long long)G.nc[d];
     int c = (int)(t >> 32);
     const unsigned frac = (unsigned)t;
-    if (d == 2 && P.zcompact) {
+    if (d == 2 && G.zcompact) {
       // spec mode with an open z axis: the grid covers [0, remove_z + rc);
       // an atom above it (an ion: other atoms there are removed) joins the
       // top layer and an atom below z = 0 the bottom one, which hold every
       // atom within rc of it
-      const double zc = S.pos[i].z * P.inv_hz;
-      c = zc < 0.0 ? 0 : (zc >= (double)P.nc[2] ? P.nc[2] - 1 : (int)zc);
+      const double zc = S.pos[i].z * G.inv_hz;
+      c = zc < 0.0 ? 0 : (zc >= (double)G.nc[2] ? G.nc[2] - 1 : (int)zc);
     } else if (frac < kGuard || frac > 0xffffffffu - kGuard) {
       const double4_32a p = S.pos[i];
-      c = ref_cell(P, d == 0 ? p.x : d == 1 ? p.y : p.z, d);
+      c = ref_cell(G, d == 0 ? p.x : d == 1 ? p.y : p.z, d);
     }
-    if (c < 0 || c >= P.nc[d]) {
+    if (c < 0 || c >= G.nc[d]) {
       oob = true;
-      c = c < 0 ? 0 : P.nc[d] - 1;
+      c = c < 0 ? 0 : G.nc[d] - 1;
     }
     ic[d] = c;
   }
   if (oob) atomicAdd(&S.sc->cell_oob, 1);
-  const int cell = ic[0] + P.nc[0] * (ic[1] + P.nc[1] * ic[2]);
+  const int cell = G.cell_off + ic[0] + G.nc[0] * (ic[1] + G.nc[1] * ic[2]);
   S.atom_cell[i] = cell;
   atomicAdd(&S.cell_count[cell], 1);
 }
@@ -205,12 +208,12 @@ __global__ void k_cell_fill(DevParams P, DevState S, int from_flag) {
 // ---- pair lists (si_nlistG pair loop, si.f90:130-189) ---------------------
 // Exact list membership of a candidate already inside the FP32 prefilter
 // band: the reference's binary64 minimum-image distance decides.
-__device__ __forceinline__ bool exact_in(const DevParams& P, const DevState& S, int i, int j,
+__device__ __forceinline__ bool exact_in(const Geo& G, const DevState& S, int i, int j,
                                          double rv2) {
   const double4_32a pi = S.pos[i], pj = S.pos[j];
-  const double xx = min_image_exact(pi.x, pj.x, P.iLb[0], P.Lb[0]);
-  const double yy = min_image_exact(pi.y, pj.y, P.iLb[1], P.Lb[1]);
-  const double zz = min_image_exact(pi.z, pj.z, P.iLb[2], P.Lb[2]);
+  const double xx = min_image_exact(pi.x, pj.x, G.iLb[0], G.Lb[0]);
+  const double yy = min_image_exact(pi.y, pj.y, G.iLb[1], G.Lb[1]);
+  const double zz = min_image_exact(pi.z, pj.z, G.iLb[2], G.Lb[2]);
   const double r2 = __dadd_rn(__dadd_rn(__dmul_rn(xx, xx), __dmul_rn(yy, yy)), __dmul_rn(zz, zz));
   return r2 < rv2;
 }
@@ -244,12 +247,14 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
   const size_t stride = (size_t)P.N;
   int n = 0;
   if (!(WIDE && ti == 3)) {
-    const int c = S.atom_cell[i];
-    const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
+    const Geo& G = S.geo[rep_of_w(qi.w)];
+    const int c = S.atom_cell[i] - G.cell_off;
+    const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
+    const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
     // inclusive x ranges of the stencil row (periodic only with > 2 cells)
     int xa0, xa1, xb0 = 0, xb1 = -1;
-    if (P.wrap[0]) {
+    if (G.wrap[0]) {
       if (cx == 0) {
         xa0 = 0; xa1 = 1; xb0 = xb1 = nx - 1;
       } else if (cx == nx - 1) {
@@ -267,13 +272,13 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
     const int4* __restrict__ qc = S.posq_cell;
     for (int dz = -1; dz <= 1; dz++) {
       int z = cz + dz;
-      if (P.wrap[2]) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
+      if (G.wrap[2]) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
       else if (z < 0 || z >= nz) continue;
       for (int dy = -1; dy <= 1; dy++) {
         int y = cy + dy;
-        if (P.wrap[1]) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+        if (G.wrap[1]) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
         else if (y < 0 || y >= ny) continue;
-        const int row = nx * (y + ny * z);
+        const int row = G.cell_off + nx * (y + ny * z);
         for (int part = 0; part < 2; part++) {
           const int x0 = part ? xb0 : xa0, x1 = part ? xb1 : xa1;
           if (x1 < x0) break;
@@ -288,7 +293,7 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
               const int p = p0 + u;
               if (p >= e) break;
               const int4 qj = u ? q1 : q0;
-              const float3 d = qsep(qi, qj, P.qinvA);
+              const float3 d = qsep(qi, qj, qinvA);
               const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
               if (r2f > thr || p == h) continue;
               bool sw = true;
@@ -298,7 +303,7 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
                 if (sw && r2f > thr_sw) continue;
               }
               if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) &&
-                  !exact_in(P, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
+                  !exact_in(G, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
                 continue;
               if (sw) {
                 if (n < kBuildBuf) buf[n][t] = p;
@@ -333,35 +338,36 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
 __global__ void __launch_bounds__(128) k_build_ion_pairs(DevParams P, DevState S,
                                                          int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  const int nion = P.N - P.Nsg;
-  const int nx = P.nc[0], ny = P.nc[1], nz = P.nc[2];
-  const int R = P.mol_reach, W = 2 * R + 1;
-  for (int k = blockIdx.x; k < nion; k += gridDim.x) {
-    const int i = P.Nsg + k;
+  for (int k = blockIdx.x; k < P.nion; k += gridDim.x) {
+    const int i = S.ion_list[k];
     const int4 qi = S.posq[i];
-    const int ci = S.atom_cell[i];
-    if ((qi.w & 0xff) != 3 || ci < 0) continue;
+    const int ci0 = S.atom_cell[i];
+    if ((qi.w & 0xff) != 3 || ci0 < 0) continue;
+    const Geo& G = S.geo[rep_of_w(qi.w)];
+    const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
+    const int R = G.mol_reach, W = 2 * R + 1;
+    const int ci = ci0 - G.cell_off;
     const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
     for (int s = threadIdx.x; s < W * W * W; s += blockDim.x) {
       const int ox = s % W, oy = (s / W) % W, oz = s / (W * W);
       int x = cx + ox - R, y = cy + oy - R, z = cz + oz - R;
       // a stencil wider than a periodic axis would visit a cell twice
-      if (P.wrap[0]) { if (ox >= nx) continue; x = ((x % nx) + nx) % nx; }
+      if (G.wrap[0]) { if (ox >= nx) continue; x = ((x % nx) + nx) % nx; }
       else if (x < 0 || x >= nx) continue;
-      if (P.wrap[1]) { if (oy >= ny) continue; y = ((y % ny) + ny) % ny; }
+      if (G.wrap[1]) { if (oy >= ny) continue; y = ((y % ny) + ny) % ny; }
       else if (y < 0 || y >= ny) continue;
-      if (P.wrap[2]) { if (oz >= nz) continue; z = ((z % nz) + nz) % nz; }
+      if (G.wrap[2]) { if (oz >= nz) continue; z = ((z % nz) + nz) % nz; }
       else if (z < 0 || z >= nz) continue;
-      const int c = x + nx * (y + ny * z);
+      const int c = G.cell_off + x + nx * (y + ny * z);
       const int b = S.cell_start[c], e = S.cell_start[c + 1];
       for (int p = b; p < e; p++) {
         const int j = S.cell_atoms[p];
         if (j == i) continue;
         const int4 qj = S.posq[j];  // posq_cell holds ions shifted
-        const float3 d = qsep(qi, qj, P.qinvA);
+        const float3 d = qsep(qi, qj, G.qinvA);
         const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
         if (r2f > P.pre_mol2A) continue;
-        if (r2f >= P.acc_mol2A && !exact_in(P, S, i, j, P.rv2lj)) continue;
+        if (r2f >= P.acc_mol2A && !exact_in(G, S, i, j, P.rv2lj)) continue;
         const bool ion_j = (qj.w & 0xff) == 3;
         const int nw = ion_j ? 1 : 2;
         const int slot = atomicAdd(&S.sc->mol_count, nw);
@@ -398,8 +404,8 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
     k_build_atoms<true><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
   else
     k_build_atoms<false><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
-  if (P.mol_reach > 1 && P.N > P.Nsg)
-    k_build_ion_pairs<<<min(P.N - P.Nsg, 4096), 128, 0, L.stream>>>(P, S, from_flag);
+  if (P.mol_reach > 1 && P.nion > 0)
+    k_build_ion_pairs<<<min(P.nion, 4096), 128, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);
   return cudaGetLastError();
 }

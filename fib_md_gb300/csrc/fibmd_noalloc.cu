@@ -39,7 +39,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 struct Layout {
   size_t pos, frc_new, posq, posq_build, posq_cell, atype, flags, cell_count, cell_start,
       cell_atoms, atom_cell, scan_blocks, nbr_sw, n_sw, mol_pairs, fast_flag,
-      fast_list, heavy_list, tab, tabu, partials, sc, total;
+      fast_list, heavy_list, tab, tabu, partials, sc, geo, ion_list, total;
 };
 
 constexpr Layout make_layout() {
@@ -68,6 +68,8 @@ constexpr Layout make_layout() {
   L.tabu = o; o += align256(sizeof(double) * (kNaTable + 2));
   L.partials = o; o += align256(sizeof(double) * 3 * kMaxRedBlocks);
   L.sc = o; o += align256(sizeof(DevScalars));
+  L.geo = o; o += align256(sizeof(Geo));
+  L.ion_list = o; o += align256(sizeof(int) * N);
   L.total = o;
   return L;
 }
@@ -94,10 +96,12 @@ std::mutex g_slots_mutex;
 double g_tab_host[kNaTable + 2];
 double g_tabu_host[kNaTable + 2];
 
-__global__ void k_na_import(int N, const double* __restrict__ X, const int* __restrict__ atype,
-                            DevState S, int* bad_type) {
+__global__ void k_na_import(int N, int Nsg, const double* __restrict__ X,
+                            const int* __restrict__ atype, DevState S, int* ion_list,
+                            int* bad_type) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
+  if (i >= Nsg) ion_list[i - Nsg] = i;
   S.pos[i] = make_double4_32a(X[i], X[(size_t)N + i], X[2 * (size_t)N + i], 0.0);
   const int t = atype[i];
   if (t < 1 || t > 3) atomicExch(bad_type, 1);
@@ -158,11 +162,12 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
   double umax = 0.0;
   int last = 0;
   DevParams P;
+  Geo G;
   {
     std::lock_guard<std::mutex> lock(g_slots_mutex);
     build_ref_table(q, g_tab_host, g_tabu_host, &umax, &last);
   }
-  const int rc = derive_dev_params(q, impact, umax, last, P, msg, sizeof msg);
+  const int rc = derive_dev_params(q, impact, umax, last, P, G, msg, sizeof msg);
   if (rc) return fail_na(rc, msg);
   if (P.ncell > kNaCells) {
     std::snprintf(msg, sizeof msg, "force_noalloc: %d cells in the reference grid, the limit is %d",
@@ -225,6 +230,10 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
   S.tabu = reinterpret_cast<const double*>(b + kLayout.tabu);
   S.partials = reinterpret_cast<double*>(b + kLayout.partials);
   S.sc = reinterpret_cast<DevScalars*>(b + kLayout.sc);
+  Geo* geo_dev = reinterpret_cast<Geo*>(b + kLayout.geo);
+  int* ion_dev = reinterpret_cast<int*>(b + kLayout.ion_list);
+  S.geo = geo_dev;
+  S.ion_list = ion_dev;
 
   int dev_sms = 152;
   cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, dev);
@@ -234,9 +243,11 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
   // the array keeps the previous call's contents: the scalars (counters,
   // reduction tickets, the bad-type flag) must start at zero
   cudaError_t e = cudaMemsetAsync(S.sc, 0, sizeof(DevScalars), s);
+  // the geometry of this call (a pageable copy: staged before the call returns)
+  if (e == cudaSuccess) e = cudaMemcpyAsync(geo_dev, &G, sizeof G, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     k_na_import<<<(q.Natm + 255) / 256, 256, 0, s>>>(
-        q.Natm, X_dev, atype_dev, S, &S.sc->nan_flag);
+        q.Natm, q.Nsg, X_dev, atype_dev, S, ion_dev, &S.sc->nan_flag);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = launch_update_posq(L, P, S);

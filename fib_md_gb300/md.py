@@ -14,7 +14,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _abi
-from ._abi import Params, Rng, Siga
+from ._abi import Params, Replica, Rng, Siga
 
 
 class FibmdError(RuntimeError):
@@ -119,6 +119,65 @@ def crystal_system(nc=(8, 8, 8), nlj: int = 1, seed: int = -1001, params: Params
     xsides = np.zeros(N, dtype=np.int32)
     xsides[:nsg] = xs
     return System(p, X, Xi, V, mass, atype, xsides, Xrand, rng)
+
+
+KB_SI = 1.381e-23
+A_LATTICE = 5.431073e-10
+
+
+@dataclass
+class SpecSlab:
+    """A spec-mode impact: a (001) Si slab with a free top surface, fixed
+    bottom layers, a thermostat layer above them, Maxwell-Boltzmann
+    velocities and one Ga ion above the surface moving towards it."""
+
+    params: Params
+    X: np.ndarray
+    Xi: np.ndarray
+    V: np.ndarray
+    mass: np.ndarray
+    atype: np.ndarray
+    tags: np.ndarray
+    surface_z: float
+
+
+def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.0,
+              ion_height: float = 10e-10, remove_above: float = 35e-10,
+              fixed_layers: int = 2, thermo_layers: int = 4, params: Params | None = None,
+              azimuth: float | None = None, impact_xy=None) -> SpecSlab:
+    """Slab of cells = (nx, ny, nz) unit cells (pureepi lattice, 8 atoms per
+    cell) plus one ion. (001) planes are a/4 apart: the lowest fixed_layers
+    are frozen (TAG_FROZEN), the next thermo_layers carry the Berendsen
+    thermostat (TAG_THERMO). The ion starts ion_height above the top plane
+    at a seeded (or given) point, with ion_eV along a direction polar_deg off
+    the inward normal at a seeded (or given) azimuth. Atoms higher than
+    remove_above over the surface are removed during the run."""
+    p = params_default() if params is None else params.copy()
+    p.mode = _abi.MODE_SPEC
+    s = crystal_system(tuple(cells), 1, -abs(int(seed)) - 1, params=p)
+    p = s.params
+    N, nsg = p.Natm, p.Nsg
+    rs = np.random.default_rng(int(seed))
+    V = np.zeros((N, 3), order="F")
+    sd = np.sqrt(KB_SI * T / s.mass[:nsg])
+    V[:nsg] = rs.normal(size=(nsg, 3)) * sd[:, None]
+    V[:nsg] -= (s.mass[:nsg, None] * V[:nsg]).sum(0) / s.mass[:nsg].sum()
+    z = s.X[:nsg, 2]
+    layer = np.rint(z / (A_LATTICE / 4)).astype(int)
+    tags = np.zeros(N, dtype=np.uint32)
+    tags[:nsg][layer < fixed_layers] = _abi.TAG_FROZEN
+    tags[:nsg][(layer >= fixed_layers) & (layer < fixed_layers + thermo_layers)] = _abi.TAG_THERMO
+    V[:nsg][layer < fixed_layers] = 0.0
+    surf = float(z.max())
+    az = rs.uniform(0.0, 2 * np.pi) if azimuth is None else float(azimuth)
+    th = np.deg2rad(polar_deg)
+    speed = np.sqrt(2 * ion_eV * p.ec / p.massGa)
+    X = s.X.copy(order="F")
+    xy = (rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1])) if impact_xy is None else impact_xy
+    X[nsg] = [xy[0], xy[1], surf + ion_height]
+    V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
+    p.remove_z = surf + remove_above
+    return SpecSlab(p, X, s.Xi.copy(order="F"), V, s.mass.copy(), s.atype.copy(), tags, surf)
 
 
 def knock(p: Params, rng: Ran1, knc: int, eV: float, phiz: float, phixy: float,
@@ -317,3 +376,57 @@ class FibMD:
         self._check(self.lib.fibmd_gpu_timers(self.h, *[C.byref(x) for x in v], c, int(reset)),
                     "timers")
         return [x.value for x in v], list(c)
+
+
+class FibMDBatch(FibMD):
+    """A batched ensemble of independent spec-mode replicas in one context
+    (fibmd_gpu_batch_create). Per-atom arrays have the padded length
+    self.N; replica r occupies rows offsets[r] : offsets[r] + natm[r]."""
+
+    def __init__(self, params: Params, replicas):
+        """replicas: sequence of (natm, nsg, Lb[3], remove_z)."""
+        self.lib = _abi.load()
+        self.params = params.copy()
+        R = len(replicas)
+        arr = (Replica * R)()
+        for r, (natm, nsg, Lb, rz) in enumerate(replicas):
+            arr[r].natm, arr[r].nsg = int(natm), int(nsg)
+            for d in range(3):
+                arr[r].Lb[d] = float(Lb[d])
+            arr[r].remove_z = float(rz)
+        h = C.c_void_p()
+        rc = self.lib.fibmd_gpu_batch_create(C.byref(self.params), R, arr, C.byref(h))
+        if rc:
+            buf = C.create_string_buffer(512)
+            self.lib.fibmd_gpu_last_error(None, buf, 512)
+            raise FibmdError(rc, buf.value.decode())
+        self.h = h
+        self.natm = np.array([int(x[0]) for x in replicas])
+        offs = np.zeros(R + 1, dtype=np.int32)
+        n = C.c_int()
+        self._check(self.lib.fibmd_gpu_batch_layout(self.h, C.byref(n), _ip(offs)), "batch_layout")
+        self.nrep = n.value
+        self.offsets = offs
+        self.N = int(offs[-1])
+
+    def pad(self, parts, fill=0.0, dtype=np.float64):
+        """Concatenate per-replica arrays into the padded layout."""
+        first = np.asarray(parts[0])
+        shape = (self.N,) + first.shape[1:]
+        out = np.full(shape, fill, dtype=dtype)
+        for r, a in enumerate(parts):
+            a = np.asarray(a)
+            out[self.offsets[r]:self.offsets[r] + len(a)] = a
+        return np.asfortranarray(out) if out.ndim > 1 else out
+
+    def rows(self, r: int) -> slice:
+        return slice(int(self.offsets[r]), int(self.offsets[r] + self.natm[r]))
+
+    def scalars(self):
+        """Per-replica (time, dt, removed count)."""
+        t = np.zeros(self.nrep)
+        dt = np.zeros(self.nrep)
+        rm = np.zeros(self.nrep, dtype=np.int32)
+        self._check(self.lib.fibmd_gpu_batch_scalars(self.h, _dp(t), _dp(dt), _ip(rm)),
+                    "batch_scalars")
+        return t, dt, rm

@@ -317,6 +317,37 @@ int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_dev,
                             const int* atype_dev, int impact, double* F_dev,
                             void* stream);
 
+/* ---- batched ensemble (spec mode) -----------------------------------------
+   Independent impacts advanced together: each replica has its own box,
+   atoms, cell grid, variable dt, thermostat factor and removal count; the
+   kernels of one step handle every replica's atoms at once. There is no
+   counterpart in the reference, which runs one impact per process. */
+typedef struct fibmd_replica {
+  int natm;          /* atoms of the replica: lattice atoms first, then ions */
+  int nsg;           /* lattice atoms (atype 1 or 2)                         */
+  double Lb[3];      /* its periodic box (m); z is open when remove_z > 0    */
+  double remove_z;   /* removal height (m), <= 0: none                       */
+  int reserved[4];
+} fibmd_replica;
+
+/* Create a batch context from shared physics p (mode must be
+   FIBMD_MODE_SPEC; p's Natm, Nsg, Nlj, Lb and remove_z are ignored) and
+   nrep replicas. The replicas' atoms are concatenated, each starting at a
+   multiple of 256; the slots between replicas are padding. Every per-atom
+   array of upload/download/set_tags then has the padded length
+   offsets[nrep] (fibmd_gpu_batch_layout); padding slots take any position,
+   mass > 0 and atype 1, and are kept as removed atoms. Lists, forces and
+   steps run as for a single system; fibmd_gpu_steps' time argument is the
+   start time of every replica and returns replica 0's. */
+int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica* reps,
+                           fibmd_ctx** out);
+/* Replica count and, if offsets is not NULL, the first atom of each replica
+   in offsets[0..nrep-1] and the padded atom count in offsets[nrep]. */
+int fibmd_gpu_batch_layout(fibmd_ctx* ctx, int* nrep, int* offsets);
+/* Per-replica simulated time (s), current step (s) and count of removed
+   (sputtered) atoms; any pointer may be NULL, else nrep entries. */
+int fibmd_gpu_batch_scalars(fibmd_ctx* ctx, double* time, double* dt, int* removed);
+
 #ifdef __cplusplus
 }
 #endif

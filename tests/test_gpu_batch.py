@@ -1,0 +1,91 @@
+"""Batched ensemble: replicas of different boxes advanced in one context
+must move exactly as the same replicas run one by one (same algorithm; only
+the order of the force sums differs)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+REPLICAS = [((4, 4, 3), 31, 800.0, 10.0), ((5, 4, 3), 32, 400.0, 25.0), ((3, 5, 3), 33, 1500.0, 0.0)]
+
+
+def _slabs(precision):
+    import fib_md_gb300 as fm
+
+    p = fm.params_default()
+    p.precision = precision
+    return [fm.spec_slab(c, seed, eV, th, params=p, ion_height=4e-10)
+            for c, seed, eV, th in REPLICAS]
+
+
+def _single(sl, steps):
+    import fib_md_gb300 as fm
+
+    g = fm.FibMD(sl.params)
+    g.upload(sl.X, sl.V, None, sl.Xi, sl.mass, sl.atype, np.zeros(sl.params.Natm, np.int32))
+    g.set_tags(sl.tags)
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+    lt, t, _, _ = g.steps(2, steps, 0, 0.0, 300.0)
+    X, V, _ = g.download()
+    g.close()
+    return X, V, t
+
+
+def _batch(slabs, steps):
+    import fib_md_gb300 as fm
+
+    reps = [(s.params.Natm, s.params.Nsg, list(s.params.Lb), s.params.remove_z) for s in slabs]
+    b = fm.FibMDBatch(slabs[0].params, reps)
+    X = b.pad([s.X for s in slabs])
+    V = b.pad([s.V for s in slabs])
+    Xi = b.pad([s.Xi for s in slabs])
+    mass = b.pad([s.mass for s in slabs], fill=1.0)
+    atype = b.pad([s.atype for s in slabs], fill=1, dtype=np.int32)
+    tags = b.pad([s.tags for s in slabs], fill=0, dtype=np.uint32)
+    b.upload(X, V, None, Xi, mass, atype, np.zeros(b.N, np.int32))
+    b.set_tags(tags)
+    b.si_nlist()
+    b.si_force()
+    b.steps(2, steps, 0, 0.0, 300.0)
+    Xb, Vb, _ = b.download()
+    t, _, _ = b.scalars()
+    return b, Xb, Vb, t, X
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_matches_single_replicas(gpu_lib, precision):
+    slabs = _slabs(precision)
+    steps = 120
+    b, Xb, Vb, tb, X0 = _batch(slabs, steps)
+    for r, sl in enumerate(slabs):
+        X, V, t = _single(sl, steps)
+        rows = b.rows(r)
+        assert abs(tb[r] - t) <= 1e-12 * t, (r, tb[r], t)
+        Lb = np.array(sl.params.Lb[:])
+        d = Xb[rows] - X
+        d[:, :2] -= Lb[:2] * np.rint(d[:, :2] / Lb[:2])
+        assert np.abs(d).max() < 1e-18, (r, np.abs(d).max())
+        assert np.abs(Vb[rows] - V).max() <= 1e-9 * np.abs(V).max()
+    # replicas advance with their own variable step
+    assert len(set(np.round(tb / tb.max(), 12))) > 1
+    # padding slots never move
+    pad = np.ones(b.N, dtype=bool)
+    for r in range(b.nrep):
+        pad[b.rows(r)] = False
+    assert pad.any() and np.array_equal(Xb[pad], X0[pad])
+    b.close()
+
+
+def test_batch_layout(gpu_lib):
+    slabs = _slabs(0)
+    import fib_md_gb300 as fm
+
+    reps = [(s.params.Natm, s.params.Nsg, list(s.params.Lb), s.params.remove_z) for s in slabs]
+    b = fm.FibMDBatch(slabs[0].params, reps)
+    assert b.nrep == 3 and np.all(b.offsets[:-1] % 256 == 0)
+    assert np.all(np.diff(b.offsets)[:3] >= b.natm)
+    b.close()
