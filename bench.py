@@ -57,6 +57,11 @@ def parse():
                     help="spec-mode list skin in Angstrom (0: the reference's list radii)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the step loop launch by launch (for a profiler's launch list)")
+    ap.add_argument("--ensemble-replicas", type=int, default=256)
+    ap.add_argument("--ensemble-steps", type=int, default=3000)
+    ap.add_argument("--ensemble-plain-sample", type=int, default=3,
+                    help="impacts run one by one in plain binary64 to time that form")
+    ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64", "build"], default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64) "
                          "or rebuild the lists 5 times (build), exit (for ncu)")
@@ -372,8 +377,8 @@ def bench_ours(args, rank, world, dist):
                           "moliere_pairs": counts[2], "stale_terms": counts[3]},
         # per MD step: drift, rebuild condition, force (begin, main, Moliere,
         # many-leg), kick + finalize = 8; per step pair the loop control;
-        # 8 kernels per list rebuild; one temperature kernel per bench step
-        "gpu_launches": int(8.5 * args.md_steps * args.steps + 8 * rebuilds + args.steps),
+        # 9 kernels per list rebuild; one temperature kernel per bench step
+        "gpu_launches": int(8.5 * args.md_steps * args.steps + 9 * rebuilds + args.steps),
         "rebuild_fraction": rebuilds / float(args.md_steps * args.steps),
         "wall_s_timed": wall,
         "clocks": clk.summary(),
@@ -381,6 +386,144 @@ def bench_ours(args, rank, world, dist):
     if e2e:
         out["e2e"] = e2e
     return out
+
+
+# ---------------------------------------------------------------------------
+# batched ensemble: independent impacts on uneven slabs
+def make_ensemble(nrep, precision, seed0=3000):
+    """Slabs of U{6..12} x U{6..12} x 10 unit cells, one Ga each at
+    U(0.5, 5) keV and U(0, 30) degrees off normal, seeded azimuth and impact
+    point (seed 3000 + r); atoms more than 15 A above the surface leave."""
+    import fib_md_gb300 as fm
+
+    p = fm.params_default()
+    p.precision = precision
+    rs = np.random.default_rng(seed0)
+    slabs = []
+    for r in range(nrep):
+        lx, ly = (int(v) for v in rs.integers(6, 13, size=2))
+        eV = float(rs.uniform(500.0, 5000.0))
+        th = float(rs.uniform(0.0, 30.0))
+        slabs.append(fm.spec_slab((lx, ly, 10), seed=seed0 + r, ion_eV=eV, polar_deg=th,
+                                  remove_above=15e-10, params=p))
+    return slabs
+
+
+def run_ensemble_batch(slabs, precision, steps):
+    """Every impact in one batch context: wall time from upload to the
+    downloaded final state, and each impact's outcome."""
+    import torch
+    import fib_md_gb300 as fm
+
+    p = slabs[0].params.copy()
+    p.precision = precision
+    reps = [(s.params.Natm, s.params.Nsg, list(s.params.Lb), s.params.remove_z) for s in slabs]
+    b = fm.FibMDBatch(p, reps)
+    X = b.pad([s.X for s in slabs])
+    V = b.pad([s.V for s in slabs])
+    Xi = b.pad([s.Xi for s in slabs])
+    mass = b.pad([s.mass for s in slabs], fill=1.0)
+    atype = b.pad([s.atype for s in slabs], fill=1, dtype=np.int32)
+    tags = b.pad([s.tags for s in slabs], fill=0, dtype=np.uint32)
+    xs = np.zeros(b.N, np.int32)
+    torch.cuda.synchronize()
+    rb0 = 0
+    w0 = time.perf_counter()
+    b.upload(X, V, None, Xi, mass, atype, xs)
+    b.set_tags(tags)
+    b.si_nlist()
+    b.si_force()
+    rb0 = b.work_counters()[4]
+    b.steps(2, steps, 0, 0.0, 300.0)
+    Xf, _, _ = b.download()
+    t_sim, _, removed = b.scalars()
+    wall = time.perf_counter() - w0
+    rebuilds = b.work_counters()[4] - rb0
+    stats = []
+    for r, s in enumerate(slabs):
+        rows = b.rows(r)
+        stats.append(fm.impact_statistics(Xf[rows], s.Xi, s.atype, list(s.params.Lb),
+                                          s.surface_z, s.params.remove_z))
+    atoms = int(b.natm.sum())
+    b.close()
+    return {"wall_s": wall, "atoms": atoms, "padded_atoms": int(b.N), "rebuilds": int(rebuilds),
+            "removed": removed.tolist(), "sim_time_s": t_sim.tolist(), "stats": stats}
+
+
+def run_plain(slab, steps):
+    """One impact alone in a plain binary64 context (no batching)."""
+    import torch
+    import fib_md_gb300 as fm
+
+    p = slab.params.copy()
+    p.precision = fm.PREC_FP64
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    g = fm.FibMD(p)
+    g.upload(slab.X, slab.V, None, slab.Xi, slab.mass, slab.atype, np.zeros(p.Natm, np.int32))
+    g.set_tags(slab.tags)
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+    g.steps(2, steps, 0, 0.0, 300.0)
+    g.download()
+    wall = time.perf_counter() - w0
+    g.close()
+    return wall
+
+
+def two_sample(a, b):
+    """Mann-Whitney U and Kolmogorov-Smirnov p-values of two samples."""
+    from scipy import stats
+
+    a = np.asarray([x for x in a if np.isfinite(x)], dtype=float)
+    b = np.asarray([x for x in b if np.isfinite(x)], dtype=float)
+    if len(a) < 2 or len(b) < 2:
+        return {"n": [len(a), len(b)], "p_mannwhitney": None, "p_ks": None}
+    if np.all(a == a[0]) and np.all(b == a[0]):
+        pm = pk = 1.0
+    else:
+        pm = float(stats.mannwhitneyu(a, b, alternative="two-sided").pvalue)
+        pk = float(stats.ks_2samp(a, b).pvalue)
+    return {"n": [len(a), len(b)], "mean": [float(a.mean()), float(b.mean())],
+            "p_mannwhitney": pm, "p_ks": pk}
+
+
+def bench_ensemble(args):
+    import fib_md_gb300 as fm
+
+    nrep, steps = args.ensemble_replicas, args.ensemble_steps
+    slabs = make_ensemble(nrep, fm.PREC_MIXED)
+    # a short warm-up batch (context set-up, graph capture, first-touch)
+    run_ensemble_batch(slabs[:4], fm.PREC_MIXED, 20)
+    mixed = run_ensemble_batch(slabs, fm.PREC_MIXED, steps)
+    fp64 = run_ensemble_batch(slabs, fm.PREC_FP64, steps)
+    k = max(1, min(args.ensemble_plain_sample, nrep))
+    run_plain(slabs[0], 20)
+    plain = [run_plain(slabs[r], steps) for r in range(k)]
+    plain_s = float(np.mean(plain))
+    ih = lambda res: 3600.0 * nrep / res["wall_s"]
+    cmp = {}
+    for q, name in enumerate(["sputter_yield", "implant_depth_m", "displaced_atoms"]):
+        cmp[name] = two_sample([s[q] for s in mixed["stats"]], [s[q] for s in fp64["stats"]])
+    ok = all(v["p_mannwhitney"] is None or v["p_mannwhitney"] > 0.05 for v in cmp.values())
+    return {
+        "config": f"{nrep} impacts, U{{6..12}}^2 x 10 unit-cell slabs, U(0.5,5) keV Ga, "
+                  f"U(0,30) deg, {steps} variable-dt steps each, one batch context",
+        "impacts_per_hour": {"mixed_batched": ih(mixed), "fp64_batched": ih(fp64),
+                             "fp64_plain": 3600.0 / plain_s},
+        "mixed_batched_over_fp64_plain": ih(mixed) * plain_s / 3600.0,
+        "mixed_batched_over_fp64_batched": fp64["wall_s"] / mixed["wall_s"],
+        "atom_steps_per_s": {"mixed_batched": mixed["atoms"] * steps / mixed["wall_s"],
+                             "fp64_batched": fp64["atoms"] * steps / fp64["wall_s"]},
+        "wall_s": {"mixed_batched": mixed["wall_s"], "fp64_batched": fp64["wall_s"],
+                   "fp64_plain_per_impact": plain_s, "fp64_plain_sample": k},
+        "atoms": mixed["atoms"], "padded_atoms": mixed["padded_atoms"],
+        "rebuild_fraction": {"mixed": mixed["rebuilds"] / steps, "fp64": fp64["rebuilds"] / steps},
+        "mixed_vs_fp64_two_sample": cmp,
+        "statistically_consistent_95": ok,
+        "timing": "wall clock from upload of the initial states to the downloaded final states",
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -461,6 +604,8 @@ def main():
 
         dist.init_process_group("nccl")
     out = bench_ours(args, rank, world, dist)
+    if not args.no_ensemble:
+        out["ensemble"] = bench_ensemble(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(cells, args.cpu_sample_steps)

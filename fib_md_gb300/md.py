@@ -180,6 +180,33 @@ def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.
     return SpecSlab(p, X, s.Xi.copy(order="F"), V, s.mass.copy(), s.atype.copy(), tags, surf)
 
 
+def impact_statistics(X, Xi, atype, Lb, surface_z: float, remove_z: float,
+                      displaced_threshold: float = 1.0e-10):
+    """Outcome of one impact from its final positions: (sputtered atoms,
+    ion depth below the surface in m (nan if the ion is above it), displaced
+    lattice atoms). Sputtered atoms are the lattice atoms above remove_z
+    (removed atoms stay where they were taken out); an atom is displaced
+    when it is farther than displaced_threshold from its initial site
+    (minimum image in x and y)."""
+    X = np.asarray(X)
+    Xi = np.asarray(Xi)
+    atype = np.asarray(atype)
+    lattice = atype < 3
+    up = X[:, 2] > remove_z
+    sputtered = int(np.count_nonzero(lattice & up))
+    ion = np.nonzero(atype == 3)[0]
+    depth = float("nan")
+    if ion.size:
+        z = float(X[ion[0], 2])
+        depth = surface_z - z if z <= surface_z else float("nan")
+    d = X - Xi
+    L = np.asarray(Lb, dtype=np.float64)[:2]
+    d[:, :2] -= L * np.rint(d[:, :2] / L)
+    r2 = np.einsum("ij,ij->i", d, d)
+    displaced = int(np.count_nonzero(lattice & ~up & (r2 > displaced_threshold ** 2)))
+    return sputtered, depth, displaced
+
+
 def knock(p: Params, rng: Ran1, knc: int, eV: float, phiz: float, phixy: float,
           Xrand: np.ndarray):
     """knock (src/knock.f90:21-55): (1-based ion index, x[3], v[3])."""
