@@ -231,6 +231,7 @@ def bench_ours(args, rank, world, dist):
         barrier()
         wall = time.perf_counter() - w0
     rebuilds = g.work_counters()[4] - rb0
+    X_end, _, _ = g.download()
     t_dev = sum(times)
     if dist is not None:
         tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
@@ -295,6 +296,7 @@ def bench_ours(args, rank, world, dist):
     g64 = make_ctx(w, fm.PREC_FP64)
     g64.set_option("timers", 0)
     s64 = torch.cuda.ExternalStream(g64.stream_ptr)
+
     n64 = args.fp64_steps if args.fp64_steps > 0 else max(2, args.steps // 2)
     run_device(g64, torch, s64, max(1, args.warmup - 1), args.md_steps, flush)
     barrier()
@@ -373,6 +375,14 @@ def bench_ours(args, rank, world, dist):
                          "frac": step_bytes / md_step_s / 1e9 / hbm_peak,
                          "bytes_per_atom_step": 150,
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "mixed_error_vs_fp64": {
+            **force_error(w, X_end),
+            "nve_drift_eV_per_atom_per_ps": {"mixed": nve_drift(w, fm.PREC_MIXED),
+                                             "fp64": nve_drift(w, fm.PREC_FP64)},
+            "nve_segment": "1 ps (1000 steps at the 1 fs cap) of the same slab at 300 K, "
+                           "ion held outside, thermostat off, fixed layers kept; drift = "
+                           "slope of a line fitted to 11 samples of the total energy",
+        },
         "work_counters": {"sw_pairs": counts[0], "angle_terms": counts[1],
                           "moliere_pairs": counts[2], "stale_terms": counts[3]},
         # per MD step: drift, rebuild condition, force (begin, main, Moliere,
@@ -386,6 +396,71 @@ def bench_ours(args, rank, world, dist):
     if e2e:
         out["e2e"] = e2e
     return out
+
+
+# ---------------------------------------------------------------------------
+def force_error(w, X):
+    """Mixed against binary64 forces on one configuration (the slab after the
+    timed cascade: thermal disorder plus the damaged region)."""
+    import fib_md_gb300 as fm
+
+    F = {}
+    for prec in (fm.PREC_MIXED, fm.PREC_FP64):
+        p = w["params"].copy()
+        p.precision = prec
+        g = fm.FibMD(p)
+        g.upload(X, w["V"], None, w["Xi"], w["mass"], w["atype"], w["xsides"])
+        g.set_tags(w["tags"])
+        g.set_impact(1)
+        g.si_nlist()
+        F[prec] = g.si_force()
+        g.close()
+    dF = F[fm.PREC_MIXED] - F[fm.PREC_FP64]
+    rms_d = float(np.sqrt(np.mean(np.sum(dF * dF, axis=1))))
+    rms_f = float(np.sqrt(np.mean(np.sum(F[fm.PREC_FP64] ** 2, axis=1))))
+    ev_a = w["params"].ec * 1e10
+    return {"force_rms_rel": rms_d / rms_f, "force_rms_abs_eV_per_A": rms_d / ev_a,
+            "force_max_abs_eV_per_A": float(np.abs(dF).max()) / ev_a,
+            "force_config": "the slab after the timed mixed run (300 K plus the cascade)"}
+
+
+def nve_drift(w, precision, steps=1000):
+    """Total-energy drift (eV per mobile atom per ps) of an unthermostatted
+    segment of the workload's slab with the ion parked far above it."""
+    import fib_md_gb300 as fm
+
+    p = w["params"].copy()
+    p.precision = precision
+    N, nsg = p.Natm, p.Nsg
+    X = w["X"].copy(order="F")
+    V = w["V"].copy(order="F")
+    X[nsg:, 2] = p.remove_z - 1e-10
+    V[nsg:] = 0.0
+    tags = (w["tags"] & fm.TAG_FROZEN).astype(np.uint32)
+    g = fm.FibMD(p)
+    g.upload(X, V, None, w["Xi"], w["mass"], w["atype"], w["xsides"])
+    g.set_tags(tags)
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+
+    def energy():
+        _, Vd, _ = g.download()
+        _, _, U = g.si_force_energy()
+        return U + 0.5 * float(np.sum(w["mass"][:, None] * Vd * Vd))
+
+    # the slope of a least-squares line through E(t), sampled every tenth of
+    # the segment: velocity Verlet's bounded energy fluctuation is not drift
+    ts, Es = [0.0], [energy()]
+    lt, t = 0, 0.0
+    for k in range(10):
+        lt, t, _, _ = g.steps(2, steps // 10, lt, t, 300.0)
+        ts.append(t)
+        Es.append(energy())
+    g.close()
+    mobile = int(np.count_nonzero(tags[:nsg] == 0))
+    slope = np.polyfit(np.array(ts) * 1e12, np.array(Es), 1)[0]
+    return float(slope / p.ec / mobile)
 
 
 # ---------------------------------------------------------------------------
