@@ -352,6 +352,11 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   const double usup = std::max(P.cut3, u_next);
   const double rsupA = usup * sigmax * 1e10 * (1 + 1e-4);
   P.pre3A2 = (float)(rsupA * rsupA);
+  // binary32: a pair at u > a - gamma/110 has exp(gamma/(u-a)) < e^-110 (zero
+  // in binary32) and exp(1/(u-a)) < e^-91 (a 2-body force below 1e-35 eV/A)
+  const double um = std::min(P.cut3, p.al - p.gamma / 110.0);
+  const double rmA = um * sigmax * 1e10 * (1 + 1e-4);
+  P.pre3mA2 = (float)(rmA * rmA);
   // fast atoms: displaced by at least half the smaller list skin
   const double skin = std::min(rc - P.cut3 * sigmax, rclj - rlj);
   const double half = 0.5 * skin * 0.99;

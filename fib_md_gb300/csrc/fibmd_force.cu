@@ -250,6 +250,39 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
   int nl = 0;
   unsigned int cnt_pairs = 0, cnt_ang = 0;
 
+  // One listed pair inside the SW cutoff: its 2-body force on the centre and
+  // its leg parameters. Returns false outside the cutoff.
+  auto pair_leg = [&](const float3& dq, float r2f, int tb, float* rinv_o, float* E_o,
+                      float* g_o) -> bool {
+    const float rinv = rsqrtf(r2f);
+    const float r = r2f * rinv;
+    const float sg = P.sigA[ta][tb];
+    const float ue = r / sg;
+    if (!(ue < cut)) return false;
+    const float inv = 1.0f / (ue - al);
+    const float ex = expf(inv);
+    const float u2 = 1.0f / (ue * ue);
+    const float u4 = u2 * u2;
+    // psi = 4, qsi = 0: dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
+    const float dphi = Ac * ex * (-4.0f * Bc * u4 / ue - (Bc * u4 - 1.0f) * inv * inv);
+    const float c = -(dphi * rinv * (P.epsA[ta][tb] / sg));
+    fx += c * dq.x;
+    fy += c * dq.y;
+    fz += c * dq.z;
+    if (COUNT) cnt_pairs++;
+    if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
+    *rinv_o = rinv;
+    *E_o = expf(gm * inv);
+    *g_o = -gm * inv * inv / sg;
+    return true;
+  };
+
+  // Phase 1: gather the listed neighbours and stage the few inside the
+  // prefilter sphere (about 4 of 16 in a crystal) in the leg slots, so the
+  // costly pair/leg arithmetic of phase 2 runs on compacted candidates
+  // with the lanes of a warp busy together. A centre with more candidates
+  // than slots evaluates the rest in place and goes to the many-leg kernel.
+  int nc = 0, extra = 0;
   for (int k0 = 0; k0 < n; k0 += kBatch) {
     int jj[kBatch];
     int4 qq[kBatch];
@@ -262,41 +295,43 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
       if (k0 + u >= n) break;
       const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-      if (r2f > P.pre3A2) continue;
+      if (r2f > P.pre3mA2) continue;
       const int tb = (qq[u].w & 0xff) - 1;
-      const float rinv = rsqrtf(r2f);
-      const float r = r2f * rinv;
-      const float sg = P.sigA[ta][tb];
-      const float ue = r / sg;
-      if (!(ue < cut)) continue;
-      const float inv = 1.0f / (ue - al);
-      const float ex = expf(inv);
-      const float u2 = 1.0f / (ue * ue);
-      const float u4 = u2 * u2;
-      // psi = 4, qsi = 0: dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
-      const float dphi = Ac * ex * (-4.0f * Bc * u4 / ue - (Bc * u4 - 1.0f) * inv * inv);
-      const float c = -(dphi * rinv * (P.epsA[ta][tb] / sg));
-      fx += c * dq.x;
-      fy += c * dq.y;
-      fz += c * dq.z;
-      if (COUNT) cnt_pairs++;
-      if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
-      const float E = expf(gm * inv);
-      // a leg whose exponential underflows in binary32 adds exactly zero
-      if (E > 0.f) {
-        if (nl < kMaxLegs) {
-          leg.at(nl, 0) = dq.x * rinv;
-          leg.at(nl, 1) = dq.y * rinv;
-          leg.at(nl, 2) = dq.z * rinv;
-          leg.at(nl, 3) = rinv;
-          leg.at(nl, 4) = E;
-          leg.at(nl, 5) = -gm * inv * inv / sg;
-          leg.idx(nl) = jj[u] | (tb << 30);
-        }
-        nl++;
+      if (nc < kMaxLegs) {
+        leg.at(nc, 0) = dq.x;
+        leg.at(nc, 1) = dq.y;
+        leg.at(nc, 2) = dq.z;
+        leg.at(nc, 3) = r2f;
+        leg.idx(nc) = jj[u] | (tb << 30);
+        nc++;
+      } else {
+        float rinv, E, g;
+        if (pair_leg(dq, r2f, tb, &rinv, &E, &g) && E > 0.f) extra++;
       }
     }
   }
+  // Phase 2: pair forces and legs of the staged candidates; active legs are
+  // compacted in place (slot nl <= c is written after slot c is read).
+  for (int c = 0; c < nc; c++) {
+    const float3 dq = make_float3(leg.at(c, 0), leg.at(c, 1), leg.at(c, 2));
+    const float r2f = leg.at(c, 3);
+    const int idx = leg.idx(c);
+    float rinv, E, g;
+    if (!pair_leg(dq, r2f, (unsigned)idx >> 30, &rinv, &E, &g)) continue;
+    // a leg whose exponential underflows in binary32 adds exactly zero
+    if (E > 0.f) {
+      leg.at(nl, 0) = dq.x * rinv;
+      leg.at(nl, 1) = dq.y * rinv;
+      leg.at(nl, 2) = dq.z * rinv;
+      leg.at(nl, 3) = rinv;
+      leg.at(nl, 4) = E;
+      leg.at(nl, 5) = g;
+      leg.idx(nl) = idx;
+      nl++;
+    }
+  }
+  // legs beyond the slots were not staged: the many-leg kernel takes the centre
+  if (extra) nl = kMaxLegs + 1 + extra;
 
   const double conv = P.f_evA_to_N;
   double ue_J = 0.0;

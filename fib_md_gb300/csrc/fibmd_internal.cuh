@@ -84,6 +84,8 @@ struct DevParams {
   float pre_sw2A, pre_mol2A;   // binary32 prefilter radii^2 (A^2), widened
   float acc_sw2A, acc_mol2A;   // binary32 accept radii^2 (A^2), narrowed
   float pre3A2;                // prefilter for active SW legs (A^2)
+  float pre3mA2;               // binary32 path: u < a - gamma/110, beyond which
+                               // every SW exponential underflows (A^2)
   // Stillinger-Weber (types 1, 2 -> index 0, 1)
   double al, gam, cut3, thrd, A, B, psi, qsi;
   double eps[2][2], isig[2][2], leps[2][2][2], epssig[2][2];
