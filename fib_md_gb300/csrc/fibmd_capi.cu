@@ -357,6 +357,9 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   const double um = std::min(P.cut3, p.al - p.gamma / 110.0);
   const double rmA = um * sigmax * 1e10 * (1 + 1e-4);
   P.pre3mA2 = (float)(rmA * rmA);
+  const double ul = std::min(um, p.al + p.gamma / std::log((double)kLegEmin));
+  const double rlA = ul * sigmax * 1e10 * (1 + 1e-4);
+  P.pre3lA2 = (float)(rlA * rlA);
   // fast atoms: displaced by at least half the smaller list skin
   const double skin = std::min(rc - P.cut3 * sigmax, rclj - rlj);
   const double half = 0.5 * skin * 0.99;

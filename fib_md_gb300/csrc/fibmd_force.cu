@@ -57,6 +57,9 @@ constexpr int kLegF64 = 9;   // ux uy uz rinv E g fx fy fz
 constexpr int kBlock64 = 64;
 constexpr int kLegF32 = 6;   // ux uy uz rinv E g
 constexpr int kBlock32 = 128;
+constexpr int kLegs32 = 8;   // staged candidates per centre (binary32 kernel);
+                             // a crystal at 300 K has 4 legs, rarely more than 6
+
 constexpr int kBatch = 8;    // neighbour gathers in flight per thread
 
 template <typename R, int BLOCK, int F>
@@ -227,11 +230,11 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
 // in registers over its row and scattered once, so the shared-memory stage
 // holds only 6 floats per leg (more resident warps for the gathers).
 template <bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState S) {
+__global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   LegSmem<float, kBlock32, kLegF32> leg;
   leg.v = reinterpret_cast<float*>(smem_raw);
-  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(float) * kMaxLegs * kLegF32 * kBlock32);
+  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(float) * kLegs32 * kLegF32 * kBlock32);
 
   const int i = blockIdx.x * kBlock32 + threadIdx.x;
   if (i >= P.N) return;
@@ -277,11 +280,12 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
     return true;
   };
 
-  // Phase 1: gather the listed neighbours and stage the few inside the
-  // prefilter sphere (about 4 of 16 in a crystal) in the leg slots, so the
-  // costly pair/leg arithmetic of phase 2 runs on compacted candidates
-  // with the lanes of a warp busy together. A centre with more candidates
-  // than slots evaluates the rest in place and goes to the many-leg kernel.
+  // Phase 1: gather the listed neighbours and stage the few that can be legs
+  // (about 4 of 16 in a crystal) in the leg slots, so the costly pair/leg
+  // arithmetic of phase 2 runs on compacted candidates with the lanes of a
+  // warp busy together. Pairs between the leg radius and the cutoff (2-body
+  // only) are evaluated in place; a centre with more legs than slots
+  // evaluates the rest in place and goes to the many-leg kernel.
   int nc = 0, extra = 0;
   for (int k0 = 0; k0 < n; k0 += kBatch) {
     int jj[kBatch];
@@ -297,7 +301,7 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
       if (r2f > P.pre3mA2) continue;
       const int tb = (qq[u].w & 0xff) - 1;
-      if (nc < kMaxLegs) {
+      if (r2f <= P.pre3lA2 && nc < kLegs32) {
         leg.at(nc, 0) = dq.x;
         leg.at(nc, 1) = dq.y;
         leg.at(nc, 2) = dq.z;
@@ -306,7 +310,7 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
         nc++;
       } else {
         float rinv, E, g;
-        if (pair_leg(dq, r2f, tb, &rinv, &E, &g) && E > 0.f) extra++;
+        if (pair_leg(dq, r2f, tb, &rinv, &E, &g) && E > kLegEmin) extra++;
       }
     }
   }
@@ -318,8 +322,7 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
     const int idx = leg.idx(c);
     float rinv, E, g;
     if (!pair_leg(dq, r2f, (unsigned)idx >> 30, &rinv, &E, &g)) continue;
-    // a leg whose exponential underflows in binary32 adds exactly zero
-    if (E > 0.f) {
+    if (E > kLegEmin) {
       leg.at(nl, 0) = dq.x * rinv;
       leg.at(nl, 1) = dq.y * rinv;
       leg.at(nl, 2) = dq.z * rinv;
@@ -331,9 +334,11 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
     }
   }
   // legs beyond the slots were not staged: the many-leg kernel takes the centre
-  if (extra) nl = kMaxLegs + 1 + extra;
+  if (extra) nl = kMaxLegs + 1;
 
-  const double conv = P.f_evA_to_N;
+  // eV/A -> N in binary32 (a normal number: 1.6e-9 times the force), so each
+  // binary64 atomic costs one conversion
+  const float convf = (float)P.f_evA_to_N;
   double ue_J = 0.0;
   if (nl > kMaxLegs) {
     const int slot = atomicAdd(&S.sc->heavy_count, 1);
@@ -363,8 +368,8 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
         if (ENERGY) ae += pref * W;
         if (COUNT && b > a && pref != 0.f) cnt_ang++;
       }
-      atomic_add3(S.frc_new, ia & 0x3fffffff, conv * (double)afx, conv * (double)afy,
-                  conv * (double)afz);
+      atomic_add3(S.frc_new, ia & 0x3fffffff, (double)(convf * afx), (double)(convf * afy),
+                  (double)(convf * afz));
       fx -= afx;
       fy -= afy;
       fz -= afz;
@@ -376,7 +381,7 @@ __global__ void __launch_bounds__(kBlock32) k_force_mixed(DevParams P, DevState 
     }
     if (ENERGY) ue_J = P.e_eV_to_J * (double)cu / 6.0;
   }
-  atomic_add3(S.frc_new, i, conv * (double)fx, conv * (double)fy, conv * (double)fz);
+  atomic_add3(S.frc_new, i, (double)(convf * fx), (double)(convf * fy), (double)(convf * fz));
   if (ENERGY) {
     const double e = P.e_eV_to_J * (double)ui + ue_J;
     if (e != 0.0) atomicAdd(&S.epot[i], e);
@@ -480,7 +485,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
         if (!(u < (float)P.cut3)) continue;
         const float ia = 1.0f / (u - (float)P.al);
         const float E = expf((float)P.gam * ia);
-        if (!(E > 0.f)) continue;
+        if (!(E > kLegEmin)) continue;
         const int q = atomicAdd(&snl[w], 1);
         sl[w][0][q] = dq.x * rinv;
         sl[w][1][q] = dq.y * rinv;
@@ -692,7 +697,7 @@ __global__ void k_force_begin(DevState S) {
 template <bool MIXED, bool ENERGY, bool COUNT>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
   constexpr int BLOCK = MIXED ? kBlock32 : kBlock64;
-  const size_t smem = MIXED ? (sizeof(float) * kMaxLegs * kLegF32 + sizeof(int) * kMaxLegs) * BLOCK
+  const size_t smem = MIXED ? (sizeof(float) * kLegs32 * kLegF32 + sizeof(int) * kLegs32) * BLOCK
                             : (sizeof(double) * kMaxLegs * kLegF64 + sizeof(int) * kMaxLegs) * BLOCK;
   auto kern = MIXED ? k_force_mixed<ENERGY, COUNT> : k_force_fp64<ENERGY, COUNT>;
   static bool attr_set = false;

@@ -29,6 +29,12 @@ constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
 constexpr int kMaxRedBlocks = 16384;  // row stride of the reduction partials
 constexpr int kKickThreads = 256;  // spec kick block; replicas start at multiples
+// Binary32 SW legs with exp(gamma/(u-a)) below this are dropped: an angle
+// term is at most lambda*eps*E_a*E_b (~45 eV E_a E_b), so such a leg moves a
+// force by less than 1e-8 eV/A, far below the binary32 arithmetic's own
+// error, and second neighbours squeezed inside the cutoff by thermal motion
+// stop counting as legs.
+constexpr float kLegEmin = 1e-12f;
 
 enum : uint32_t {
   FL_FROZEN = 1u,   // xsides > 0 (ref) / FIBMD_TAG_FROZEN (spec)
@@ -86,6 +92,7 @@ struct DevParams {
   float pre3A2;                // prefilter for active SW legs (A^2)
   float pre3mA2;               // binary32 path: u < a - gamma/110, beyond which
                                // every SW exponential underflows (A^2)
+  float pre3lA2;               // binary32 legs: exp(gamma/(u-a)) > kLegEmin (A^2)
   // Stillinger-Weber (types 1, 2 -> index 0, 1)
   double al, gam, cut3, thrd, A, B, psi, qsi;
   double eps[2][2], isig[2][2], leps[2][2][2], epssig[2][2];
