@@ -70,9 +70,9 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
   const int4 q = S.posq[i];
+  S.n_sw[i] = 0;  // the list build appends with atomics
   if ((q.w >> 8) & FL_REMOVED) {
     S.atom_cell[i] = -1;
-    S.n_sw[i] = 0;
     S.posq_build[i] = q;
     S.fast_flag[i] = 0;
     return;
@@ -218,23 +218,34 @@ __device__ __forceinline__ bool exact_in(const Geo& G, const DevState& S, int i,
   return r2 < rv2;
 }
 
-// One thread per binned atom, in cell order. The lanes of a warp hold the
-// atoms of a few x-adjacent cells, so they walk nearly the same nine
-// stencil rows, and their candidate loads hit the same cached lines. A row
-// of three x-adjacent cells is one run of the cell-sorted arrays (two runs
-// where it wraps in x). Candidates are tested in binary32 on the
-// fixed-point separations; within 1e-4 of a radius the reference's
-// binary64 test decides. Accepted SW neighbours are kept (as cell-order
-// slots) in shared memory and written to the list after the scan, one list
-// slot of all lanes at a time. A pair with an ion goes to the Moliere pair
-// list; with WIDE (spec mode) the ion scan below lists those instead and
-// ions are skipped here.
+// One thread per binned atom, in cell order, over half the stencil: the
+// forward cells (dz = +1; dz = 0, dy = +1; dz = dy = 0, dx = +1) and the
+// atoms after it in its own cell, so each pair is tested once and entered in
+// both atoms' lists. The lanes of a warp hold the atoms of a few x-adjacent
+// cells and walk nearly the same rows; a row of x-adjacent cells is one run
+// of the cell-sorted arrays (two where it wraps in x). Candidates are tested
+// in binary32 on the fixed-point separations; within 1e-4 of a radius the
+// reference's binary64 test decides. Accepted pairs are buffered in shared
+// memory and entered afterwards: the centre's own entries with one atomic
+// reservation, each partner's with one atomic slot. A pair with an ion goes
+// to the Moliere pair list in both orders; with WIDE (spec mode) the ion
+// scan below lists those and ions are skipped here.
 constexpr int kBuildThreads = 128;
-constexpr int kBuildBuf = 24;  // buffered neighbours per atom
+constexpr int kBuildBuf = 24;  // buffered pairs per atom
+
+// A slot in atom x's list, or -1 (counted) when the list is full; the count
+// ends at min(entries, max_sw) whatever the order of the atomics.
+__device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, int x) {
+  const int slot = atomicAdd(&S.n_sw[x], 1);
+  if (slot < P.max_sw) return slot;
+  atomicSub(&S.n_sw[x], 1);
+  atomicAdd(&S.sc->overflow_sw, 1);
+  return -1;
+}
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, DevState S,
-                                                               int from_flag) {
+__global__ void __launch_bounds__(kBuildThreads, 10) k_build_atoms(DevParams P, DevState S,
+                                                                   int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   __shared__ int buf[kBuildBuf][kBuildThreads];
   const int t = threadIdx.x;
@@ -243,16 +254,15 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
   const int i = S.cell_atoms[h];
   const int4 qi = S.posq_cell[h];
   const int ti = qi.w & 0xff;
-  int* const nbr = S.nbr_sw + i;
   const size_t stride = (size_t)P.N;
-  int n = 0;
+  int n = 0;  // accepted SW pairs
   if (!(WIDE && ti == 3)) {
     const Geo& G = S.geo[rep_of_w(qi.w)];
     const int c = S.atom_cell[i] - G.cell_off;
     const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
     const int cx = c % nx, cy = (c / nx) % ny, cz = c / (nx * ny);
     const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
-    // inclusive x ranges of the stencil row (periodic only with > 2 cells)
+    // inclusive x ranges of a full stencil row (periodic only with > 2 cells)
     int xa0, xa1, xb0 = 0, xb1 = -1;
     if (G.wrap[0]) {
       if (cx == 0) {
@@ -270,62 +280,89 @@ __global__ void __launch_bounds__(kBuildThreads, 12) k_build_atoms(DevParams P, 
     // binary32 bound of any listed pair of this atom
     const float thr = WIDE ? P.pre_sw2A : fmaxf(P.pre_sw2A, P.pre_mol2A);
     const int4* __restrict__ qc = S.posq_cell;
-    for (int dz = -1; dz <= 1; dz++) {
-      int z = cz + dz;
-      if (G.wrap[2]) z = z < 0 ? z + nz : (z >= nz ? z - nz : z);
-      else if (z < 0 || z >= nz) continue;
-      for (int dy = -1; dy <= 1; dy++) {
-        int y = cy + dy;
-        if (G.wrap[1]) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
-        else if (y < 0 || y >= ny) continue;
-        const int row = G.cell_off + nx * (y + ny * z);
-        for (int part = 0; part < 2; part++) {
-          const int x0 = part ? xb0 : xa0, x1 = part ? xb1 : xa1;
-          if (x1 < x0) break;
-          const int b = S.cell_start[row + x0], e = S.cell_start[row + x1 + 1];
-          // two candidates per pass, their loads in flight together; the
-          // common case (outside the prefilter sphere) is the first test
-          for (int p0 = b; p0 < e; p0 += 2) {
-            const int4 q0 = __ldg(&qc[p0]);
-            const int4 q1 = p0 + 1 < e ? __ldg(&qc[p0 + 1]) : q0;
+    // candidate runs: [b, e) of the cell-sorted arrays
+    auto scan = [&](int b, int e) {
+      for (int p0 = b; p0 < e; p0 += 2) {
+        const int4 q0 = __ldg(&qc[p0]);
+        const int4 q1 = p0 + 1 < e ? __ldg(&qc[p0 + 1]) : q0;
 #pragma unroll
-            for (int u = 0; u < 2; u++) {
-              const int p = p0 + u;
-              if (p >= e) break;
-              const int4 qj = u ? q1 : q0;
-              const float3 d = qsep(qi, qj, qinvA);
-              const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-              if (r2f > thr || p == h) continue;
-              bool sw = true;
-              if (!WIDE) {
-                const int tj = qj.w & 0xff;
-                sw = (ti > tj ? ti : tj) < 3;
-                if (sw && r2f > thr_sw) continue;
-              }
-              if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) &&
-                  !exact_in(G, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
-                continue;
-              if (sw) {
-                if (n < kBuildBuf) buf[n][t] = p;
-                else if (n < P.max_sw) nbr[(size_t)n * stride] = __ldg(&S.cell_atoms[p]);
-                n++;
-              } else {
-                const int slot = atomicAdd(&S.sc->mol_count, 1);
-                if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, __ldg(&S.cell_atoms[p]));
-              }
+        for (int u = 0; u < 2; u++) {
+          const int p = p0 + u;
+          if (p >= e) break;
+          const int4 qj = u ? q1 : q0;
+          const float3 d = qsep(qi, qj, qinvA);
+          const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
+          if (r2f > thr) continue;
+          // rare from here on: inside the larger prefilter sphere
+          bool sw = true;
+          if (!WIDE) {
+            const int tj = qj.w & 0xff;
+            sw = (ti > tj ? ti : tj) < 3;
+            if (sw && r2f > thr_sw) continue;
+          }
+          if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) &&
+              !exact_in(G, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
+            continue;
+          if (sw) {
+            if (n < kBuildBuf) {
+              buf[n][t] = p;
+            } else {
+              const int j = __ldg(&S.cell_atoms[p]);
+              const int si = list_slot(P, S, i);
+              if (si >= 0) S.nbr_sw[(size_t)si * stride + i] = j;
+              const int sj = list_slot(P, S, j);
+              if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
             }
+            n++;
+          } else {
+            const int j = __ldg(&S.cell_atoms[p]);
+            const int slot = atomicAdd(&S.sc->mol_count, 2);
+            if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
+            if (slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
           }
         }
       }
+    };
+    const int rowc = G.cell_off + nx * (cy + ny * cz);
+    // own row: the atoms after this one in its cell and the cell at x + 1
+    if (G.wrap[0] && cx == nx - 1) {
+      scan(h + 1, S.cell_start[rowc + nx]);
+      scan(S.cell_start[rowc], S.cell_start[rowc + 1]);
+    } else {
+      const int xe = min(cx + 1, nx - 1);
+      scan(h + 1, S.cell_start[rowc + xe + 1]);
+    }
+    // forward rows: (dy, dz) = (+1, 0) and (-1..+1, +1)
+    for (int r = 0; r < 4; r++) {
+      const int dy = r == 0 ? 1 : r - 2, dz = r == 0 ? 0 : 1;
+      int z = cz + dz;
+      if (G.wrap[2]) z = z >= nz ? z - nz : z;
+      else if (z >= nz) continue;
+      int y = cy + dy;
+      if (G.wrap[1]) y = y < 0 ? y + ny : (y >= ny ? y - ny : y);
+      else if (y < 0 || y >= ny) continue;
+      const int row = G.cell_off + nx * (y + ny * z);
+      scan(S.cell_start[row + xa0], S.cell_start[row + xa1 + 1]);
+      if (xb1 >= xb0) scan(S.cell_start[row + xb0], S.cell_start[row + xb1 + 1]);
     }
   }
-  if (n > P.max_sw) {
-    atomicAdd(&S.sc->overflow_sw, 1);
-    n = P.max_sw;
-  }
+  // enter the buffered pairs: the centre's entries in one reservation, then
+  // the partners' (independent atomics, several in flight)
   const int nb = min(n, kBuildBuf);
-  for (int k = 0; k < nb; k++) nbr[(size_t)k * stride] = S.cell_atoms[buf[k][t]];
-  S.n_sw[i] = n;
+  if (nb > 0) {
+    int base = atomicAdd(&S.n_sw[i], nb);
+    int keep = min(nb, max(0, P.max_sw - base));
+    if (keep < nb) {
+      atomicSub(&S.n_sw[i], nb - keep);
+      atomicAdd(&S.sc->overflow_sw, 1);
+    }
+    for (int k = 0; k < nb; k++) {
+      const int j = S.cell_atoms[buf[k][t]];
+      if (k < keep) S.nbr_sw[(size_t)(base + k) * stride + i] = j;
+      const int sj = list_slot(P, S, j);
+      if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
+    }
+  }
   S.posq_build[i] = (WIDE && ti == 3) ? S.posq[i] : qi;
   S.fast_flag[i] = 0;
 }
