@@ -450,13 +450,13 @@ static int sync_scalars(fibmd_ctx* ctx) {
 }
 
 // Force launch, with events around the main kernel when kernel timing is on.
-static int force_launch(fibmd_ctx* ctx, bool energy, bool count) {
+static int force_launch(fibmd_ctx* ctx, bool energy, bool count, bool spec_step = false) {
   Launch L = launch_of(ctx);
   if (ctx->kernel_timing) {
     L.force_a = get_event(ctx);
     L.force_b = get_event(ctx);
   }
-  cudaError_t e = launch_force(L, ctx->P, ctx->S, energy, count);
+  cudaError_t e = launch_force(L, ctx->P, ctx->S, energy, count, spec_step);
   if (L.force_a) {
     ctx->pending.push_back({PH_FK, L.force_a, L.force_b});
     ctx->c[PH_FK]++;
@@ -1263,7 +1263,6 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     if (e_ != cudaSuccess) return abort_capture(e_, what); \
   } while (0)
   for (int half = 0; half < 2; half++) {
-    CKC(launch_spec_drift(L, P, Sx, Ttar), "drift");
     cudaStreamCaptureStatus st;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -1271,7 +1270,8 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
     cudaGraphConditionalHandle hi;
     CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
-    CKC(launch_set_rebuild_cond(cs, Sx.sc, hi), "cond");
+    // the drift's last block sets the rebuild condition
+    CKC(launch_spec_drift(L, P, Sx, Ttar, &hi), "drift");
     CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd), "deps");
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
@@ -1290,7 +1290,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     cudaError_t ee = cudaStreamEndCapture(ctx->cap2, &tmp);
     if (eb != cudaSuccess) return abort_capture(eb, "rebuild");
     if (ee != cudaSuccess) return abort_capture(ee, "if end");
-    CKC(launch_force(L, P, Sx, false, false), "force");
+    CKC(launch_force(L, P, Sx, false, false, true), "force");
     CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
     std::swap(Sx.frc, Sx.frc_new);
   }
@@ -1339,6 +1339,9 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     CK(cudaStreamSynchronize(ctx->stream));
     ctx->spec_ready = true;
   }
+  // the step's force accumulates into a buffer the previous kick zeroed;
+  // the first step of a call starts from whatever the buffer holds
+  CK(cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, ctx->stream));
   long long todo = max_steps;
   if (ctx->use_graph && todo >= 2) {
     int rc = run_spec_graph(ctx, todo / 2);
@@ -1357,7 +1360,7 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     }
     {
       PhaseTimer t(ctx, PH_F);
-      int rcf = force_launch(ctx, false, false);
+      int rcf = force_launch(ctx, false, false, true);
       if (rcf) return rcf;
     }
     {

@@ -716,14 +716,17 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
 }
 
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S, bool energy,
-                         bool count) {
-  cudaError_t e = cudaMemsetAsync(S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, L.stream);
-  if (e != cudaSuccess) return e;
+                         bool count, bool spec_step) {
+  cudaError_t e = cudaSuccess;
+  if (!spec_step) {
+    e = cudaMemsetAsync(S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, L.stream);
+    if (e != cudaSuccess) return e;
+  }
   if (energy) {
     e = cudaMemsetAsync(S.epot, 0, sizeof(double) * (size_t)P.N, L.stream);
     if (e != cudaSuccess) return e;
   }
-  k_force_begin<<<1, 32, 0, L.stream>>>(S);
+  if (!spec_step) k_force_begin<<<1, 32, 0, L.stream>>>(S);
   const bool mixed = P.precision == FIBMD_PREC_MIXED;
   if (mixed) {
     if (energy) return count ? force_impl<true, true, true>(L, P, S) : force_impl<true, true, false>(L, P, S);

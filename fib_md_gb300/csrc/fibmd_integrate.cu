@@ -322,7 +322,9 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z, and the rebuild trigger at half the list skin.
-__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
+__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
+                                                    cudaGraphConditionalHandle cond,
+                                                    int use_cond) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool trig = false;
   if (i < P.N) {
@@ -375,13 +377,32 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
       if (track_displacement(P, G, S, i, q) >= P.disp_fastA2) trig = true;
     }
   }
-  if (__syncthreads_or(trig) && threadIdx.x == 0) S.sc->need_rebuild = 1;
+  const bool any = __syncthreads_or(trig);
+  if (threadIdx.x != 0) return;
+  if (any) S.sc->need_rebuild = 1;
+  if (blockIdx.x == 0) {
+    // the force counters of this step (the previous step's force is done)
+    S.sc->heavy_count = 0;
+    S.sc->table_err = 0;
+    for (int k = 0; k < 4; k++) S.sc->counters[k] = 0ull;
+  }
+  if (use_cond) {
+    // the last block to finish sets the rebuild condition of the graph
+    __threadfence();
+    const unsigned t = atomicAdd(&S.sc->ticket[6], 1u);
+    if (t == gridDim.x - 1) {
+      __threadfence();
+      cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
+      S.sc->ticket[6] = 0u;
+    }
+  }
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
-                              double Ttar) {
+                              double Ttar, const cudaGraphConditionalHandle* cond) {
   (void)Ttar;
-  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S);
+  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, cond ? *cond : 0ull,
+                                                        cond ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -389,9 +410,14 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 // largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
 // thermostat layer's sum m v^2 and count. Each block writes its partials
 // (the max through the bit order of non-negative doubles, integer shuffles);
-// k_spec_finalize reduces them in block order and derives dt and the
-// Berendsen factor. No atomics, so the result does not depend on timing.
-__global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply) {
+// the last of a replica's blocks to finish (a ticket counter) reduces them
+// in block order and derives dt and the Berendsen factor, so the result does
+// not depend on which block finishes last.
+__device__ void spec_finalize(const DevParams& P, const DevState& S, int r, int apply,
+                              double Ttar);
+
+__global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
+                                                             double Ttar) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double v2 = 0.0, ts = 0.0, tc = 0.0;
   if (i < P.N) {
@@ -409,6 +435,8 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
         v.y = v.y + c * (f.y + g.y);
         v.z = v.z + c * (f.z + g.z);
         S.vel[i] = v;
+        // the old force's buffer accumulates the next force (after the swap)
+        S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
       }
       v2 = v.x * v.x + v.y * v.y + v.z * v.z;
       if ((fl & FL_THERMO) && S.atype[i] < 3) {
@@ -437,6 +465,7 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     scnt[w] = thermo ? tc : 0.0;
   }
   __syncthreads();
+  __shared__ int s_last, s_rep;
   if (threadIdx.x == 0) {
     unsigned long long m = 0ull;
     double a = 0.0, b = 0.0;
@@ -448,24 +477,48 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     S.partials[blockIdx.x] = __longlong_as_double((long long)m);
     S.partials[kMaxRedBlocks + blockIdx.x] = a;
     S.partials[2 * kMaxRedBlocks + blockIdx.x] = b;
+    // the replica of this block (blocks never straddle replicas); the last
+    // of its blocks to finish reduces the replica's partials
+    int r = 0;
+    if (P.nrep > 1) {
+      int lo = 0, hi = P.nrep - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (S.geo[mid].blk_begin <= (int)blockIdx.x) lo = mid;
+        else hi = mid - 1;
+      }
+      r = lo;
+    }
+    const Geo& G = S.geo[r];
+    __threadfence();
+    const unsigned t = atomicAdd(&S.sc[r].ticket[5], 1u);
+    s_last = t == (unsigned)(G.blk_end - G.blk_begin - 1);
+    s_rep = r;
   }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  spec_finalize(P, S, s_rep, apply, Ttar);
 }
 
-// One block per replica, over the replica's kick blocks.
-__global__ void __launch_bounds__(256) k_spec_finalize(DevParams P, DevState S, int apply,
-                                                       double Ttar) {
-  const Geo& G = S.geo[blockIdx.x];
+// dt, time and the thermostat factor of replica r from its kick blocks'
+// partials; called by all threads of the last of those blocks.
+__device__ void spec_finalize(const DevParams& P, const DevState& S, int r, int apply,
+                              double Ttar) {
+  const Geo& G = S.geo[r];
   double v[2] = {0.0, 0.0};
   double mx = 0.0;
+  const volatile double* part = S.partials;
   for (int b = G.blk_begin + threadIdx.x; b < G.blk_end; b += blockDim.x) {
-    mx = fmax(mx, S.partials[b]);
-    v[0] += S.partials[kMaxRedBlocks + b];
-    v[1] += S.partials[2 * kMaxRedBlocks + b];
+    mx = fmax(mx, part[b]);
+    v[0] += part[kMaxRedBlocks + b];
+    v[1] += part[2 * kMaxRedBlocks + b];
   }
   mx = block_max(mx);
   block_sum<2>(v);
   if (threadIdx.x != 0) return;
-  DevScalars* sc = S.sc + blockIdx.x;
+  DevScalars* sc = S.sc + r;
+  sc->ticket[5] = 0u;
   const double tsum = v[0], tcnt = v[1];
   sc->thermo_sum = tsum;
   sc->thermo_cnt = tcnt;
@@ -488,8 +541,7 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
                              double Ttar, int apply) {
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
-  k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply);
-  k_spec_finalize<<<P.nrep, 256, 0, L.stream>>>(P, S, apply, Ttar);
+  k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
   return cudaGetLastError();
 }
 

@@ -371,8 +371,10 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
 cudaError_t launch_count_triplets(const Launch& L, const DevParams& P, const DevState& S,
                                   unsigned long long* d_count, int3* out, long long cap);
 // fibmd_force.cu
+// spec_step: inside the spec-mode step, where the drift has reset the force
+// counters and the kick has zeroed the accumulation buffer
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
-                         bool energy, bool count);
+                         bool energy, bool count, bool spec_step = false);
 // fibmd_integrate.cu
 cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S,
                                double Ts, double Tau, double Ttar);
@@ -388,13 +390,12 @@ cudaError_t launch_pack(const Launch& L, int N, double4_32a* dst, const double* 
 cudaError_t launch_unpack(const Launch& L, int N, const double4_32a* src, double* dst_cm);
 cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S);
 cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevState& S);
+// cond (in a captured graph): the IF handle the rebuild hangs on
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
-                              double Ttar);
+                              double Ttar, const cudaGraphConditionalHandle* cond = nullptr);
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
 // fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
-cudaError_t launch_set_rebuild_cond(cudaStream_t s, DevScalars* sc,
-                                    cudaGraphConditionalHandle h);
 cudaError_t launch_loop_ctl(cudaStream_t s, int* remaining, cudaGraphConditionalHandle h);
 
 }  // namespace fibmd
