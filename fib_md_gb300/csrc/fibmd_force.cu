@@ -229,8 +229,21 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
 // The leg pairs are evaluated as ordered pairs: each leg's reaction is summed
 // in registers over its row and scattered once, so the shared-memory stage
 // holds only 6 floats per leg (more resident warps for the gathers).
+template <bool MIXED, bool ENERGY>
+__device__ __forceinline__ void moliere_entries(const DevParams& P, const DevState& S, int first,
+                                                int stride);
+constexpr int kMolBlocks = 2;  // blocks of the mixed force kernel that do the Moliere pairs
+
 template <bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
+  // the last kMolBlocks blocks evaluate the Moliere list (a few dozen pairs
+  // per ion), which saves a launch per step
+  const int nbm = (P.N + kBlock32 - 1) / kBlock32;
+  if ((int)blockIdx.x >= nbm) {
+    moliere_entries<true, ENERGY>(P, S, ((int)blockIdx.x - nbm) * kBlock32 + threadIdx.x,
+                                  kMolBlocks * kBlock32);
+    return;
+  }
   extern __shared__ __align__(16) unsigned char smem_raw[];
   LegSmem<float, kBlock32, kLegF32> leg;
   leg.v = reinterpret_cast<float*>(smem_raw);
@@ -634,12 +647,14 @@ __global__ void k_force_stale(DevParams P, DevState S) {
 
 // Moliere (si.f90:426-446): one thread per full-list entry (i, j) adds the
 // force on i; the (j, i) entry adds the mirror. Unfired ions are skipped.
+// Entries first, first + stride, ...
 template <bool MIXED, bool ENERGY>
-__global__ void k_force_moliere(DevParams P, DevState S) {
+__device__ __forceinline__ void moliere_entries(const DevParams& P, const DevState& S, int first,
+                                                int stride) {
   int cnt = *((volatile int*)&S.sc->mol_count);
   if (cnt > P.mol_cap) cnt = P.mol_cap;
   unsigned int npair = 0;
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
+  for (int e = first; e < cnt; e += stride) {
     const int2 pr = S.mol_pairs[e];
     const int i = pr.x, j = pr.y;
     // si_force skips unfired ions (si.f90:428); si_potential does not
@@ -686,6 +701,12 @@ __global__ void k_force_moliere(DevParams P, DevState S) {
   if (npair) atomicAdd(&S.sc->counters[2], (unsigned long long)npair);
 }
 
+template <bool MIXED, bool ENERGY>
+__global__ void k_force_moliere(DevParams P, DevState S) {
+  moliere_entries<MIXED, ENERGY>(P, S, blockIdx.x * blockDim.x + threadIdx.x,
+                                 gridDim.x * blockDim.x);
+}
+
 __global__ void k_force_begin(DevState S) {
   if (threadIdx.x == 0) {
     S.sc->heavy_count = 0;
@@ -706,10 +727,10 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
     attr_set = true;
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
-  kern<<<(P.N + BLOCK - 1) / BLOCK, BLOCK, smem, L.stream>>>(P, S);
+  kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? kMolBlocks : 0), BLOCK, smem, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
-  k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
+  if (!MIXED) k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
   k_force_heavy<MIXED, ENERGY><<<side, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
   return cudaGetLastError();
