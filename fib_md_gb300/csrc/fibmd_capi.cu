@@ -370,6 +370,8 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
     for (int b = 0; b < 2; b++) {
       P.epsA[a][b] = (float)(P.eps[a][b] / p.ec);
       P.sigA[a][b] = (float)(1e10 / P.isig[a][b]);
+      P.isigA[a][b] = (float)(P.isig[a][b] * 1e-10);
+      P.epssigA[a][b] = (float)(P.eps[a][b] / p.ec * P.isig[a][b] * 1e-10);
       for (int c = 0; c < 2; c++) P.lepsA[a][b][c] = (float)(P.leps[a][b][c] / p.ec);
     }
   for (int a = 0; a < 3; a++)

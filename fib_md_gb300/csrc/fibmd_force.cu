@@ -272,16 +272,17 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
                       float* g_o) -> bool {
     const float rinv = rsqrtf(r2f);
     const float r = r2f * rinv;
-    const float sg = P.sigA[ta][tb];
-    const float ue = r / sg;
+    const float is = P.isigA[ta][tb];
+    const float ue = r * is;
     if (!(ue < cut)) return false;
-    const float inv = 1.0f / (ue - al);
+    const float inv = __frcp_rn(ue - al);
     const float ex = expf(inv);
-    const float u2 = 1.0f / (ue * ue);
+    const float iu = P.sigA[ta][tb] * rinv;  // 1/u
+    const float u2 = iu * iu;
     const float u4 = u2 * u2;
     // psi = 4, qsi = 0: dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
-    const float dphi = Ac * ex * (-4.0f * Bc * u4 / ue - (Bc * u4 - 1.0f) * inv * inv);
-    const float c = -(dphi * rinv * (P.epsA[ta][tb] / sg));
+    const float dphi = Ac * ex * (-4.0f * Bc * u4 * iu - (Bc * u4 - 1.0f) * inv * inv);
+    const float c = -(dphi * rinv * P.epssigA[ta][tb]);
     fx += c * dq.x;
     fy += c * dq.y;
     fz += c * dq.z;
@@ -289,7 +290,7 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
     if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
     *rinv_o = rinv;
     *E_o = expf(gm * inv);
-    *g_o = -gm * inv * inv / sg;
+    *g_o = -gm * inv * inv * is;
     return true;
   };
 
@@ -493,10 +494,10 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
         const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
         const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
         const float rinv = rsqrtf(r2);
-        const float sg = P.sigA[tc - 1][tj - 1];
-        const float u = r2 * rinv / sg;
+        const float is = P.isigA[tc - 1][tj - 1];
+        const float u = r2 * rinv * is;
         if (!(u < (float)P.cut3)) continue;
-        const float ia = 1.0f / (u - (float)P.al);
+        const float ia = __frcp_rn(u - (float)P.al);
         const float E = expf((float)P.gam * ia);
         if (!(E > kLegEmin)) continue;
         const int q = atomicAdd(&snl[w], 1);
@@ -505,7 +506,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
         sl[w][2][q] = dq.z * rinv;
         sl[w][3][q] = rinv;
         sl[w][4][q] = E;
-        sl[w][5][q] = -(float)P.gam * ia * ia / sg;
+        sl[w][5][q] = -(float)P.gam * ia * ia * is;
         sj[w][q] = j | ((tj - 1) << 30);
       } else {
         const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);

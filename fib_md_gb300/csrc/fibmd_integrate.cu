@@ -334,6 +334,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
       const Geo& G = S.geo[r];
       DevScalars* R = S.sc + r;
       const double dt = ((volatile DevScalars*)R)->dt;
+      const double h2 = ((volatile DevScalars*)R)->half_dt2;
       double4_32a x = S.pos[i];
       double4_32a v = S.vel[i];
       if (fl & FL_THERMO) {
@@ -343,7 +344,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
         v.z *= s;
       }
       const double4_32a f = S.frc[i];
-      const double c = 0.5 * dt * dt * S.inv_mass[i];
+      const double c = h2 * S.inv_mass[i];
       x.x = x.x + v.x * dt + c * f.x;
       x.y = x.y + v.y * dt + c * f.y;
       x.z = x.z + v.z * dt + c * f.z;
@@ -358,12 +359,20 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
       // the bottom of a periodic box is not taken for a sputtered one
       const bool removed = G.remove_z > 0.0 && x.z > G.remove_z && S.atype[i] < 3;
       // spec mode has no bit-compatibility constraint with the reference's
-      // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped; with the
-      // cell grid cut at remove_z, z is an open axis and is not wrapped
-      x.x = x.x < 0.0 ? x.x + G.Lb[0] : (x.x >= G.Lb[0] ? x.x - G.Lb[0] : x.x);
-      x.y = x.y < 0.0 ? x.y + G.Lb[1] : (x.y >= G.Lb[1] ? x.y - G.Lb[1] : x.y);
-      if (!G.zcompact)
-        x.z = x.z < 0.0 ? x.z + G.Lb[2] : (x.z >= G.Lb[2] ? x.z - G.Lb[2] : x.z);
+      // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped, found
+      // from the integer part of the fixed-point shadow (one binary64 FMA
+      // per axis gives both); with the cell grid cut at remove_z, z is an
+      // open axis and is not wrapped
+      long long k[3];
+      double* xc[3] = {&x.x, &x.y, &x.z};
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        k[d] = fixq64(*xc[d], G.qscale[d]);
+        if ((d < 2 || !G.zcompact) && (unsigned long long)k[d] >> 32) {
+          *xc[d] += k[d] < 0 ? G.Lb[d] : -G.Lb[d];
+          k[d] = fixq64(*xc[d], G.qscale[d]);
+        }
+      }
       if (removed) {
         fl |= FL_REMOVED;
         S.flags[i] = fl;
@@ -373,7 +382,9 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
       }
       S.pos[i] = x;
       S.vel[i] = v;
-      const int4 q = store_posq(G, S, i, x.x, x.y, x.z, fl);
+      const int4 q = make_int4((int)(unsigned)k[0], (int)(unsigned)k[1], (int)(unsigned)k[2],
+                               posq_w(S.atype[i], fl));
+      S.posq[i] = q;
       if (track_displacement(P, G, S, i, q) >= P.disp_fastA2) trig = true;
     }
   }
@@ -425,12 +436,12 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     if (!(fl & FL_REMOVED)) {
       // a kick block lies inside one replica (replicas start at multiples
       // of the block size)
-      const double dt = ((volatile DevScalars*)(S.sc + rep_of_flags(fl)))->dt;
+      const double hdt = ((volatile DevScalars*)(S.sc + rep_of_flags(fl)))->half_dt;
       double4_32a v = S.vel[i];
       if (apply) {
         const double4_32a f = S.frc[i];
         const double4_32a g = S.frc_new[i];
-        const double c = 0.5 * dt * S.inv_mass[i];
+        const double c = hdt * S.inv_mass[i];
         v.x = v.x + c * (f.x + g.x);
         v.y = v.y + c * (f.y + g.y);
         v.z = v.z + c * (f.z + g.z);
@@ -528,6 +539,8 @@ __device__ void spec_finalize(const DevParams& P, const DevState& S, int r, int 
   double nd = P.dt_max;
   if (vm > 0.0 && P.dx_max / vm < nd) nd = P.dx_max / vm;
   sc->dt = nd;
+  sc->half_dt = 0.5 * nd;
+  sc->half_dt2 = 0.5 * nd * nd;
   // Berendsen factor of the thermostat layer for the next step
   double sf = 1.0;
   if (tcnt > 0.0) {

@@ -106,6 +106,7 @@ struct DevParams {
   float disp_fastA2;  // the same in A^2
   // mixed precision, reduced units (A, eV)
   float epsA[2][2], sigA[2][2], lepsA[2][2][2];
+  float isigA[2][2], epssigA[2][2];  // 1/sigma (1/A), eps/sigma (eV/A)
   float molKA[3][3];       // ie0*Zi*Zj*ec*ec in eV*A
   float amolA[3][3];       // screening length in A
   double f_evA_to_N;       // eV/A -> N
@@ -132,6 +133,8 @@ struct DevScalars {
   double ke_max;       // calc_atm: max 0.5 m v^2 / ec
   double vmax2;        // spec: max |v|^2
   double dt;           // spec: current step
+  double half_dt;      //       dt / 2 (kick)
+  double half_dt2;     //       dt^2 / 2 (drift)
   double dt_next;      // spec: step chosen from this step's velocities
   double thermo_sum, thermo_cnt;  // spec thermostat layer
   double ekin, epot;   // energies (J)
@@ -235,6 +238,12 @@ __device__ __forceinline__ double rebox1(double x, double L) {
 // |x * qscale| < 2^51.
 __device__ __forceinline__ unsigned int fixq(double x, double qscale) {
   return (unsigned int)__double_as_longlong(fma(x, qscale, 6755399441055744.0));
+}
+
+// The same integer without the wrap: round(x * qscale) as a signed 64-bit
+// value, whose high bits say how many boxes x lies away from [0, Lb).
+__device__ __forceinline__ long long fixq64(double x, double qscale) {
+  return __double_as_longlong(fma(x, qscale, 6755399441055744.0)) - 0x4338000000000000ll;
 }
 
 // binary32 separation (Angstrom) of two fixed-point positions.
