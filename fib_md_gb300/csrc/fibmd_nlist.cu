@@ -244,7 +244,7 @@ __device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, 
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kBuildThreads, 10) k_build_atoms(DevParams P, DevState S,
+__global__ void __launch_bounds__(kBuildThreads, 8) k_build_atoms(DevParams P, DevState S,
                                                                    int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   __shared__ int buf[kBuildBuf][kBuildThreads];
@@ -282,14 +282,15 @@ __global__ void __launch_bounds__(kBuildThreads, 10) k_build_atoms(DevParams P, 
     const int4* __restrict__ qc = S.posq_cell;
     // candidate runs: [b, e) of the cell-sorted arrays
     auto scan = [&](int b, int e) {
-      for (int p0 = b; p0 < e; p0 += 2) {
-        const int4 q0 = __ldg(&qc[p0]);
-        const int4 q1 = p0 + 1 < e ? __ldg(&qc[p0 + 1]) : q0;
+      for (int p0 = b; p0 < e; p0 += 4) {
+        int4 qq[4];
 #pragma unroll
-        for (int u = 0; u < 2; u++) {
+        for (int u = 0; u < 4; u++) qq[u] = __ldg(&qc[min(p0 + u, e - 1)]);
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
           const int p = p0 + u;
           if (p >= e) break;
-          const int4 qj = u ? q1 : q0;
+          const int4 qj = qq[u];
           const float3 d = qsep(qi, qj, qinvA);
           const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
           if (r2f > thr) continue;
