@@ -80,7 +80,7 @@ struct fibmd_ctx {
   cudaStream_t cap2 = nullptr;
   double4_32a* graph_frc = nullptr;  // S.frc when the graph was captured
   int graph_nfired = -1;
-  int* d_remaining = nullptr;
+  LoopCtl* d_loop = nullptr;
   // replicas: one for a single system, several for a batched ensemble
   Geo geo0;                 // the single system's geometry
   std::vector<Geo> geo;     // per replica (uploaded to S.geo)
@@ -656,7 +656,7 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   S.ion_list = ion_list;
   AL(ctx->d_stage, 3 * N);
   AL(ctx->d_u64, 4);
-  AL(ctx->d_remaining, 1);
+  AL(ctx->d_loop, 1);
 #undef AL
   if (cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
     set_noctx_error("cudaMallocHost failed");
@@ -1296,7 +1296,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
     std::swap(Sx.frc, Sx.frc_new);
   }
-  CKC(launch_loop_ctl(cs, ctx->d_remaining, hw), "loop");
+  CKC(launch_loop_ctl(cs, ctx->d_loop, Sx.sc, hw), "loop");
 #undef CKC
   cudaGraph_t out = nullptr;
   CK(cudaStreamEndCapture(cs, &out));
@@ -1311,19 +1311,16 @@ static int build_spec_graph(fibmd_ctx* ctx) {
 }
 
 // Runs `pairs` x 2 spec-mode steps with one graph launch.
-static int run_spec_graph(fibmd_ctx* ctx, long long pairs) {
+// Enqueues `pairs` step pairs (stopping early after `relax` seconds of
+// simulated time when relax > 0); returns without waiting.
+static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired) {
     int rc = build_spec_graph(ctx);
     if (rc) return rc;
   }
-  while (pairs > 0) {
-    const int chunk = (int)std::min<long long>(pairs, 1 << 30);
-    CK(cudaMemcpyAsync(ctx->d_remaining, &chunk, sizeof(int), cudaMemcpyHostToDevice,
-                       ctx->stream));
-    CK(cudaStreamSynchronize(ctx->stream));  // the host value must be read before reuse
-    CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-    pairs -= chunk;
-  }
+  if (pairs <= 0) return FIBMD_OK;
+  CK(launch_loop_set(ctx->stream, ctx->d_loop, ctx->S.sc, pairs, relax));
+  CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
   return FIBMD_OK;
 }
 
@@ -1381,6 +1378,85 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
   }
   *reason = FIBMD_STOP_MAXSTEPS;
   return check_list_status(ctx);
+}
+
+int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double* x,
+                   const double* v, long long steps, double relax_s, int* removed_after,
+                   int* ions_removed_after, double* time_after) {
+  if (!ctx || nimp < 0 || (nimp > 0 && (!ion_atoms || !x || !v)) || steps < 1)
+    return fail(ctx, FIBMD_EINVAL, "dose: bad arguments");
+  if (ctx->P.mode != FIBMD_MODE_SPEC || ctx->P.nrep != 1)
+    return fail(ctx, FIBMD_ESTATE, "dose: needs a single spec-mode system");
+  if (!ctx->use_graph) return fail(ctx, FIBMD_ESTATE, "dose: needs the graph step loop");
+  if (!ctx->lists_built) return fail(ctx, FIBMD_ESTATE, "dose: lists not built");
+  if (nimp == 0) return FIBMD_OK;
+  const int N = ctx->P.N;
+  std::vector<Impact> tab((size_t)nimp);
+  for (int k = 0; k < nimp; k++) {
+    const int a = ion_atoms[k];
+    if (a < 1 || a > N) return fail(ctx, FIBMD_EINVAL, "dose: ion atom %d out of range", a);
+    tab[k].atom = a - 1;
+    for (int d = 0; d < 3; d++) {
+      tab[k].x[d] = x[(size_t)d * nimp + k];
+      tab[k].v[d] = v[(size_t)d * nimp + k];
+    }
+  }
+  Impact* d_tab = nullptr;
+  int* d_rec = nullptr;
+  double* d_time = nullptr;
+  if (cudaMalloc((void**)&d_tab, sizeof(Impact) * (size_t)nimp) != cudaSuccess ||
+      cudaMalloc((void**)&d_rec, sizeof(int) * 2 * (size_t)nimp) != cudaSuccess ||
+      cudaMalloc((void**)&d_time, sizeof(double) * (size_t)nimp) != cudaSuccess) {
+    cudaFree(d_tab);
+    cudaFree(d_rec);
+    cudaFree(d_time);
+    return fail(ctx, FIBMD_ENOMEM, "dose: %d impacts", nimp);
+  }
+  auto done = [&](int rc) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_tab);
+    cudaFree(d_rec);
+    cudaFree(d_time);
+    return rc;
+  };
+  const Launch L = launch_of(ctx);
+  const DevParams& P = ctx->P;
+  const double Ttar = ctx->p.Ttar1;
+  cudaError_t e = cudaMemcpyAsync(d_tab, tab.data(), sizeof(Impact) * (size_t)nimp,
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)N, ctx->stream);
+  if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
+  ctx->spec_ready = true;
+  // every impact is enqueued at once: inject, a fresh step size for the new
+  // ion's speed, the cascade steps, the relaxation, the counts
+  for (int k = 0; k < nimp; k++) {
+    e = launch_inject(L, P, ctx->S, d_tab, k);
+    if (e == cudaSuccess) e = launch_spec_kick(L, P, ctx->S, Ttar, 0);
+    if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
+    int rc = run_spec_graph(ctx, (steps + 1) / 2);
+    if (rc == FIBMD_OK && relax_s > 0.0) rc = run_spec_graph(ctx, 1ll << 50, relax_s);
+    if (rc) return done(rc);
+    e = launch_dose_record(L, ctx->S, k, d_rec, d_rec + nimp, d_time);
+    if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
+  }
+  std::vector<int> rec(2 * (size_t)nimp);
+  std::vector<double> tm((size_t)nimp);
+  e = cudaMemcpyAsync(rec.data(), d_rec, sizeof(int) * rec.size(), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(tm.data(), d_time, sizeof(double) * tm.size(), cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
+  for (int k = 0; k < nimp; k++) {
+    if (removed_after) removed_after[k] = rec[k];
+    if (ions_removed_after) ions_removed_after[k] = rec[nimp + k];
+    if (time_after) time_after[k] = tm[k];
+  }
+  int rc = sync_scalars(ctx);
+  if (rc == FIBMD_OK) rc = check_list_status(ctx);
+  return done(rc);
 }
 
 int fibmd_gpu_steps(fibmd_ctx* ctx, int whichctrl, long long max_steps, long long* lt,

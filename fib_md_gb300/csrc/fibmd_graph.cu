@@ -4,20 +4,33 @@
 // runs pairs of MD steps until a device counter reaches zero, and whose IF
 // nodes run the list rebuild only on the steps where the drift found an atom
 // beyond half the skin (the drift kernel's last block sets that condition).
-// This single-thread kernel counts the step pairs down on the device, so no
-// step needs the host.
+// These single-thread kernels count the step pairs down (and stop a
+// relaxation at its end time) on the device, so no step needs the host.
 #include "fibmd_internal.cuh"
 
 namespace fibmd {
 
-__global__ void k_loop_ctl(int* remaining, cudaGraphConditionalHandle h) {
-  const int r = *remaining - 1;
-  *remaining = r;
-  cudaGraphSetConditional(h, r > 0 ? 1u : 0u);
+__global__ void k_loop_ctl(LoopCtl* loop, const DevScalars* sc, cudaGraphConditionalHandle h) {
+  const long long r = loop->pairs - 1;
+  loop->pairs = r;
+  const double t = ((const volatile DevScalars*)sc)->time;
+  cudaGraphSetConditional(h, (r > 0 && t < loop->t_stop) ? 1u : 0u);
 }
 
-cudaError_t launch_loop_ctl(cudaStream_t s, int* remaining, cudaGraphConditionalHandle h) {
-  k_loop_ctl<<<1, 1, 0, s>>>(remaining, h);
+__global__ void k_loop_set(LoopCtl* loop, const DevScalars* sc, long long pairs, double relax) {
+  loop->pairs = pairs;
+  loop->t_stop = relax > 0.0 ? ((const volatile DevScalars*)sc)->time + relax : 1.0e300;
+}
+
+cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
+                            cudaGraphConditionalHandle h) {
+  k_loop_ctl<<<1, 1, 0, s>>>(loop, sc, h);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc, long long pairs,
+                            double relax) {
+  k_loop_set<<<1, 1, 0, s>>>(loop, sc, pairs, relax);
   return cudaGetLastError();
 }
 

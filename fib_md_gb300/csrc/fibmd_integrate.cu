@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
       }
       // removal looks at the unwrapped height, so an atom leaving through
       // the bottom of a periodic box is not taken for a sputtered one
-      const bool removed = G.remove_z > 0.0 && x.z > G.remove_z && S.atype[i] < 3;
+      const bool removed = G.remove_z > 0.0 && x.z > G.remove_z;
       // spec mode has no bit-compatibility constraint with the reference's
       // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped, found
       // from the integer part of the fixed-point shadow (one binary64 FMA
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
         S.flags[i] = fl;
         v.x = v.y = v.z = 0.0;
         trig = true;
-        atomicAdd(&R->removed_count, 1);
+        atomicAdd(S.atype[i] < 3 ? &R->removed_count : &R->ions_removed, 1);
       }
       S.pos[i] = x;
       S.vel[i] = v;
@@ -555,6 +555,44 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
   k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
+  return cudaGetLastError();
+}
+
+// ---- dose: successive impacts without host round trips ---------------------
+// The device side of knock (src/knock.f90:21-55) for a dose: impact k's ion,
+// a pre-allocated atom kept removed until now, gets its start position and
+// velocity and joins the run; the lists are rebuilt before the next force.
+__global__ void k_inject(DevParams P, DevState S, const Impact* table, int k) {
+  const Impact m = table[k];
+  const int i = m.atom;
+  const uint32_t fl = S.flags[i] & ~(uint32_t)FL_REMOVED;
+  S.flags[i] = fl;
+  S.pos[i] = make_double4_32a(m.x[0], m.x[1], m.x[2], 0.0);
+  S.vel[i] = make_double4_32a(m.v[0], m.v[1], m.v[2], 0.0);
+  S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+  S.frc_new[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+  const int4 q = store_posq(S.geo[rep_of_flags(fl)], S, i, m.x[0], m.x[1], m.x[2], fl);
+  S.posq_build[i] = q;
+  S.sc->need_rebuild = 1;
+  (void)P;
+}
+
+cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S,
+                          const Impact* table, int k) {
+  k_inject<<<1, 1, 0, L.stream>>>(P, S, table, k);
+  return cudaGetLastError();
+}
+
+__global__ void k_dose_record(DevState S, int k, int* removed, int* ions_removed, double* time) {
+  const volatile DevScalars* sc = S.sc;
+  removed[k] = sc->removed_count;
+  ions_removed[k] = sc->ions_removed;
+  time[k] = sc->time;
+}
+
+cudaError_t launch_dose_record(const Launch& L, const DevState& S, int k, int* removed,
+                               int* ions_removed, double* time) {
+  k_dose_record<<<1, 1, 0, L.stream>>>(S, k, removed, ions_removed, time);
   return cudaGetLastError();
 }
 

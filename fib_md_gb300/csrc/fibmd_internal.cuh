@@ -149,10 +149,24 @@ struct DevScalars {
   int cell_oob;
   int nan_flag;
   int need_rebuild;
-  int removed_count;
+  int removed_count;   // spec: lattice atoms removed (sputtered)
+  int ions_removed;    //       ions removed (backscattered)
   unsigned long long rebuilds;  // list builds since creation
   unsigned int ticket[8];
   unsigned long long counters[4];
+};
+
+// Step-loop control of the spec-mode graph: step pairs left, and a time at
+// which the loop stops early (a relaxation of given length).
+struct LoopCtl {
+  long long pairs;
+  double t_stop;
+};
+
+// One impact of a dose: the pre-allocated ion atom and its start state.
+struct Impact {
+  int atom;
+  double x[3], v[3];
 };
 
 struct DevState {
@@ -405,6 +419,16 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
 // fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
-cudaError_t launch_loop_ctl(cudaStream_t s, int* remaining, cudaGraphConditionalHandle h);
+cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
+                            cudaGraphConditionalHandle h);
+// sets the loop to `pairs` step pairs, stopping early once the time of
+// replica 0 passes its value at this point plus `relax` (relax <= 0: no stop)
+cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc, long long pairs,
+                            double relax);
+// dose: bring impact k's ion into the run; record the counts after it
+cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S,
+                          const Impact* table, int k);
+cudaError_t launch_dose_record(const Launch& L, const DevState& S, int k, int* removed,
+                               int* ions_removed, double* time);
 
 }  // namespace fibmd

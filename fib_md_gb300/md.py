@@ -180,6 +180,55 @@ def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.
     return SpecSlab(p, X, s.Xi.copy(order="F"), V, s.mass.copy(), s.atype.copy(), tags, surf)
 
 
+@dataclass
+class DoseSlab:
+    """A spec-mode slab with pre-allocated ions for a dose of impacts: the
+    ions are atoms Nsg+1 .. Nsg+n (1-based), tagged removed until injected;
+    X0/V0 are their start states, one row per impact."""
+
+    slab: SpecSlab
+    ion_atoms: np.ndarray
+    X0: np.ndarray
+    V0: np.ndarray
+
+
+def dose_slab(cells, nimp: int, seed: int, ion_eV: float = 2000.0, window: float = 30e-10,
+              ion_height: float = 10e-10, remove_above: float = 15e-10,
+              params: Params | None = None) -> DoseSlab:
+    """A slab (spec_slab's layers, tags and 300 K velocities) with nimp ions
+    for successive impacts at normal incidence, each at a seeded uniform
+    point of a window x window square centred on the slab."""
+    p = params_default() if params is None else params.copy()
+    p.mode = _abi.MODE_SPEC
+    base = spec_slab(cells, seed, ion_eV, 0.0, ion_height=ion_height, remove_above=remove_above,
+                     params=p)
+    q = base.params
+    nsg = q.Nsg
+    s = crystal_system(tuple(cells), nimp, -abs(int(seed)) - 1, params=q)
+    q = s.params
+    N = q.Natm
+    rs = np.random.default_rng(int(seed) + 7919)
+    cx, cy = 0.5 * q.Lb[0], 0.5 * q.Lb[1]
+    X0 = np.zeros((nimp, 3))
+    X0[:, 0] = cx + rs.uniform(-0.5, 0.5, nimp) * window
+    X0[:, 1] = cy + rs.uniform(-0.5, 0.5, nimp) * window
+    X0[:, 2] = base.surface_z + ion_height
+    V0 = np.zeros((nimp, 3))
+    V0[:, 2] = -np.sqrt(2 * ion_eV * q.ec / q.massGa)
+    X = np.zeros((N, 3), order="F")
+    V = np.zeros((N, 3), order="F")
+    X[:nsg] = base.X[:nsg]
+    V[:nsg] = base.V[:nsg]
+    X[nsg:] = X0
+    tags = np.zeros(N, dtype=np.uint32)
+    tags[:nsg] = base.tags[:nsg]
+    tags[nsg:] = _abi.TAG_REMOVED
+    q.remove_z = base.params.remove_z
+    slab = SpecSlab(q, X, s.Xi.copy(order="F"), V, s.mass.copy(), s.atype.copy(), tags,
+                    base.surface_z)
+    return DoseSlab(slab, np.arange(nsg + 1, nsg + nimp + 1, dtype=np.int32), X0, V0)
+
+
 def impact_statistics(X, Xi, atype, Lb, surface_z: float, remove_z: float,
                       displaced_threshold: float = 1.0e-10):
     """Outcome of one impact from its final positions: (sputtered atoms,
@@ -363,6 +412,21 @@ class FibMD:
         self._check(self.lib.fibmd_gpu_steps(self.h, whichctrl, max_steps, C.byref(l), C.byref(t),
                                              C.byref(T), C.byref(why)), "steps")
         return l.value, t.value, T.value, why.value
+
+    def dose(self, ion_atoms, X0, V0, steps: int, relax_s: float = 0.0):
+        """Successive impacts run on the device (fibmd_gpu_dose): ion_atoms are
+        1-based indices of pre-allocated ions, X0/V0 their (n, 3) start states.
+        Returns per impact (lattice atoms removed, ions removed, time) so far."""
+        a = np.ascontiguousarray(ion_atoms, dtype=np.int32)
+        n = len(a)
+        X0 = _fortran(X0)
+        V0 = _fortran(V0)
+        rm = np.zeros(n, dtype=np.int32)
+        ir = np.zeros(n, dtype=np.int32)
+        t = np.zeros(n)
+        self._check(self.lib.fibmd_gpu_dose(self.h, n, _ip(a), _dp(X0), _dp(V0), int(steps),
+                                            float(relax_s), _ip(rm), _ip(ir), _dp(t)), "dose")
+        return rm, ir, t
 
     def temperature(self) -> float:
         T = C.c_double()

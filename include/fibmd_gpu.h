@@ -317,6 +317,20 @@ int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_dev,
                             const int* atype_dev, int impact, double* F_dev,
                             void* stream);
 
+/* A dose of successive impacts on one spec-mode system without host round
+   trips (the device side of knock, src/knock.f90:21-55, repeated): impact k
+   brings atom ion_atoms[k] (1-based; a pre-allocated ion kept removed, for
+   example tagged FIBMD_TAG_REMOVED, until its turn) to position x (nimp,3
+   column-major, m) with velocity v (m/s), then runs `steps` steps (rounded
+   up to even) and a relaxation of relax_s seconds of simulated time (<= 0:
+   none). All impacts are enqueued before the first finishes. Outputs, nimp
+   entries each (any may be NULL): lattice atoms removed (sputtered) and ions
+   removed (backscattered) so far, and the simulated time, after each impact.
+   Needs lists built and the graph step loop (fibmd_gpu_set_option "graph"). */
+int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double* x,
+                   const double* v, long long steps, double relax_s, int* removed_after,
+                   int* ions_removed_after, double* time_after);
+
 /* ---- batched ensemble (spec mode) -----------------------------------------
    Independent impacts advanced together: each replica has its own box,
    atoms, cell grid, variable dt, thermostat factor and removal count; the
