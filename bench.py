@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--ensemble-plain-sample", type=int, default=3,
                     help="impacts run one by one in plain binary64 to time that form")
     ap.add_argument("--no-ensemble", action="store_true")
+    ap.add_argument("--dose-impacts", type=int, default=10,
+                    help="impacts of the cumulative-dose run (0: skip)")
+    ap.add_argument("--dose-fp64-impacts", type=int, default=-1,
+                    help="impacts of its binary64 counterpart (default: as many)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "build"], default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64) "
                          "or rebuild the lists 5 times (build), exit (for ncu)")
@@ -602,6 +606,66 @@ def bench_ensemble(args):
 
 
 # ---------------------------------------------------------------------------
+# cumulative dose: successive impacts on one slab, run on the device
+def run_dose(d, precision, nimp, steps=3000, relax=2e-12):
+    import torch
+    import fib_md_gb300 as fm
+
+    sl = d.slab
+    p = sl.params.copy()
+    p.precision = precision
+    g = fm.FibMD(p)
+    torch.cuda.synchronize()
+    w0 = time.perf_counter()
+    g.upload(sl.X, sl.V, None, sl.Xi, sl.mass, sl.atype, np.zeros(p.Natm, np.int32))
+    g.set_tags(sl.tags)
+    g.set_impact(len(d.ion_atoms))
+    g.si_nlist()
+    g.si_force()
+    rm, ir, t = g.dose(d.ion_atoms[:nimp], d.X0[:nimp], d.V0[:nimp], steps, relax)
+    X, _, _ = g.download()
+    wall = time.perf_counter() - w0
+    g.close()
+    crater = fm.crater_depth(X, sl.atype, list(p.Lb), sl.surface_z, p.remove_z,
+                             (0.5 * p.Lb[0], 0.5 * p.Lb[1]), 30e-10)
+    return {"wall_s": wall, "removed": rm.tolist(), "ions_removed": ir.tolist(),
+            "sim_time_s": t.tolist(), "crater_depth_m": crater}
+
+
+def bench_dose(args):
+    import fib_md_gb300 as fm
+
+    n = args.dose_impacts
+    n64 = n if args.dose_fp64_impacts < 0 else min(n, args.dose_fp64_impacts)
+    d = fm.dose_slab((20, 20, 12), n, seed=4001, ion_eV=2000.0, window=30e-10,
+                     remove_above=15e-10)
+    mixed = run_dose(d, fm.PREC_MIXED, n)
+    fp64 = run_dose(d, fm.PREC_FP64, n64) if n64 > 0 else None
+    per = lambda r: np.diff(np.concatenate([[0], r["removed"]])).tolist()
+    out = {
+        "config": f"20x20x12 unit-cell slab ({d.slab.params.Nsg} Si), {n} successive 2 keV Ga "
+                  "impacts at normal incidence in a 30x30 A window (seed 4001), 3000 steps "
+                  "then 2 ps relaxation each, atoms 15 A above the surface removed, one "
+                  "device-side dose call",
+        "impacts": n,
+        "impacts_per_hour": {"mixed": 3600.0 * n / mixed["wall_s"]},
+        "wall_s": {"mixed": mixed["wall_s"]},
+        "yield_vs_dose": {"mixed": mixed["removed"]},
+        "reflected_ions": {"mixed": mixed["ions_removed"][-1]},
+        "crater_depth_m": {"mixed": mixed["crater_depth_m"]},
+        "timing": "wall clock from upload to the downloaded final state",
+    }
+    if fp64:
+        out["impacts_per_hour"]["fp64"] = 3600.0 * n64 / fp64["wall_s"]
+        out["wall_s"]["fp64"] = fp64["wall_s"]
+        out["yield_vs_dose"]["fp64"] = fp64["removed"]
+        out["reflected_ions"]["fp64"] = fp64["ions_removed"][-1]
+        out["crater_depth_m"]["fp64"] = fp64["crater_depth_m"]
+        out["mixed_vs_fp64_per_impact_yield"] = two_sample(per(mixed)[:n64], per(fp64))
+    return out
+
+
+# ---------------------------------------------------------------------------
 def cpu_baseline(cells, sample_steps, nthreads=None):
     """The oracle's onestep (binary64, the reference's algorithm) on the same
     slab over all host cores; one list build per 50 steps as ntlist_i."""
@@ -681,6 +745,8 @@ def main():
     out = bench_ours(args, rank, world, dist)
     if not args.no_ensemble:
         out["ensemble"] = bench_ensemble(args)
+    if args.dose_impacts > 0:
+        out["dose"] = bench_dose(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(cells, args.cpu_sample_steps)

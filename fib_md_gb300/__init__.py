@@ -9,12 +9,12 @@ from ._abi import (MODE_REF, MODE_SPEC, PREC_FP64, PREC_MIXED, STOP_DONE, STOP_D
                    STOP_MAXSTEPS, STOP_REGIME, TAG_FROZEN, TAG_REMOVED, TAG_THERMO, Params,
                    Siga)
 from .md import (DoseSlab, FibMD, FibMDBatch, FibmdError, Ran1, SpecSlab, System, crystal_system,
-                 dose_slab, knock,
+                 crater_depth, dose_slab, knock,
                  impact_statistics, params_default, pureepi, read_siga, spec_slab)
 
 __all__ = [
     "FibMD", "FibMDBatch", "FibmdError", "Params", "Siga", "Ran1", "SpecSlab", "System",
-    "crystal_system", "DoseSlab", "dose_slab", "impact_statistics", "knock", "spec_slab",
+    "crater_depth", "crystal_system", "DoseSlab", "dose_slab", "impact_statistics", "knock", "spec_slab",
     "params_default", "pureepi", "read_siga", "MODE_REF", "MODE_SPEC", "PREC_FP64",
     "PREC_MIXED", "TAG_FROZEN", "TAG_THERMO", "TAG_REMOVED", "STOP_MAXSTEPS", "STOP_DUMP",
     "STOP_DONE", "STOP_REGIME",

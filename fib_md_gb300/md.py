@@ -229,6 +229,26 @@ def dose_slab(cells, nimp: int, seed: int, ion_eV: float = 2000.0, window: float
     return DoseSlab(slab, np.arange(nsg + 1, nsg + nimp + 1, dtype=np.int32), X0, V0)
 
 
+def crater_depth(X, atype, Lb, surface_z: float, remove_z: float, centre, window: float,
+                 column: float = 3.0e-10) -> float:
+    """Deepest point of the surface inside a window x window square around
+    centre (x, y): the top lattice atom of each column x column bin, and the
+    largest drop of those below the initial surface (m; 0 if none)."""
+    X = np.asarray(X)
+    keep = (np.asarray(atype) < 3) & (X[:, 2] <= remove_z)
+    L = np.asarray(Lb, dtype=np.float64)[:2]
+    d = X[keep, :2] - np.asarray(centre, dtype=np.float64)[None, :]
+    d -= L * np.rint(d / L)
+    inside = np.all(np.abs(d) < 0.5 * window, axis=1)
+    z = X[keep, 2][inside]
+    ij = np.floor((d[inside] + 0.5 * window) / column).astype(int)
+    nb = int(np.ceil(window / column))
+    top = np.full((nb, nb), -np.inf)
+    np.maximum.at(top, (ij[:, 0].clip(0, nb - 1), ij[:, 1].clip(0, nb - 1)), z)
+    top = top[np.isfinite(top)]
+    return float(max(0.0, surface_z - top.min())) if top.size else 0.0
+
+
 def impact_statistics(X, Xi, atype, Lb, surface_z: float, remove_z: float,
                       displaced_threshold: float = 1.0e-10):
     """Outcome of one impact from its final positions: (sputtered atoms,
