@@ -474,6 +474,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
   // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sl[kHeavyWarps][6][kHeavyLegs];
+  __shared__ R sr[kHeavyWarps][4][kHeavyLegs];  // reaction x, y, z and energy per leg
   __shared__ int sj[kHeavyWarps][kHeavyLegs];
   __shared__ int snl[kHeavyWarps];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -524,48 +525,66 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     }
     __syncwarp();
     const int nl = snl[w];
-    double fcx = 0, fcy = 0, fcz = 0, uc = 0;
+    for (int k = lane; k < nl; k += 32) sr[w][0][k] = sr[w][1][k] = sr[w][2][k] = sr[w][3][k] = 0;
+    __syncwarp();
+    // the nl(nl-1)/2 leg pairs shared out over the lanes; each leg's reaction
+    // is summed in shared memory and scattered once
+    R fcx = 0, fcy = 0, fcz = 0, uc = 0;
     const R thrd = (R)P.thrd;
-    for (int a = 0; a < nl; a++) {
-      for (int b = a + 1 + lane; b < nl; b += 32) {
-        const R ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
-        const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
-        const R ar = sl[w][3][a], br = sl[w][3][b];
-        const int ja = sj[w][a], jb = sj[w][b];
-        const R cs = ax * bx + ay * by + az * bz;
-        const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
-        R lp;
-        if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-        else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-        const R pref = lp * sl[w][4][a] * sl[w][4][b];
-        const R wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
-        const R wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
-        const double Fax = conv * (double)(pref * (wa * ax + sa * bx));
-        const double Fay = conv * (double)(pref * (wa * ay + sa * by));
-        const double Faz = conv * (double)(pref * (wa * az + sa * bz));
-        const double Fbx = conv * (double)(pref * (wb * bx + sb * ax));
-        const double Fby = conv * (double)(pref * (wb * by + sb * ay));
-        const double Fbz = conv * (double)(pref * (wb * bz + sb * az));
-        atomic_add3(S.frc_new, ja & 0x3fffffff, Fax, Fay, Faz);
-        atomic_add3(S.frc_new, jb & 0x3fffffff, Fbx, Fby, Fbz);
-        fcx -= Fax + Fbx;
-        fcy -= Fay + Fby;
-        fcz -= Faz + Fbz;
-        if (ENERGY) {
-          const double e3 = econv * (double)(pref * W) / 3.0;
-          uc += e3;
-          atomicAdd(&S.epot[ja & 0x3fffffff], e3);
-          atomicAdd(&S.epot[jb & 0x3fffffff], e3);
-        }
+    const int npair = nl * (nl - 1) / 2;
+    int a = 0, a_end = nl - 1;  // pairs of leg a are [a_end - (nl - 1 - a), a_end)
+    for (int q = lane; q < npair; q += 32) {
+      while (q >= a_end) {
+        a++;
+        a_end += nl - 1 - a;
+      }
+      const int b = nl - (a_end - q);
+      const R ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
+      const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
+      const R ar = sl[w][3][a], br = sl[w][3][b];
+      const int ja = sj[w][a], jb = sj[w][b];
+      const R cs = ax * bx + ay * by + az * bz;
+      const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
+      R lp;
+      if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+      else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+      const R pref = lp * sl[w][4][a] * sl[w][4][b];
+      const R wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
+      const R wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
+      const R Fax = pref * (wa * ax + sa * bx), Fay = pref * (wa * ay + sa * by),
+              Faz = pref * (wa * az + sa * bz);
+      const R Fbx = pref * (wb * bx + sb * ax), Fby = pref * (wb * by + sb * ay),
+              Fbz = pref * (wb * bz + sb * az);
+      atomicAdd(&sr[w][0][a], Fax);
+      atomicAdd(&sr[w][1][a], Fay);
+      atomicAdd(&sr[w][2][a], Faz);
+      atomicAdd(&sr[w][0][b], Fbx);
+      atomicAdd(&sr[w][1][b], Fby);
+      atomicAdd(&sr[w][2][b], Fbz);
+      fcx -= Fax + Fbx;
+      fcy -= Fay + Fby;
+      fcz -= Faz + Fbz;
+      if (ENERGY) {
+        const R e3 = pref * W / (R)3;
+        uc += e3;
+        atomicAdd(&sr[w][3][a], e3);
+        atomicAdd(&sr[w][3][b], e3);
       }
     }
-    fcx = warp_sum(fcx);
-    fcy = warp_sum(fcy);
-    fcz = warp_sum(fcz);
-    if (ENERGY) uc = warp_sum(uc);
+    __syncwarp();
+    for (int k = lane; k < nl; k += 32) {
+      const int j = sj[w][k] & 0x3fffffff;
+      atomic_add3(S.frc_new, j, conv * (double)sr[w][0][k], conv * (double)sr[w][1][k],
+                  conv * (double)sr[w][2][k]);
+      if (ENERGY && sr[w][3][k] != (R)0) atomicAdd(&S.epot[j], econv * (double)sr[w][3][k]);
+    }
+    const double dcx = warp_sum(conv * (double)fcx);
+    const double dcy = warp_sum(conv * (double)fcy);
+    const double dcz = warp_sum(conv * (double)fcz);
+    const double duc = ENERGY ? warp_sum(econv * (double)uc) : 0.0;
     if (lane == 0) {
-      atomic_add3(S.frc_new, c, fcx, fcy, fcz);
-      if (ENERGY && uc != 0.0) atomicAdd(&S.epot[c], uc);
+      atomic_add3(S.frc_new, c, dcx, dcy, dcz);
+      if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
     }
     __syncwarp();
   }
