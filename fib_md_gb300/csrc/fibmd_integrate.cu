@@ -419,14 +419,10 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 
 // Kick (apply != 0) followed by the reductions the next step needs: the
 // largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
-// thermostat layer's sum m v^2 and count. Each block writes its partials
-// (the max through the bit order of non-negative doubles, integer shuffles);
-// the last of a replica's blocks to finish (a ticket counter) reduces them
-// in block order and derives dt and the Berendsen factor, so the result does
-// not depend on which block finishes last.
-__device__ void spec_finalize(const DevParams& P, const DevState& S, int r, int apply,
-                              double Ttar);
-
+// thermostat layer's sum m v^2 and count. Each block adds its share to the
+// replica's accumulators (the max through the bit order of non-negative
+// doubles, an integer atomic); the last of a replica's blocks to finish (a
+// ticket counter) derives dt and the Berendsen factor from them.
 __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
                                                              double Ttar) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -476,78 +472,53 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     scnt[w] = thermo ? tc : 0.0;
   }
   __syncthreads();
-  __shared__ int s_last, s_rep;
-  if (threadIdx.x == 0) {
-    unsigned long long m = 0ull;
-    double a = 0.0, b = 0.0;
-    for (int q = 0; q < kKickThreads / 32; q++) {
-      m = smax[q] > m ? smax[q] : m;
-      a += ssum[q];
-      b += scnt[q];
-    }
-    S.partials[blockIdx.x] = __longlong_as_double((long long)m);
-    S.partials[kMaxRedBlocks + blockIdx.x] = a;
-    S.partials[2 * kMaxRedBlocks + blockIdx.x] = b;
-    // the replica of this block (blocks never straddle replicas); the last
-    // of its blocks to finish reduces the replica's partials
-    int r = 0;
-    if (P.nrep > 1) {
-      int lo = 0, hi = P.nrep - 1;
-      while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (S.geo[mid].blk_begin <= (int)blockIdx.x) lo = mid;
-        else hi = mid - 1;
-      }
-      r = lo;
-    }
-    const Geo& G = S.geo[r];
-    __threadfence();
-    const unsigned t = atomicAdd(&S.sc[r].ticket[5], 1u);
-    s_last = t == (unsigned)(G.blk_end - G.blk_begin - 1);
-    s_rep = r;
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  spec_finalize(P, S, s_rep, apply, Ttar);
-}
-
-// dt, time and the thermostat factor of replica r from its kick blocks'
-// partials; called by all threads of the last of those blocks.
-__device__ void spec_finalize(const DevParams& P, const DevState& S, int r, int apply,
-                              double Ttar) {
-  const Geo& G = S.geo[r];
-  double v[2] = {0.0, 0.0};
-  double mx = 0.0;
-  const volatile double* part = S.partials;
-  for (int b = G.blk_begin + threadIdx.x; b < G.blk_end; b += blockDim.x) {
-    mx = fmax(mx, part[b]);
-    v[0] += part[kMaxRedBlocks + b];
-    v[1] += part[2 * kMaxRedBlocks + b];
-  }
-  mx = block_max(mx);
-  block_sum<2>(v);
   if (threadIdx.x != 0) return;
-  DevScalars* sc = S.sc + r;
-  sc->ticket[5] = 0u;
-  const double tsum = v[0], tcnt = v[1];
-  sc->thermo_sum = tsum;
-  sc->thermo_cnt = tcnt;
-  sc->vmax2 = mx;
-  if (apply) sc->time += sc->dt;
+  unsigned long long m = 0ull;
+  double a = 0.0, b = 0.0;
+  for (int q = 0; q < kKickThreads / 32; q++) {
+    m = smax[q] > m ? smax[q] : m;
+    a += ssum[q];
+    b += scnt[q];
+  }
+  // the replica of this block: its first atom's (blocks never straddle
+  // replicas, and a replica's padding only ends its last block)
+  const int i0 = blockIdx.x * blockDim.x;
+  const int r = i0 < P.N ? rep_of_flags(S.flags[i0]) : 0;
+  DevScalars* R = S.sc + r;
+  atomicMax(&R->acc_vmax2, m);
+  if (a != 0.0) atomicAdd(&R->acc_tsum, a);
+  if (b != 0.0) atomicAdd(&R->acc_tcnt, b);
+  // the last of the replica's blocks derives dt and the thermostat factor
+  // and clears the accumulators for the next kick
+  const Geo& G = S.geo[r];
+  __threadfence();
+  const unsigned t = atomicAdd(&R->ticket[5], 1u);
+  if (t != (unsigned)(G.blk_end - G.blk_begin - 1)) return;
+  __threadfence();
+  volatile DevScalars* V = R;
+  const double mx = __longlong_as_double((long long)V->acc_vmax2);
+  const double tsum = V->acc_tsum, tcnt = V->acc_tcnt;
+  R->acc_vmax2 = 0ull;
+  R->acc_tsum = 0.0;
+  R->acc_tcnt = 0.0;
+  R->ticket[5] = 0u;
+  R->thermo_sum = tsum;
+  R->thermo_cnt = tcnt;
+  R->vmax2 = mx;
+  if (apply) R->time += R->dt;
   const double vm = sqrt(mx);
   double nd = P.dt_max;
   if (vm > 0.0 && P.dx_max / vm < nd) nd = P.dx_max / vm;
-  sc->dt = nd;
-  sc->half_dt = 0.5 * nd;
-  sc->half_dt2 = 0.5 * nd * nd;
+  R->dt = nd;
+  R->half_dt = 0.5 * nd;
+  R->half_dt2 = 0.5 * nd * nd;
   // Berendsen factor of the thermostat layer for the next step
   double sf = 1.0;
   if (tcnt > 0.0) {
     const double T = tsum / 3. / tcnt / P.kB;
     if (T > 0.0) sf = sqrt(1. + nd / P.tau_spec * (Ttar / T - 1.));
   }
-  sc->thermo_s = sf;
+  R->thermo_s = sf;
 }
 
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,

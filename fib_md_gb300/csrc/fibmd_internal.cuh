@@ -135,6 +135,8 @@ struct DevScalars {
   double dt;           // spec: current step
   double half_dt;      //       dt / 2 (kick)
   double half_dt2;     //       dt^2 / 2 (drift)
+  unsigned long long acc_vmax2;   // spec kick accumulators: max |v|^2 (bits),
+  double acc_tsum, acc_tcnt;      // thermostat layer sum m v^2 and count
   double dt_next;      // spec: step chosen from this step's velocities
   double thermo_sum, thermo_cnt;  // spec thermostat layer
   double ekin, epot;   // energies (J)
