@@ -874,6 +874,8 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   CK(launch_update_posq(L, ctx->P, ctx->S));
   if (ctx->lists_built) CK(launch_track_all(L, ctx->P, ctx->S));
   CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemsetAsync(&ctx->S.sc->nan_flag, 0, sizeof(int), ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
   return FIBMD_OK;
@@ -951,6 +953,8 @@ int fibmd_gpu_regime(fibmd_ctx* ctx, double* Ts, int* tic) {
 
 static int check_list_status(fibmd_ctx* ctx) {
   const DevScalars& h = *ctx->h_sc;
+  if (h.nan_flag)
+    return fail(ctx, FIBMD_ENAN, "non-finite velocity after a kick (upload a valid state)");
   if (h.overflow_sw)
     return fail(ctx, FIBMD_EOVERFLOW, "%d atoms exceeded %d SW list slots", h.overflow_sw,
                 ctx->P.max_sw);

@@ -35,8 +35,11 @@ namespace fibmd {
 __device__ __forceinline__ double table_df(const DevParams& P, const double* __restrict__ tab,
                                            const double* __restrict__ tabu, double ue,
                                            int* err) {
-  const int it = (int)(ue / P.umax * (double)(P.Ntable - 1));
-  if (it > P.tab_last) return 0.0;  // all three stencil entries are zero
+  const double t = ue / P.umax * (double)(P.Ntable - 1);
+  // all three stencil entries are zero beyond tab_last; a non-finite ue (a
+  // corrupted state, reported by the kick) must not become an index either
+  if (!(t >= 0.0 && t < (double)(P.tab_last + 1))) return 0.0;
+  const int it = (int)t;
   if (it + 1 > P.Ntable) {
     *err = 1;
     return 0.0;

@@ -229,6 +229,7 @@ __global__ void __launch_bounds__(256) k_kick(DevParams P, DevState S, double Ts
   v.y = v.y + c * (f.y + g.y);
   v.z = v.z + c * (f.z + g.z);
   S.vel[i] = v;
+  if (!(v.x * v.x + v.y * v.y + v.z * v.z < INFINITY)) atomicOr(&S.sc->nan_flag, 1);
 }
 
 cudaError_t launch_kick(const Launch& L, const DevParams& P, const DevState& S, double Ts) {
@@ -446,6 +447,11 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
         S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
       }
       v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+      // a non-finite force or velocity shows here; the host reports it
+      if (!(v2 < INFINITY)) {
+        atomicOr(&S.sc->nan_flag, 1);
+        v2 = 0.0;
+      }
       if ((fl & FL_THERMO) && S.atype[i] < 3) {
         ts = S.mass[i] * v2;
         tc = 1.0;

@@ -181,3 +181,30 @@ def test_spec_compact_grid_trajectory(gpu_lib):
     assert dmax < 1e-18, dmax
     assert ca[4] > 10 and abs(ca[4] - cb[4]) <= 3, (ca[4], cb[4])
     assert np.array_equal(swa, swb) and np.array_equal(ma, mb) and len(ma) > 0
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_nonfinite_state_is_reported(gpu_lib, mode):
+    """A non-finite velocity (a failure made on the host: a NaN uploaded)
+    ends the step call with FIBMD_ENAN; a valid upload clears it."""
+    import fib_md_gb300 as fm
+
+    s, X, V = _spec_system(nc=(4, 4, 3))
+    p = s.params.copy()
+    p.mode = mode
+    g = fm.FibMD(p)
+    Vbad = V.copy()
+    Vbad[7, 1] = np.nan
+    g.upload(X, Vbad, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+    with pytest.raises(fm.FibmdError) as e:
+        g.steps(2, 4, 0, 0.0, 300.0)
+    assert e.value.code == fm._abi.ENAN
+    assert "non-finite" in str(e.value)
+    g.upload(X, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+    g.si_nlist()
+    g.si_force()
+    g.steps(2, 4, 0, 0.0, 300.0)
+    g.close()
