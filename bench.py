@@ -388,7 +388,8 @@ def bench_ours(args, rank, world, dist):
                            "slope of a line fitted to 11 samples of the total energy",
         },
         "work_counters": {"sw_pairs": counts[0], "angle_terms": counts[1],
-                          "moliere_pairs": counts[2], "stale_terms": counts[3]},
+                          "moliere_pairs": counts[2], "stale_terms": counts[3],
+                          "many_leg_centres": counts[5]},
         # per MD step: drift, rebuild condition, force (begin, main, Moliere,
         # many-leg), kick + finalize = 8; per step pair the loop control;
         # 9 kernels per list rebuild; one temperature kernel per bench step
