@@ -24,6 +24,7 @@
 //     With it the set of non-zero terms equals the reference's exactly.
 // Centres with more than kMaxLegs active legs are deferred to a direct
 // binary64 kernel.
+#include <algorithm>
 #include <type_traits>
 
 #include "fibmd_internal.cuh"
@@ -235,16 +236,18 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
 template <bool MIXED, bool ENERGY>
 __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevState& S, int first,
                                                 int stride);
-constexpr int kMolBlocks = 2;  // blocks of the mixed force kernel that do the Moliere pairs
+// blocks of the mixed force kernel that do the Moliere pairs: one per two
+// ions (an ion has a few dozen listed pairs, both orders), at least two
+inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P.nion + 1) / 2)); }
 
 template <bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
-  // the last kMolBlocks blocks evaluate the Moliere list (a few dozen pairs
+  // the last mol_blocks blocks evaluate the Moliere list (a few dozen pairs
   // per ion), which saves a launch per step
   const int nbm = (P.N + kBlock32 - 1) / kBlock32;
   if ((int)blockIdx.x >= nbm) {
     moliere_entries<true, ENERGY>(P, S, ((int)blockIdx.x - nbm) * kBlock32 + threadIdx.x,
-                                  kMolBlocks * kBlock32);
+                                  ((int)gridDim.x - nbm) * kBlock32);
     return;
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -750,11 +753,15 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
     attr_set = true;
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
-  kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? kMolBlocks : 0), BLOCK, smem, L.stream>>>(P, S);
+  kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   if (!MIXED) k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
-  k_force_heavy<MIXED, ENERGY><<<side, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
+  // one warp per many-leg centre; the count is known only on the device, so
+  // the grid covers thousands of centres (cascade cores of a batch) in one
+  // round and idle warps return at once
+  const int heavy_blocks = std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
+  k_force_heavy<MIXED, ENERGY><<<heavy_blocks, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
   return cudaGetLastError();
 }
