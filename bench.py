@@ -623,14 +623,15 @@ def run_dose(d, precision, nimp, steps=3000, relax=2e-12):
     g.set_impact(len(d.ion_atoms))
     g.si_nlist()
     g.si_force()
-    rm, ir, t = g.dose(d.ion_atoms[:nimp], d.X0[:nimp], d.V0[:nimp], steps, relax)
+    rm, ir, t, st = g.dose(d.ion_atoms[:nimp], d.X0[:nimp], d.V0[:nimp], steps, relax)
     X, _, _ = g.download()
     wall = time.perf_counter() - w0
     g.close()
     crater = fm.crater_depth(X, sl.atype, list(p.Lb), sl.surface_z, p.remove_z,
                              (0.5 * p.Lb[0], 0.5 * p.Lb[1]), 30e-10)
     return {"wall_s": wall, "removed": rm.tolist(), "ions_removed": ir.tolist(),
-            "sim_time_s": t.tolist(), "crater_depth_m": crater}
+            "sim_time_s": t.tolist(), "md_steps": int(st[-1]), "atoms": int(sl.params.Natm),
+            "crater_depth_m": crater}
 
 
 def bench_dose(args):
@@ -651,6 +652,8 @@ def bench_dose(args):
         "impacts": n,
         "impacts_per_hour": {"mixed": 3600.0 * n / mixed["wall_s"]},
         "wall_s": {"mixed": mixed["wall_s"]},
+        "md_steps": {"mixed": mixed["md_steps"]},
+        "atom_steps_per_s": {"mixed": mixed["atoms"] * mixed["md_steps"] / mixed["wall_s"]},
         "yield_vs_dose": {"mixed": mixed["removed"]},
         "reflected_ions": {"mixed": mixed["ions_removed"][-1]},
         "crater_depth_m": {"mixed": mixed["crater_depth_m"]},
@@ -659,6 +662,8 @@ def bench_dose(args):
     if fp64:
         out["impacts_per_hour"]["fp64"] = 3600.0 * n64 / fp64["wall_s"]
         out["wall_s"]["fp64"] = fp64["wall_s"]
+        out["md_steps"]["fp64"] = fp64["md_steps"]
+        out["atom_steps_per_s"]["fp64"] = fp64["atoms"] * fp64["md_steps"] / fp64["wall_s"]
         out["yield_vs_dose"]["fp64"] = fp64["removed"]
         out["reflected_ions"]["fp64"] = fp64["ions_removed"][-1]
         out["crater_depth_m"]["fp64"] = fp64["crater_depth_m"]

@@ -119,7 +119,7 @@ SIGNATURES = {
     "fibmd_gpu_phase_times": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),
     "fibmd_gpu_force_noalloc": (_I, [C.POINTER(Params), _VP, _VP, _I, _VP, _VP]),
-    "fibmd_gpu_dose": (_I, [_VP, _I, _IP, _DP, _DP, C.c_longlong, _D, _IP, _IP, _DP]),
+    "fibmd_gpu_dose": (_I, [_VP, _I, _IP, _DP, _DP, C.c_longlong, _D, _IP, _IP, _DP, _LLP]),
     "fibmd_gpu_batch_create": (_I, [C.POINTER(Params), _I, C.POINTER(Replica), C.POINTER(_VP)]),
     "fibmd_gpu_batch_layout": (_I, [_VP, _IP, _IP]),
     "fibmd_gpu_batch_scalars": (_I, [_VP, _DP, _DP, _IP]),

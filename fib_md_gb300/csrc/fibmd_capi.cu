@@ -657,6 +657,7 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   AL(ctx->d_stage, 3 * N);
   AL(ctx->d_u64, 4);
   AL(ctx->d_loop, 1);
+  cudaMemsetAsync(ctx->d_loop, 0, sizeof(LoopCtl), ctx->stream);
 #undef AL
   if (cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
     set_noctx_error("cudaMallocHost failed");
@@ -1386,7 +1387,7 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
 
 int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double* x,
                    const double* v, long long steps, double relax_s, int* removed_after,
-                   int* ions_removed_after, double* time_after) {
+                   int* ions_removed_after, double* time_after, long long* steps_after) {
   if (!ctx || nimp < 0 || (nimp > 0 && (!ion_atoms || !x || !v)) || steps < 1)
     return fail(ctx, FIBMD_EINVAL, "dose: bad arguments");
   if (ctx->P.mode != FIBMD_MODE_SPEC || ctx->P.nrep != 1)
@@ -1408,12 +1409,15 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
   Impact* d_tab = nullptr;
   int* d_rec = nullptr;
   double* d_time = nullptr;
+  long long* d_steps = nullptr;
   if (cudaMalloc((void**)&d_tab, sizeof(Impact) * (size_t)nimp) != cudaSuccess ||
       cudaMalloc((void**)&d_rec, sizeof(int) * 2 * (size_t)nimp) != cudaSuccess ||
-      cudaMalloc((void**)&d_time, sizeof(double) * (size_t)nimp) != cudaSuccess) {
+      cudaMalloc((void**)&d_time, sizeof(double) * (size_t)nimp) != cudaSuccess ||
+      cudaMalloc((void**)&d_steps, sizeof(long long) * (size_t)(nimp + 1)) != cudaSuccess) {
     cudaFree(d_tab);
     cudaFree(d_rec);
     cudaFree(d_time);
+    cudaFree(d_steps);
     return fail(ctx, FIBMD_ENOMEM, "dose: %d impacts", nimp);
   }
   auto done = [&](int rc) {
@@ -1421,6 +1425,7 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
     cudaFree(d_tab);
     cudaFree(d_rec);
     cudaFree(d_time);
+    cudaFree(d_steps);
     return rc;
   };
   const Launch L = launch_of(ctx);
@@ -1432,6 +1437,10 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
     e = cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)N, ctx->stream);
   if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
   ctx->spec_ready = true;
+  // the step count before the first impact
+  if (e == cudaSuccess) e = launch_dose_record(L, ctx->S, ctx->d_loop, 0, d_rec, d_rec + nimp,
+                                               d_time, d_steps);
+  if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
   // every impact is enqueued at once: inject, a fresh step size for the new
   // ion's speed, the cascade steps, the relaxation, the counts
   for (int k = 0; k < nimp; k++) {
@@ -1441,11 +1450,15 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
     int rc = run_spec_graph(ctx, (steps + 1) / 2);
     if (rc == FIBMD_OK && relax_s > 0.0) rc = run_spec_graph(ctx, 1ll << 50, relax_s);
     if (rc) return done(rc);
-    e = launch_dose_record(L, ctx->S, k, d_rec, d_rec + nimp, d_time);
+    e = launch_dose_record(L, ctx->S, ctx->d_loop, k, d_rec, d_rec + nimp, d_time, d_steps + 1);
     if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
   }
   std::vector<int> rec(2 * (size_t)nimp);
   std::vector<double> tm((size_t)nimp);
+  std::vector<long long> st((size_t)nimp + 1);
+  e = cudaMemcpyAsync(st.data(), d_steps, sizeof(long long) * st.size(), cudaMemcpyDeviceToHost,
+                      ctx->stream);
+  if (e != cudaSuccess) return done(fail(ctx, FIBMD_ECUDA, "dose: %s", cudaGetErrorString(e)));
   e = cudaMemcpyAsync(rec.data(), d_rec, sizeof(int) * rec.size(), cudaMemcpyDeviceToHost,
                       ctx->stream);
   if (e == cudaSuccess)
@@ -1457,6 +1470,7 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
     if (removed_after) removed_after[k] = rec[k];
     if (ions_removed_after) ions_removed_after[k] = rec[nimp + k];
     if (time_after) time_after[k] = tm[k];
+    if (steps_after) steps_after[k] = st[k + 1] - st[0];
   }
   int rc = sync_scalars(ctx);
   if (rc == FIBMD_OK) rc = check_list_status(ctx);

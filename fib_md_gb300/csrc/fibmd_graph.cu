@@ -13,6 +13,7 @@ namespace fibmd {
 __global__ void k_loop_ctl(LoopCtl* loop, const DevScalars* sc, cudaGraphConditionalHandle h) {
   const long long r = loop->pairs - 1;
   loop->pairs = r;
+  loop->pairs_run += 1;
   const double t = ((const volatile DevScalars*)sc)->time;
   cudaGraphSetConditional(h, (r > 0 && t < loop->t_stop) ? 1u : 0u);
 }

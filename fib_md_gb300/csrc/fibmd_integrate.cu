@@ -560,16 +560,18 @@ cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S
   return cudaGetLastError();
 }
 
-__global__ void k_dose_record(DevState S, int k, int* removed, int* ions_removed, double* time) {
+__global__ void k_dose_record(DevState S, const LoopCtl* loop, int k, int* removed,
+                              int* ions_removed, double* time, long long* steps) {
   const volatile DevScalars* sc = S.sc;
   removed[k] = sc->removed_count;
   ions_removed[k] = sc->ions_removed;
   time[k] = sc->time;
+  steps[k] = 2 * ((const volatile LoopCtl*)loop)->pairs_run;
 }
 
-cudaError_t launch_dose_record(const Launch& L, const DevState& S, int k, int* removed,
-                               int* ions_removed, double* time) {
-  k_dose_record<<<1, 1, 0, L.stream>>>(S, k, removed, ions_removed, time);
+cudaError_t launch_dose_record(const Launch& L, const DevState& S, const LoopCtl* loop, int k,
+                               int* removed, int* ions_removed, double* time, long long* steps) {
+  k_dose_record<<<1, 1, 0, L.stream>>>(S, loop, k, removed, ions_removed, time, steps);
   return cudaGetLastError();
 }
 

@@ -163,6 +163,7 @@ struct DevScalars {
 struct LoopCtl {
   long long pairs;
   double t_stop;
+  long long pairs_run;  // step pairs run since the context was created
 };
 
 // One impact of a dose: the pre-allocated ion atom and its start state.
@@ -430,7 +431,7 @@ cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
 // dose: bring impact k's ion into the run; record the counts after it
 cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S,
                           const Impact* table, int k);
-cudaError_t launch_dose_record(const Launch& L, const DevState& S, int k, int* removed,
-                               int* ions_removed, double* time);
+cudaError_t launch_dose_record(const Launch& L, const DevState& S, const LoopCtl* loop, int k,
+                               int* removed, int* ions_removed, double* time, long long* steps);
 
 }  // namespace fibmd

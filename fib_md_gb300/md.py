@@ -436,7 +436,8 @@ class FibMD:
     def dose(self, ion_atoms, X0, V0, steps: int, relax_s: float = 0.0):
         """Successive impacts run on the device (fibmd_gpu_dose): ion_atoms are
         1-based indices of pre-allocated ions, X0/V0 their (n, 3) start states.
-        Returns per impact (lattice atoms removed, ions removed, time) so far."""
+        Returns per impact (lattice atoms removed, ions removed, time, MD steps)
+        so far."""
         a = np.ascontiguousarray(ion_atoms, dtype=np.int32)
         n = len(a)
         X0 = _fortran(X0)
@@ -444,9 +445,11 @@ class FibMD:
         rm = np.zeros(n, dtype=np.int32)
         ir = np.zeros(n, dtype=np.int32)
         t = np.zeros(n)
+        st = np.zeros(n, dtype=np.int64)
         self._check(self.lib.fibmd_gpu_dose(self.h, n, _ip(a), _dp(X0), _dp(V0), int(steps),
-                                            float(relax_s), _ip(rm), _ip(ir), _dp(t)), "dose")
-        return rm, ir, t
+                                            float(relax_s), _ip(rm), _ip(ir), _dp(t),
+                                            st.ctypes.data_as(C.POINTER(C.c_longlong))), "dose")
+        return rm, ir, t, st
 
     def temperature(self) -> float:
         T = C.c_double()

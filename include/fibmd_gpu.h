@@ -325,11 +325,12 @@ int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_dev,
    up to even) and a relaxation of relax_s seconds of simulated time (<= 0:
    none). All impacts are enqueued before the first finishes. Outputs, nimp
    entries each (any may be NULL): lattice atoms removed (sputtered) and ions
-   removed (backscattered) so far, and the simulated time, after each impact.
+   removed (backscattered) so far, the simulated time, and the MD steps this
+   call has run, after each impact.
    Needs lists built and the graph step loop (fibmd_gpu_set_option "graph"). */
 int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double* x,
                    const double* v, long long steps, double relax_s, int* removed_after,
-                   int* ions_removed_after, double* time_after);
+                   int* ions_removed_after, double* time_after, long long* steps_after);
 
 /* ---- batched ensemble (spec mode) -----------------------------------------
    Independent impacts advanced together: each replica has its own box,

@@ -35,7 +35,8 @@ def test_dose_matches_host_driven_impacts(gpu_lib):
     d = _dose_slab(3)
     steps = 60
     g = _ctx(d)
-    rm, ir, t = g.dose(d.ion_atoms[:2], d.X0[:2], d.V0[:2], steps)
+    rm, ir, t, st = g.dose(d.ion_atoms[:2], d.X0[:2], d.V0[:2], steps)
+    assert list(st) == [steps, 2 * steps]
     Xd, Vd, _ = g.download()
     g.close()
 
@@ -67,7 +68,8 @@ def test_dose_relaxation_and_records(gpu_lib):
     d = _dose_slab(2)
     g = _ctx(d)
     relax = 20e-15
-    rm, ir, t = g.dose(d.ion_atoms, d.X0, d.V0, 40, relax)
+    rm, ir, t, st = g.dose(d.ion_atoms, d.X0, d.V0, 40, relax)
+    assert st[0] > 40 and st[1] - st[0] > 40
     g.close()
     assert np.all(np.diff(t) > relax) and t[0] > relax
     assert np.all(np.diff(rm) >= 0) and np.all(rm >= 0) and np.all(ir >= 0)
