@@ -10,11 +10,12 @@ from ._abi import (MODE_REF, MODE_SPEC, PREC_FP64, PREC_MIXED, STOP_DONE, STOP_D
                    Siga)
 from .md import (DoseSlab, FibMD, FibMDBatch, FibmdError, Ran1, SpecSlab, System, crystal_system,
                  crater_depth, dose_slab, knock,
-                 impact_statistics, params_default, pureepi, read_siga, spec_slab)
+                 impact_statistics, params_default, pureepi, read_restart, read_siga, spec_slab,
+                 write_restart, XyzWriter)
 
 __all__ = [
     "FibMD", "FibMDBatch", "FibmdError", "Params", "Siga", "Ran1", "SpecSlab", "System",
-    "crater_depth", "crystal_system", "DoseSlab", "dose_slab", "impact_statistics", "knock", "spec_slab",
+    "XyzWriter", "read_restart", "write_restart", "crater_depth", "crystal_system", "DoseSlab", "dose_slab", "impact_statistics", "knock", "spec_slab",
     "params_default", "pureepi", "read_siga", "MODE_REF", "MODE_SPEC", "PREC_FP64",
     "PREC_MIXED", "TAG_FROZEN", "TAG_THERMO", "TAG_REMOVED", "STOP_MAXSTEPS", "STOP_DUMP",
     "STOP_DONE", "STOP_REGIME",

@@ -119,6 +119,13 @@ SIGNATURES = {
     "fibmd_gpu_phase_times": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),
     "fibmd_gpu_force_noalloc": (_I, [C.POINTER(Params), _VP, _VP, _I, _VP, _VP]),
+    "fibmd_gpu_xyz_frame": (_I, [_VP, _DP, _DP]),
+    "fibmd_host_xyz_open": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_VP)]),
+    "fibmd_host_xyz_write": (_I, [_VP, _I, _D, _DP, _IP, _DP, _IP]),
+    "fibmd_host_xyz_flush": (_I, [_VP]),
+    "fibmd_host_xyz_close": (_I, [_VP]),
+    "fibmd_host_write_restart": (_I, [C.c_char_p, _I, _I, _D, _DP, _DP, _DP, _IP, _I]),
+    "fibmd_host_read_restart": (_I, [C.c_char_p, _I, _IP, _DP, _DP, _DP, _DP, _IP, _IP]),
     "fibmd_gpu_dose": (_I, [_VP, _I, _IP, _DP, _DP, C.c_longlong, _D, _IP, _IP, _DP, _LLP]),
     "fibmd_gpu_batch_create": (_I, [C.POINTER(Params), _I, C.POINTER(Replica), C.POINTER(_VP)]),
     "fibmd_gpu_batch_layout": (_I, [_VP, _IP, _IP]),

@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
             if verbose and log.strip():
                 print(log, file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc, ARCH, "-shared", "-o", str(tmp), *map(str, objs)]
+    cmd = [nvcc, ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

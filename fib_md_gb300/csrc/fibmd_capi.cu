@@ -55,6 +55,7 @@ struct fibmd_ctx {
   DevState S;
   DevScalars* h_sc = nullptr;  // pinned mirror
   double* d_stage = nullptr;   // 3N doubles
+  double* d_ke = nullptr;      // N doubles (xyz frames)
   unsigned long long* d_u64 = nullptr;
   std::vector<void*> allocs;
   std::vector<double> tab, tabu;
@@ -655,6 +656,7 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   S.geo = geo;
   S.ion_list = ion_list;
   AL(ctx->d_stage, 3 * N);
+  AL(ctx->d_ke, N);
   AL(ctx->d_u64, 4);
   AL(ctx->d_loop, 1);
   cudaMemsetAsync(ctx->d_loop, 0, sizeof(LoopCtl), ctx->stream);
@@ -909,6 +911,21 @@ int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F) {
     CK(launch_unpack(L, N, srcv[k], ctx->d_stage));
     CK(cudaMemcpyAsync(dstv[k], ctx->d_stage, b3, cudaMemcpyDeviceToHost, ctx->stream));
   }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
+}
+
+int fibmd_gpu_xyz_frame(fibmd_ctx* ctx, double* xyz_A, double* ke_eV) {
+  if (!ctx) return FIBMD_EINVAL;
+  if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "xyz frame before upload");
+  const int N = ctx->P.N;
+  CK(launch_xyz_frame(launch_of(ctx), ctx->S, N, ctx->d_stage, ctx->d_ke));
+  if (xyz_A)
+    CK(cudaMemcpyAsync(xyz_A, ctx->d_stage, sizeof(double) * 3 * (size_t)N,
+                       cudaMemcpyDeviceToHost, ctx->stream));
+  if (ke_eV)
+    CK(cudaMemcpyAsync(ke_eV, ctx->d_ke, sizeof(double) * (size_t)N, cudaMemcpyDeviceToHost,
+                       ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return FIBMD_OK;
 }

@@ -575,4 +575,25 @@ cudaError_t launch_dose_record(const Launch& L, const DevState& S, const LoopCtl
   return cudaGetLastError();
 }
 
+// ---- writeatoms' columns, packed on the device ----------------------------------
+// x y z in Angstrom ((N,3) column-major) and 0.5 m |v|^2 in eV with the
+// reference's factor and operation order (src/out.f90:82-90).
+__global__ void k_xyz_frame(int N, const double4_32a* __restrict__ pos,
+                            const double4_32a* __restrict__ vel, const double* __restrict__ mass,
+                            double* xyz, double* ke) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const double4_32a x = pos[i], v = vel[i];
+  xyz[i] = x.x * 1e10;
+  xyz[(size_t)N + i] = x.y * 1e10;
+  xyz[2 * (size_t)N + i] = x.z * 1e10;
+  const double coef = 6.252e18;  // J -> eV as the reference writes it
+  ke[i] = 0.5 * mass[i] * (v.x * v.x + v.y * v.y + v.z * v.z) * coef;
+}
+
+cudaError_t launch_xyz_frame(const Launch& L, const DevState& S, int N, double* xyz, double* ke) {
+  k_xyz_frame<<<(N + 255) / 256, 256, 0, L.stream>>>(N, S.pos, S.vel, S.mass, xyz, ke);
+  return cudaGetLastError();
+}
+
 }  // namespace fibmd

@@ -431,6 +431,8 @@ cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
 // dose: bring impact k's ion into the run; record the counts after it
 cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S,
                           const Impact* table, int k);
+// writeatoms' columns: x y z (Angstrom, (N,3) column-major) and KE (eV)
+cudaError_t launch_xyz_frame(const Launch& L, const DevState& S, int N, double* xyz, double* ke);
 cudaError_t launch_dose_record(const Launch& L, const DevState& S, const LoopCtl* loop, int k,
                                int* removed, int* ions_removed, double* time, long long* steps);
 

@@ -451,6 +451,14 @@ class FibMD:
                                             st.ctypes.data_as(C.POINTER(C.c_longlong))), "dose")
         return rm, ir, t, st
 
+    def xyz_frame(self):
+        """writeatoms' columns computed on the device: positions in Angstrom
+        (N, 3) and kinetic energies in eV (N)."""
+        xyz = np.zeros((self.N, 3), order="F")
+        ke = np.zeros(self.N)
+        self._check(self.lib.fibmd_gpu_xyz_frame(self.h, _dp(xyz), _dp(ke)), "xyz_frame")
+        return xyz, ke
+
     def temperature(self) -> float:
         T = C.c_double()
         self._check(self.lib.fibmd_gpu_temperature(self.h, C.byref(T)), "temperature")
@@ -544,3 +552,75 @@ class FibMDBatch(FibMD):
         self._check(self.lib.fibmd_gpu_batch_scalars(self.h, _dp(t), _dp(dt), _ip(rm)),
                     "batch_scalars")
         return t, dt, rm
+
+
+class XyzWriter:
+    """writeatoms' dump files (fibmd_host_xyz_*): frames appended to `path`
+    in the reference's extended-xyz layout and, if given, the snapshot file
+    rewritten with each frame, both written by a background thread."""
+
+    def __init__(self, path, snap_path=None):
+        self.lib = _abi.load()
+        h = C.c_void_p()
+        rc = self.lib.fibmd_host_xyz_open(str(path).encode(),
+                                          None if snap_path is None else str(snap_path).encode(),
+                                          C.byref(h))
+        if rc:
+            raise FibmdError(rc, f"cannot open {path}")
+        self.h = h
+
+    def write(self, time_s, xyz_A, atype, ke_eV, proc=None):
+        xyz = _fortran(xyz_A)
+        t = np.ascontiguousarray(atype, dtype=np.int32)
+        ke = np.ascontiguousarray(ke_eV, dtype=np.float64)
+        pr = None if proc is None else np.ascontiguousarray(proc, dtype=np.int32)
+        rc = self.lib.fibmd_host_xyz_write(self.h, len(t), float(time_s), _dp(xyz), _ip(t),
+                                           _dp(ke), None if pr is None else _ip(pr))
+        if rc:
+            raise FibmdError(rc, "xyz write")
+
+    def flush(self):
+        rc = self.lib.fibmd_host_xyz_flush(self.h)
+        if rc:
+            raise FibmdError(rc, "xyz flush")
+
+    def close(self):
+        if getattr(self, "h", None):
+            rc = self.lib.fibmd_host_xyz_close(self.h)
+            self.h = None
+            if rc:
+                raise FibmdError(rc, "xyz close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def write_restart(path, lt: int, restart_time: float, X, V, mass, atype, impact: int):
+    """writerestart (src/out.f90:34-58): Fortran unformatted records."""
+    X, V = _fortran(X), _fortran(V)
+    m = np.ascontiguousarray(mass, dtype=np.float64)
+    t = np.ascontiguousarray(atype, dtype=np.int32)
+    rc = _abi.load().fibmd_host_write_restart(str(path).encode(), len(m), int(lt),
+                                              float(restart_time), _dp(X), _dp(V), _dp(m),
+                                              _ip(t), int(impact))
+    if rc:
+        raise FibmdError(rc, f"write_restart {path}")
+
+
+def read_restart(path, natm: int):
+    """The records of write_restart: (lt, restart_time, X, V, mass, atype, impact)."""
+    X = np.zeros((natm, 3), order="F")
+    V = np.zeros((natm, 3), order="F")
+    m = np.zeros(natm)
+    t = np.zeros(natm, dtype=np.int32)
+    lt, imp = C.c_int(), C.c_int()
+    rt = C.c_double()
+    rc = _abi.load().fibmd_host_read_restart(str(path).encode(), natm, C.byref(lt), C.byref(rt),
+                                             _dp(X), _dp(V), _dp(m), _ip(t), C.byref(imp))
+    if rc:
+        raise FibmdError(rc, f"read_restart {path}")
+    return lt.value, rt.value, X, V, m, t, imp.value
+

@@ -183,6 +183,14 @@ int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F);
 /* Spec-mode per-atom tags (FIBMD_TAG_* bits), (Natm) entries. */
 int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags);
 
+/* The device side of writeatoms (src/out.f90:62-100): the columns of an
+   extended-xyz frame computed on the GPU — x y z in Angstrom ((Natm,3)
+   column-major) and the kinetic energy 0.5 m |v|^2 in eV (the reference's
+   J->eV factor 6.252e18) — copied into host arrays (either may be NULL).
+   fibmd_host_xyz_write (fibmd_host.h) then writes the frame on a background
+   thread. */
+int fibmd_gpu_xyz_frame(fibmd_ctx* ctx, double* xyz_A, double* ke_eV);
+
 /* Overwrite one atom's position and velocity (1-based index). This is the
    device side of knock (src/knock.f90:21-55): the host draws the ion's start
    point and velocity and sends them here. */

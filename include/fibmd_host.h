@@ -3,9 +3,9 @@
  * libfibmd_gpu.so next to the GPU entry points.
  *
  * In a Fortran build these routines stay the reference's own (prms.f90,
- * data.f90, knock.f90, ran1.f); this C++ restatement lets the C++ driver
- * (mdrun2_gpu) and the Python package run the same set-up without a Fortran
- * compiler. None of it is on the per-step path.
+ * data.f90, knock.f90, ran1.f, out.f90); this C++ restatement lets C/C++
+ * hosts and the Python package run the same set-up and write the same dump
+ * files without a Fortran compiler. None of it is on the per-step path.
  */
 #ifndef FIBMD_HOST_H
 #define FIBMD_HOST_H
@@ -71,6 +71,38 @@ int fibmd_host_init_state(const fibmd_params* p, fibmd_rng* r, double Uo, double
    index 0 is taken as 1. Returns the 1-based atom index (Nsg + knc). */
 int fibmd_host_knock(const fibmd_params* p, fibmd_rng* r, int knc, double eV, double phiz,
                      double phixy, const double* Xrand, int Nrand, double x[3], double v[3]);
+
+/* ---- dump files (src/out.f90) ---------------------------------------------
+   writeatoms (src/out.f90:62-100): frames appended to an extended-xyz file
+   (data/mdrun2.xyz in the reference) in its fixed-width layout — the atom
+   count (I9); "Time (ps) = " and the time with the column titles; per atom
+   x y z in Angstrom (3F12.4), the species (A8), the owning process (I8, 0
+   here) and the kinetic energy in eV (ES14.3) — and, if snap_path is given,
+   the snapshot file (data/3dmol2.xyz) rewritten with each frame. A
+   background thread formats and writes queued frames, so a host can queue
+   a frame (fibmd_gpu_xyz_frame fills its arrays) and step on. Type 2 is
+   written "Ge" (the reference leaves that name unset). */
+typedef struct fibmd_xyz_writer fibmd_xyz_writer;
+int fibmd_host_xyz_open(const char* path, const char* snap_path, fibmd_xyz_writer** out);
+/* Queue one frame; the arrays are copied (xyz_A: (natm,3) column-major;
+   proc may be NULL). */
+int fibmd_host_xyz_write(fibmd_xyz_writer* w, int natm, double time_s, const double* xyz_A,
+                         const int* atype, const double* ke_eV, const int* proc);
+/* Wait until every queued frame is written. */
+int fibmd_host_xyz_flush(fibmd_xyz_writer* w);
+/* Flush, stop the writer thread and close the file. */
+int fibmd_host_xyz_close(fibmd_xyz_writer* w);
+
+/* writerestart (src/out.f90:34-58) and its reader: Fortran unformatted
+   sequential records with gfortran's 4-byte length markers — (lt,
+   restart_time), (X, V, mass, atype), (impact); X, V: (natm,3) column-major
+   binary64, atype 4-byte integers. The reader checks every marker against
+   natm and fails on a mismatch. */
+int fibmd_host_write_restart(const char* path, int natm, int lt, double restart_time,
+                             const double* X, const double* V, const double* mass,
+                             const int* atype, int impact);
+int fibmd_host_read_restart(const char* path, int natm, int* lt, double* restart_time, double* X,
+                            double* V, double* mass, int* atype, int* impact);
 
 #ifdef __cplusplus
 }
