@@ -244,7 +244,7 @@ __device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, 
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kBuildThreads, 8) k_build_atoms(DevParams P, DevState S,
+__global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, DevState S,
                                                                    int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   __shared__ int buf[kBuildBuf][kBuildThreads];
