@@ -61,6 +61,7 @@ constexpr int kLegF64 = 9;   // ux uy uz rinv E g fx fy fz
 constexpr int kBlock64 = 64;
 constexpr int kLegF32 = 6;   // ux uy uz rinv E g
 constexpr int kBlock32 = 128;
+constexpr int kCandF64 = 16;  // prefiltered neighbours staged per centre (binary64 kernel)
 constexpr int kLegs32 = 8;   // staged candidates per centre (binary32 kernel);
                              // a crystal at 300 K has 4 legs, rarely more than 6
 
@@ -80,6 +81,7 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
   LegSmem<double, kBlock64, kLegF64> leg;
   leg.v = reinterpret_cast<double*>(smem_raw);
   leg.j = reinterpret_cast<int*>(smem_raw + sizeof(double) * kMaxLegs * kLegF64 * kBlock64);
+  int* cand = leg.j + kMaxLegs * kBlock64;  // [kCandF64][kBlock64]
 
   const int i = blockIdx.x * kBlock64 + threadIdx.x;
   if (i >= P.N) return;
@@ -98,6 +100,53 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
   int nl = 0, terr = 0;
   unsigned int cnt_pairs = 0, cnt_ang = 0;
 
+  // One listed neighbour inside the prefilter: the table 2-body force on the
+  // centre and, inside 0.999*a*sigma, its staged leg.
+  auto neighbour = [&](int j, int tb) {
+    const double4_32a pj = S.pos[j];
+    const double dx = min_image(pi.x, pj.x, iLb[0], Lb[0]);
+    const double dy = min_image(pi.y, pj.y, iLb[1], Lb[1]);
+    const double dz = min_image(pi.z, pj.z, iLb[2], Lb[2]);
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    const double r = sqrt(r2);
+    const double rinv = 1.0 / r;
+    const double isig = P.isig[ta][tb];
+    const double ue = r * isig;
+    const double df = table_df(P, S.tab, S.tabu, ue, &terr);
+    if (df != 0.0) {
+      const double c = -(df * rinv * P.epssig[ta][tb]);
+      fx += c * dx;
+      fy += c * dy;
+      fz += c * dz;
+      if (COUNT) cnt_pairs++;
+    }
+    if (ue < P.cut3) {
+      const double inv = 1.0 / (ue - P.al);
+      if (ENERGY)
+        ui += 0.5 * P.eps[ta][tb] * P.A * (P.B * pow(ue, -P.psi) - pow(ue, -P.qsi)) * exp(inv);
+      if (nl < kMaxLegs) {
+        leg.at(nl, 0) = dx * rinv;
+        leg.at(nl, 1) = dy * rinv;
+        leg.at(nl, 2) = dz * rinv;
+        leg.at(nl, 3) = rinv;
+        leg.at(nl, 4) = exp(P.gam * inv);
+        leg.at(nl, 5) = -P.gam * inv * inv * isig;
+        leg.at(nl, 6) = 0.0;
+        leg.at(nl, 7) = 0.0;
+        leg.at(nl, 8) = 0.0;
+        leg.idx(nl) = j | (tb << 30);
+      }
+      nl++;
+    }
+  };
+
+  // Phase 1: gather the listed neighbours and keep (in list order) the few
+  // inside the prefilter; phase 2 runs the binary64 work on that compacted
+  // set, so the lanes of a warp issue it together (binary64 instructions are
+  // the scarce resource, and a warp instruction costs the pipe the same
+  // whether 8 or 32 lanes take part). Candidates beyond the slots are
+  // evaluated at once.
+  int nc = 0;
   for (int k0 = 0; k0 < n; k0 += kBatch) {
     int jj[kBatch];
     int4 qq[kBatch];
@@ -108,47 +157,18 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
 #pragma unroll
     for (int u = 0; u < kBatch; u++) {
       if (k0 + u >= n) break;
-      const int j = jj[u];
       const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
       if (r2f > P.pre3A2) continue;  // beyond the table support and 3-body cutoff
       const int tb = (qq[u].w & 0xff) - 1;
-      const double4_32a pj = S.pos[j];
-      const double dx = min_image(pi.x, pj.x, iLb[0], Lb[0]);
-      const double dy = min_image(pi.y, pj.y, iLb[1], Lb[1]);
-      const double dz = min_image(pi.z, pj.z, iLb[2], Lb[2]);
-      const double r2 = dx * dx + dy * dy + dz * dz;
-      const double r = sqrt(r2);
-      const double rinv = 1.0 / r;
-      const double isig = P.isig[ta][tb];
-      const double ue = r * isig;
-      const double df = table_df(P, S.tab, S.tabu, ue, &terr);
-      if (df != 0.0) {
-        const double c = -(df * rinv * P.epssig[ta][tb]);
-        fx += c * dx;
-        fy += c * dy;
-        fz += c * dz;
-        if (COUNT) cnt_pairs++;
-      }
-      if (ue < P.cut3) {
-        const double inv = 1.0 / (ue - P.al);
-        if (ENERGY)
-          ui += 0.5 * P.eps[ta][tb] * P.A * (P.B * pow(ue, -P.psi) - pow(ue, -P.qsi)) * exp(inv);
-        if (nl < kMaxLegs) {
-          leg.at(nl, 0) = dx * rinv;
-          leg.at(nl, 1) = dy * rinv;
-          leg.at(nl, 2) = dz * rinv;
-          leg.at(nl, 3) = rinv;
-          leg.at(nl, 4) = exp(P.gam * inv);
-          leg.at(nl, 5) = -P.gam * inv * inv * isig;
-          leg.at(nl, 6) = 0.0;
-          leg.at(nl, 7) = 0.0;
-          leg.at(nl, 8) = 0.0;
-          leg.idx(nl) = j | (tb << 30);
-        }
-        nl++;
-      }
+      if (nc < kCandF64) cand[nc++ * kBlock64 + threadIdx.x] = jj[u] | (tb << 30);
+      else neighbour(jj[u], tb);
     }
+  }
+  // Phase 2
+  for (int c = 0; c < nc; c++) {
+    const int e = cand[c * kBlock64 + threadIdx.x];
+    neighbour(e & 0x3fffffff, (unsigned)e >> 30);
   }
 
   if (nl > kMaxLegs) {
@@ -745,7 +765,8 @@ template <bool MIXED, bool ENERGY, bool COUNT>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
   constexpr int BLOCK = MIXED ? kBlock32 : kBlock64;
   const size_t smem = MIXED ? (sizeof(float) * kLegs32 * kLegF32 + sizeof(int) * kLegs32) * BLOCK
-                            : (sizeof(double) * kMaxLegs * kLegF64 + sizeof(int) * kMaxLegs) * BLOCK;
+                            : (sizeof(double) * kMaxLegs * kLegF64 +
+                               sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
   auto kern = MIXED ? k_force_mixed<ENERGY, COUNT> : k_force_fp64<ENERGY, COUNT>;
   static bool attr_set = false;
   if (!attr_set) {
