@@ -25,6 +25,7 @@
 // Centres with more than kMaxLegs active legs are deferred to a direct
 // binary64 kernel.
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "fibmd_internal.cuh"
@@ -768,10 +769,17 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
                             : (sizeof(double) * kMaxLegs * kLegF64 +
                                sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
   auto kern = MIXED ? k_force_mixed<ENERGY, COUNT> : k_force_fp64<ENERGY, COUNT>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    attr_set = true;
+  // the dynamic shared-memory limit is a per-device attribute of the kernel:
+  // set it once on each device that launches it
+  static std::atomic<unsigned long long> attr_devices{0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const unsigned long long bit = 1ull << (dev & 63);
+  if (!(attr_devices.load() & bit)) {
+    const cudaError_t ea =
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (ea != cudaSuccess) return ea;
+    attr_devices.fetch_or(bit);
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
   kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(P, S);
