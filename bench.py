@@ -519,11 +519,10 @@ def run_ensemble_batch(slabs, precision, steps):
     t_sim, _, removed = b.scalars()
     wall = time.perf_counter() - w0
     rebuilds = b.work_counters()[4] - rb0
-    stats = []
-    for r, s in enumerate(slabs):
-        rows = b.rows(r)
-        stats.append(fm.impact_statistics(Xf[rows], s.Xi, s.atype, list(s.params.Lb),
-                                          s.surface_z, s.params.remove_z))
+    # each impact's outcome, computed on the device (the same quantities as
+    # impact_statistics on the downloaded states)
+    sp, dc, dp = b.impact_stats([s.surface_z for s in slabs])
+    stats = [(int(sp[r]), float(dp[r]), int(dc[r])) for r in range(len(slabs))]
     atoms = int(b.natm.sum())
     b.close()
     return {"wall_s": wall, "atoms": atoms, "padded_atoms": int(b.N), "rebuilds": int(rebuilds),

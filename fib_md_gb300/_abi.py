@@ -129,6 +129,7 @@ SIGNATURES = {
     "fibmd_gpu_dose": (_I, [_VP, _I, _IP, _DP, _DP, C.c_longlong, _D, _IP, _IP, _DP, _LLP]),
     "fibmd_gpu_batch_create": (_I, [C.POINTER(Params), _I, C.POINTER(Replica), C.POINTER(_VP)]),
     "fibmd_gpu_batch_layout": (_I, [_VP, _IP, _IP]),
+    "fibmd_gpu_impact_stats": (_I, [_VP, _DP, _D, _IP, _IP, _DP]),
     "fibmd_gpu_batch_scalars": (_I, [_VP, _DP, _DP, _IP]),
     # fibmd_host.h
     "fibmd_host_rng_seed": (None, [C.POINTER(Rng), _I]),

@@ -771,6 +771,50 @@ int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica*
   return finish_create(ctx, ions, out);
 }
 
+int fibmd_gpu_impact_stats(fibmd_ctx* ctx, const double* surface_z, double displaced_m,
+                           int* sputtered, int* displaced, double* ion_depth) {
+  if (!ctx || !surface_z || !(displaced_m > 0.0)) return FIBMD_EINVAL;
+  if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "impact stats before upload");
+  const int R = ctx->P.nrep;
+  double* d_sz = nullptr;
+  int* d_cnt = nullptr;
+  double* d_depth = nullptr;
+  if (cudaMalloc((void**)&d_sz, sizeof(double) * R) != cudaSuccess ||
+      cudaMalloc((void**)&d_cnt, sizeof(int) * R) != cudaSuccess ||
+      cudaMalloc((void**)&d_depth, sizeof(double) * R) != cudaSuccess) {
+    cudaFree(d_sz);
+    cudaFree(d_cnt);
+    cudaFree(d_depth);
+    return fail(ctx, FIBMD_ENOMEM, "impact stats: %d replicas", R);
+  }
+  std::vector<int> cnt((size_t)R);
+  std::vector<double> depth((size_t)R);
+  std::vector<DevScalars> h((size_t)R);
+  cudaError_t e = cudaMemcpyAsync(d_sz, surface_z, sizeof(double) * R, cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e == cudaSuccess)
+    e = launch_impact_stats(launch_of(ctx), ctx->P, ctx->S, d_sz, displaced_m, d_cnt, d_depth);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * R, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(depth.data(), d_depth, sizeof(double) * R, cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(h.data(), ctx->S.sc, sizeof(DevScalars) * R, cudaMemcpyDeviceToHost,
+                        ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  cudaFree(d_sz);
+  cudaFree(d_cnt);
+  cudaFree(d_depth);
+  if (e != cudaSuccess) return fail(ctx, FIBMD_ECUDA, "impact stats: %s", cudaGetErrorString(e));
+  for (int r = 0; r < R; r++) {
+    if (sputtered) sputtered[r] = h[(size_t)r].removed_count;
+    if (displaced) displaced[r] = cnt[(size_t)r];
+    if (ion_depth) ion_depth[r] = depth[(size_t)r];
+  }
+  return FIBMD_OK;
+}
+
 int fibmd_gpu_batch_layout(fibmd_ctx* ctx, int* nrep, int* offsets) {
   if (!ctx) return FIBMD_EINVAL;
   const int R = (int)ctx->geo.size();

@@ -596,4 +596,55 @@ cudaError_t launch_xyz_frame(const Launch& L, const DevState& S, int N, double* 
   return cudaGetLastError();
 }
 
+// ---- outcome of each impact, one block per replica -----------------------------
+// Lattice atoms farther than `thr` from their initial site (minimum image in
+// x and y, removed atoms left out), and the depth of the replica's first ion
+// below its surface height (NaN when the ion is above it or removed).
+__global__ void __launch_bounds__(256) k_impact_stats(DevState S, const double* surface_z,
+                                                      double thr2, int* displaced,
+                                                      double* ion_depth) {
+  const int r = blockIdx.x;
+  const Geo& G = S.geo[r];
+  int cnt = 0;
+  int ion = 0x7fffffff;
+  for (int i = G.atom_begin + threadIdx.x; i < G.atom_end; i += blockDim.x) {
+    const uint32_t fl = S.flags[i];
+    if (fl & FL_REMOVED) continue;
+    if (S.atype[i] == 3) {
+      ion = min(ion, i);
+      continue;
+    }
+    const double4_32a x = S.pos[i], x0 = S.xi[i];
+    double dx = x.x - x0.x, dy = x.y - x0.y;
+    dx -= G.Lb[0] * rint(dx * G.iLb[0]);
+    dy -= G.Lb[1] * rint(dy * G.iLb[1]);
+    const double dz = x.z - x0.z;
+    if (dx * dx + dy * dy + dz * dz > thr2) cnt++;
+  }
+  __shared__ int s_cnt, s_ion;
+  if (threadIdx.x == 0) {
+    s_cnt = 0;
+    s_ion = 0x7fffffff;
+  }
+  __syncthreads();
+  if (cnt) atomicAdd(&s_cnt, cnt);
+  if (ion != 0x7fffffff) atomicMin(&s_ion, ion);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  displaced[r] = s_cnt;
+  double depth = nan("");
+  if (s_ion != 0x7fffffff) {
+    const double z = S.pos[s_ion].z;
+    if (z <= surface_z[r]) depth = surface_z[r] - z;
+  }
+  ion_depth[r] = depth;
+}
+
+cudaError_t launch_impact_stats(const Launch& L, const DevParams& P, const DevState& S,
+                                const double* surface_z, double thr, int* displaced,
+                                double* ion_depth) {
+  k_impact_stats<<<P.nrep, 256, 0, L.stream>>>(S, surface_z, thr * thr, displaced, ion_depth);
+  return cudaGetLastError();
+}
+
 }  // namespace fibmd

@@ -431,6 +431,10 @@ cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
 // dose: bring impact k's ion into the run; record the counts after it
 cudaError_t launch_inject(const Launch& L, const DevParams& P, const DevState& S,
                           const Impact* table, int k);
+// per replica: displaced lattice atoms and the first ion's depth
+cudaError_t launch_impact_stats(const Launch& L, const DevParams& P, const DevState& S,
+                                const double* surface_z, double thr, int* displaced,
+                                double* ion_depth);
 // writeatoms' columns: x y z (Angstrom, (N,3) column-major) and KE (eV)
 cudaError_t launch_xyz_frame(const Launch& L, const DevState& S, int N, double* xyz, double* ke);
 cudaError_t launch_dose_record(const Launch& L, const DevState& S, const LoopCtl* loop, int k,

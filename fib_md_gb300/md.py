@@ -451,6 +451,18 @@ class FibMD:
                                             st.ctypes.data_as(C.POINTER(C.c_longlong))), "dose")
         return rm, ir, t, st
 
+    def impact_stats(self, surface_z, displaced_m: float = 1.0e-10):
+        """Per replica (sputtered atoms, displaced lattice atoms, ion depth in
+        m or nan), computed on the device (fibmd_gpu_impact_stats)."""
+        sz = np.ascontiguousarray(np.atleast_1d(surface_z), dtype=np.float64)
+        R = len(sz)
+        sp = np.zeros(R, dtype=np.int32)
+        dc = np.zeros(R, dtype=np.int32)
+        dp = np.zeros(R)
+        self._check(self.lib.fibmd_gpu_impact_stats(self.h, _dp(sz), float(displaced_m), _ip(sp),
+                                                    _ip(dc), _dp(dp)), "impact_stats")
+        return sp, dc, dp
+
     def xyz_frame(self):
         """writeatoms' columns computed on the device: positions in Angstrom
         (N, 3) and kinetic energies in eV (N)."""

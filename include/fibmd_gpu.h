@@ -364,6 +364,16 @@ typedef struct fibmd_replica {
    start time of every replica and returns replica 0's. */
 int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica* reps,
                            fibmd_ctx** out);
+/* The outcome of each impact (a batch's replicas, or a single system as one
+   replica), computed on the device, after the statistics of temp.f90:70-127
+   that the reference writes per impact: lattice atoms removed (sputtered),
+   lattice atoms farther than displaced_m from their initial site (minimum
+   image in x and y; removed atoms left out), and the depth of the replica's
+   first ion below surface_z[r] (m; NaN when the ion is above it or
+   removed). surface_z and the outputs have one entry per replica; any
+   output may be NULL. */
+int fibmd_gpu_impact_stats(fibmd_ctx* ctx, const double* surface_z, double displaced_m,
+                           int* sputtered, int* displaced, double* ion_depth);
 /* Replica count and, if offsets is not NULL, the first atom of each replica
    in offsets[0..nrep-1] and the padded atom count in offsets[nrep]. */
 int fibmd_gpu_batch_layout(fibmd_ctx* ctx, int* nrep, int* offsets);

@@ -92,3 +92,20 @@ def test_batch_layout(gpu_lib):
     assert b.nrep == 3 and np.all(b.offsets[:-1] % 256 == 0)
     assert np.all(np.diff(b.offsets)[:3] >= b.natm)
     b.close()
+
+
+def test_impact_stats_on_device(gpu_lib):
+    """fibmd_gpu_impact_stats against impact_statistics on the downloaded
+    final states of a batch after its cascades."""
+    import fib_md_gb300 as fm
+
+    slabs = _slabs(1)
+    b, Xb, Vb, tb, X0 = _batch(slabs, 300)
+    sp, dc, dp = b.impact_stats([s.surface_z for s in slabs])
+    for r, s in enumerate(slabs):
+        hs, hd, hdisp = fm.impact_statistics(Xb[b.rows(r)], s.Xi, s.atype, list(s.params.Lb),
+                                             s.surface_z, s.params.remove_z)
+        assert sp[r] == hs and dc[r] == hdisp, (r, sp[r], hs, dc[r], hdisp)
+        assert (np.isnan(dp[r]) and np.isnan(hd)) or abs(dp[r] - hd) <= 1e-20
+    assert dc.sum() > 0
+    b.close()
