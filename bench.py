@@ -203,6 +203,21 @@ def flops_per_force(counts):
     return 40 * pairs + 100 * angles + 60 * mol + 100 * stale
 
 
+def replica_rate(dist, units, seconds, device):
+    """Whole-job rate of independent replicas (one per rank, no data-path
+    collective): the units all ranks processed over the slowest rank's
+    time. Returns (rate, slowest time, total units)."""
+    if dist is None:
+        return units / seconds, seconds, units
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(u.item()) / float(t.item()), float(t.item()), float(u.item())
+
+
 def bench_ours(args, rank, world, dist):
     import torch
 
@@ -236,13 +251,8 @@ def bench_ours(args, rank, world, dist):
         wall = time.perf_counter() - w0
     rebuilds = g.work_counters()[4] - rb0
     X_end, _, _ = g.download()
-    t_dev = sum(times)
-    if dist is not None:
-        tt = torch.tensor([t_dev], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_dev = float(tt.item())
-    atom_steps = float(N) * args.md_steps * args.steps * world
-    value = atom_steps / t_dev
+    value, t_dev, atom_steps = replica_rate(dist, float(N) * args.md_steps * args.steps,
+                                            sum(times), "cuda")
     # the main force kernel, timed live with CUDA events on the library's
     # stream over a segment run launch by launch (events cannot sit inside
     # the graph's conditional bodies)
@@ -287,11 +297,8 @@ def bench_ours(args, rank, world, dist):
             hX[:], hV[:], hF[:] = X, V, F
         barrier()
         t_e2e = time.perf_counter() - w0
-        if dist is not None:
-            tt = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            t_e2e = float(tt.item())
-        e2e = {"value": atom_steps / t_e2e, "unit": "atom-steps/s",
+        e2e_value, _, _ = replica_rate(dist, float(N) * args.md_steps * args.steps, t_e2e, "cuda")
+        e2e = {"value": e2e_value, "unit": "atom-steps/s",
                "h2d_bytes_per_step": N * (4 * 24 + 8 + 4 + 4),
                "d2h_bytes_per_step": N * 3 * 24}
     g.close()
@@ -313,12 +320,7 @@ def bench_ours(args, rank, world, dist):
     g64.si_force()
     c64 = g64.work_counters()
     g64.close()
-    t64_sum = sum(t64)
-    if dist is not None:
-        tt = torch.tensor([t64_sum], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t64_sum = float(tt.item())
-    value64 = float(N) * args.md_steps * n64 * world / t64_sum
+    value64, _, _ = replica_rate(dist, float(N) * args.md_steps * n64, sum(t64), "cuda")
     f64_avg = f64_total / max(f64_n, 1)
 
     # HBM view of the whole step: 150 algorithmic bytes per atom-step
