@@ -357,6 +357,7 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
   }
   // Phase 2: pair forces and legs of the staged candidates; active legs are
   // compacted in place (slot nl <= c is written after slot c is read).
+#pragma unroll 2
   for (int c = 0; c < nc; c++) {
     const float3 dq = make_float3(leg.at(c, 0), leg.at(c, 1), leg.at(c, 2));
     const float r2f = leg.at(c, 3);
@@ -393,6 +394,7 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
       const int ia = leg.idx(a);
       const int tbA = (unsigned)ia >> 30;
       float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+#pragma unroll 2
       for (int b = 0; b < nl; b++) {
         if (b == a) continue;
         const float bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
