@@ -272,9 +272,14 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
     return;
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  LegSmem<float, kBlock32, kLegF32> leg;
-  leg.v = reinterpret_cast<float*>(smem_raw);
-  leg.j = reinterpret_cast<int*>(smem_raw + sizeof(float) * kLegs32 * kLegF32 * kBlock32);
+  // per slot and thread: A = (dq, r^2) of a candidate, then (unit vector, E)
+  // of a leg; B = (1/r, g) of a leg; I = neighbour index | type << 30. Vector
+  // accesses keep the shared-memory instruction count low.
+  float4* sA = reinterpret_cast<float4*>(smem_raw);
+  float2* sB = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * kLegs32 * kBlock32);
+  int* sI = reinterpret_cast<int*>(smem_raw + (sizeof(float4) + sizeof(float2)) * kLegs32 *
+                                                  kBlock32);
+  const int t = threadIdx.x;
 
   const int i = blockIdx.x * kBlock32 + threadIdx.x;
   if (i >= P.N) return;
@@ -343,11 +348,8 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
       if (r2f > P.pre3mA2) continue;
       const int tb = (qq[u].w & 0xff) - 1;
       if (r2f <= P.pre3lA2 && nc < kLegs32) {
-        leg.at(nc, 0) = dq.x;
-        leg.at(nc, 1) = dq.y;
-        leg.at(nc, 2) = dq.z;
-        leg.at(nc, 3) = r2f;
-        leg.idx(nc) = jj[u] | (tb << 30);
+        sA[nc * kBlock32 + t] = make_float4(dq.x, dq.y, dq.z, r2f);
+        sI[nc * kBlock32 + t] = jj[u] | (tb << 30);
         nc++;
       } else {
         float rinv, E, g;
@@ -359,19 +361,16 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
   // compacted in place (slot nl <= c is written after slot c is read).
 #pragma unroll 2
   for (int c = 0; c < nc; c++) {
-    const float3 dq = make_float3(leg.at(c, 0), leg.at(c, 1), leg.at(c, 2));
-    const float r2f = leg.at(c, 3);
-    const int idx = leg.idx(c);
+    const float4 cd = sA[c * kBlock32 + t];
+    const float3 dq = make_float3(cd.x, cd.y, cd.z);
+    const float r2f = cd.w;
+    const int idx = sI[c * kBlock32 + t];
     float rinv, E, g;
     if (!pair_leg(dq, r2f, (unsigned)idx >> 30, &rinv, &E, &g)) continue;
     if (E > kLegEmin) {
-      leg.at(nl, 0) = dq.x * rinv;
-      leg.at(nl, 1) = dq.y * rinv;
-      leg.at(nl, 2) = dq.z * rinv;
-      leg.at(nl, 3) = rinv;
-      leg.at(nl, 4) = E;
-      leg.at(nl, 5) = g;
-      leg.idx(nl) = idx;
+      sA[nl * kBlock32 + t] = make_float4(dq.x * rinv, dq.y * rinv, dq.z * rinv, E);
+      sB[nl * kBlock32 + t] = make_float2(rinv, g);
+      sI[nl * kBlock32 + t] = idx;
       nl++;
     }
   }
@@ -389,20 +388,23 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
     const float thrd = (float)P.thrd;
     float cu = 0.f;
     for (int a = 0; a < nl; a++) {
-      const float ax = leg.at(a, 0), ay = leg.at(a, 1), az = leg.at(a, 2);
-      const float ar = leg.at(a, 3), aE = leg.at(a, 4), ag = leg.at(a, 5);
-      const int ia = leg.idx(a);
+      const float4 la = sA[a * kBlock32 + t];
+      const float2 lb = sB[a * kBlock32 + t];
+      const float ax = la.x, ay = la.y, az = la.z, aE = la.w;
+      const float ar = lb.x, ag = lb.y;
+      const int ia = sI[a * kBlock32 + t];
       const int tbA = (unsigned)ia >> 30;
       float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
 #pragma unroll 2
       for (int b = 0; b < nl; b++) {
         if (b == a) continue;
-        const float bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
-        const int tbB = (unsigned)leg.idx(b) >> 30;
+        const float4 lbb = sA[b * kBlock32 + t];
+        const float bx = lbb.x, by = lbb.y, bz = lbb.z;
+        const int tbB = (unsigned)sI[b * kBlock32 + t] >> 30;
         const float cs = ax * bx + ay * by + az * bz;
         const float c3 = cs + thrd;
         const float W = c3 * c3;
-        const float pref = P.lepsA[ta][tbA][tbB] * aE * leg.at(b, 4);
+        const float pref = P.lepsA[ta][tbA][tbB] * aE * lbb.w;
         const float s2 = 2.0f * c3;
         const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
         afx += pref * (wa * ax + sa * bx);
