@@ -66,9 +66,10 @@ def parse():
                     help="impacts of the cumulative-dose run (0: skip)")
     ap.add_argument("--dose-fp64-impacts", type=int, default=-1,
                     help="impacts of its binary64 counterpart (default: as many)")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "build"], default=None,
-                    help="set up the workload, evaluate the force 3 times (mixed, fp64) "
-                         "or rebuild the lists 5 times (build), exit (for ncu)")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step"], default=None,
+                    help="set up the workload, evaluate the force 3 times (mixed, fp64), "
+                         "rebuild the lists 5 times (build) or run 10 mixed steps launch "
+                         "by launch (step), exit (for ncu)")
     return ap.parse_args()
 
 
@@ -392,10 +393,13 @@ def bench_ours(args, rank, world, dist):
         "work_counters": {"sw_pairs": counts[0], "angle_terms": counts[1],
                           "moliere_pairs": counts[2], "stale_terms": counts[3],
                           "many_leg_centres": counts[5]},
-        # per MD step: drift, rebuild condition, force (begin, main, Moliere,
-        # many-leg), kick + finalize = 8; per step pair the loop control;
-        # 9 kernels per list rebuild; one temperature kernel per bench step
-        "gpu_launches": int(8.5 * args.md_steps * args.steps + 9 * rebuilds + args.steps),
+        # per MD step: drift, rebuild condition, force (main with the Moliere
+        # blocks, many-leg), kick, kick reduction = 6; per step pair the loop
+        # control; 9 kernels per list rebuild; the loop set-up per bench step.
+        # Launch by launch: the 9 list kernels every step (they return at once
+        # when no rebuild is due), no condition or loop kernels
+        "gpu_launches": int(14 * args.md_steps * args.steps if args.no_graph else
+                            6.5 * args.md_steps * args.steps + 9 * rebuilds + args.steps),
         "rebuild_fraction": rebuilds / float(args.md_steps * args.steps),
         "wall_s_timed": wall,
         "clocks": clk.summary(),
@@ -736,6 +740,12 @@ def main():
 
         w = make_workload(cells, list_skin_A=args.list_skin)
         g = make_ctx(w, fm.PREC_FP64 if args.profile == "fp64" else fm.PREC_MIXED)
+        if args.profile == "step":
+            # ten mixed spec-mode steps launch by launch (the integrator kernels)
+            g.set_option("graph", 0)
+            g.steps(2, 10, 0, 0.0, 300.0)
+            g.close()
+            return 0
         for _ in range(5 if args.profile == "build" else 3):
             if args.profile == "build":
                 g.si_nlist()

@@ -320,32 +320,40 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 }
 
 // ---- spec mode ----------------------------------------------------------------
+// Both spec-mode kernels issue every load of an atom before its first use, so
+// a thread waits for one memory round trip rather than a chain of them (the
+// flags, then the replica's scalars, then the state); removal only masks the
+// stores. BATCH = 0 (a single system) takes the replica's geometry and
+// scalars without reading the flags first.
+
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z, and the rebuild trigger at half the list skin.
-__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
-                                                    cudaGraphConditionalHandle cond,
-                                                    int use_cond) {
+template <int BATCH>
+__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool trig = false;
   if (i < P.N) {
     uint32_t fl = S.flags[i];
+    double4_32a x = S.pos[i];
+    double4_32a v = S.vel[i];
+    const double4_32a f = S.frc[i];
+    const double im = S.inv_mass[i];
+    const int8_t at = S.atype[i];
+    const int4 qb = S.posq_build[i];
+    const int r = BATCH ? rep_of_flags(fl) : 0;
+    const Geo& G = S.geo[r];
+    DevScalars* R = S.sc + r;
+    const double dt = R->dt;
+    const double h2 = R->half_dt2;
+    const double ts = R->thermo_s;
     if (!(fl & FL_REMOVED)) {
-      const int r = rep_of_flags(fl);
-      const Geo& G = S.geo[r];
-      DevScalars* R = S.sc + r;
-      const double dt = ((volatile DevScalars*)R)->dt;
-      const double h2 = ((volatile DevScalars*)R)->half_dt2;
-      double4_32a x = S.pos[i];
-      double4_32a v = S.vel[i];
       if (fl & FL_THERMO) {
-        const double s = R->thermo_s;
-        v.x *= s;
-        v.y *= s;
-        v.z *= s;
+        v.x *= ts;
+        v.y *= ts;
+        v.z *= ts;
       }
-      const double4_32a f = S.frc[i];
-      const double c = h2 * S.inv_mass[i];
+      const double c = h2 * im;
       x.x = x.x + v.x * dt + c * f.x;
       x.y = x.y + v.y * dt + c * f.y;
       x.z = x.z + v.z * dt + c * f.z;
@@ -379,14 +387,15 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
         S.flags[i] = fl;
         v.x = v.y = v.z = 0.0;
         trig = true;
-        atomicAdd(S.atype[i] < 3 ? &R->removed_count : &R->ions_removed, 1);
+        atomicAdd(at < 3 ? &R->removed_count : &R->ions_removed, 1);
       }
       S.pos[i] = x;
       S.vel[i] = v;
       const int4 q = make_int4((int)(unsigned)k[0], (int)(unsigned)k[1], (int)(unsigned)k[2],
-                               posq_w(S.atype[i], fl));
+                               posq_w(at, fl));
       S.posq[i] = q;
-      if (track_displacement(P, G, S, i, q) >= P.disp_fastA2) trig = true;
+      const float3 d = qsep(q, qb, G.qinvA);
+      if (d.x * d.x + d.y * d.y + d.z * d.z >= P.disp_fastA2) trig = true;
     }
   }
   const bool any = __syncthreads_or(trig);
@@ -398,47 +407,85 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S,
     S.sc->table_err = 0;
     for (int k = 0; k < 4; k++) S.sc->counters[k] = 0ull;
   }
-  if (use_cond) {
-    // the last block to finish sets the rebuild condition of the graph
-    __threadfence();
-    const unsigned t = atomicAdd(&S.sc->ticket[6], 1u);
-    if (t == gridDim.x - 1) {
-      __threadfence();
-      cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
-      S.sc->ticket[6] = 0u;
-    }
-  }
+}
+
+// Sets the graph's rebuild condition from the drift's flag. A kernel of its
+// own rather than a last-block ticket in the drift: a same-address atomic
+// from each of ~1000 blocks serialises in L2 for longer than a launch.
+__global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond) {
+  if (threadIdx.x == 0)
+    cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
                               double Ttar, const cudaGraphConditionalHandle* cond) {
   (void)Ttar;
-  k_spec_drift<<<(P.N + 255) / 256, 256, 0, L.stream>>>(P, S, cond ? *cond : 0ull,
-                                                        cond ? 1 : 0);
+  const int nb = (P.N + 255) / 256;
+  if (P.nrep > 1)
+    k_spec_drift<1><<<nb, 256, 0, L.stream>>>(P, S);
+  else
+    k_spec_drift<0><<<nb, 256, 0, L.stream>>>(P, S);
+  // in a graph, the rebuild condition of the IF node that follows
+  if (cond) k_spec_cond<<<1, 32, 0, L.stream>>>(S, *cond);
   return cudaGetLastError();
 }
 
 // Kick (apply != 0) followed by the reductions the next step needs: the
 // largest speed (variable dt = min(dt_max, dx_max / max|v|)) and the
-// thermostat layer's sum m v^2 and count. Each block adds its share to the
-// replica's accumulators (the max through the bit order of non-negative
-// doubles, an integer atomic); the last of a replica's blocks to finish (a
-// ticket counter) derives dt and the Berendsen factor from them.
+// thermostat layer's sum m v^2 and count.
+//
+// The reductions stay off the critical path of the ~1000 co-resident
+// blocks: the max of v^2 >= 0 is taken on its bit pattern (integer order),
+// the layer count is an integer, only warps holding layer atoms sum m v^2
+// (binary64 is scarce: a warp instruction holds the SM's FP64 unit for 16
+// cycles), and after one barrier only warp 0 goes on. Completion is counted
+// in two levels — a ticket per group of kKickGroup blocks, whose last block
+// combines the group's partials, then one ticket per replica, whose last
+// block combines the group partials — because a same-address atomic from
+// every block serialises in L2, and a last block reducing all block
+// partials is a long dependent chain. Sums run in a fixed order
+// (deterministic). The replica's last warp derives dt and the Berendsen
+// factor.
+// Warp max of non-negative doubles held as bits: redux.sync on the high
+// words, then on the low words of the lanes holding the high maximum.
+__device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
+  const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32));
+  const unsigned lo = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32) == hi ? (unsigned)v : 0u);
+  return ((unsigned long long)hi << 32) | lo;
+}
+
+__device__ __forceinline__ void kick_combine(unsigned long long& m, double& a, int& c) {
+  m = warp_max_bits(m);
+  c = (int)__reduce_add_sync(0xffffffffu, (unsigned)c);
+  if (c) a = warp_sum(a);
+}
+
+template <int BATCH>
 __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
                                                              double Ttar) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double v2 = 0.0, ts = 0.0, tc = 0.0;
+  uint32_t fl = FL_REMOVED;
+  unsigned long long vb = 0ull;  // bits of v^2
+  double ts = 0.0;
+  int tc = 0;
   if (i < P.N) {
-    const uint32_t fl = S.flags[i];
+    fl = S.flags[i];
+    double4_32a v = S.vel[i];
+    double4_32a f = {}, g = {};
+    double im = 0.0;
+    if (apply) {
+      f = S.frc[i];
+      g = S.frc_new[i];
+      im = S.inv_mass[i];
+    }
+    const double m = S.mass[i];
+    const int8_t at = S.atype[i];
+    // a kick block lies inside one replica (replicas start at multiples of
+    // the block size)
+    const double hdt = S.sc[BATCH ? rep_of_flags(fl) : 0].half_dt;
     if (!(fl & FL_REMOVED)) {
-      // a kick block lies inside one replica (replicas start at multiples
-      // of the block size)
-      const double hdt = ((volatile DevScalars*)(S.sc + rep_of_flags(fl)))->half_dt;
-      double4_32a v = S.vel[i];
       if (apply) {
-        const double4_32a f = S.frc[i];
-        const double4_32a g = S.frc_new[i];
-        const double c = hdt * S.inv_mass[i];
+        const double c = hdt * im;
         v.x = v.x + c * (f.x + g.x);
         v.y = v.y + c * (f.y + g.y);
         v.z = v.z + c * (f.z + g.z);
@@ -446,68 +493,99 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
         // the old force's buffer accumulates the next force (after the swap)
         S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
       }
-      v2 = v.x * v.x + v.y * v.y + v.z * v.z;
-      // a non-finite force or velocity shows here; the host reports it
-      if (!(v2 < INFINITY)) {
+      const double v2 = v.x * v.x + v.y * v.y + v.z * v.z;
+      vb = (unsigned long long)__double_as_longlong(v2);
+      // a non-finite force or velocity shows here (exponent all ones, or a
+      // negative NaN); the host reports it
+      if (vb >= 0x7ff0000000000000ull) {
         atomicOr(&S.sc->nan_flag, 1);
-        v2 = 0.0;
-      }
-      if ((fl & FL_THERMO) && S.atype[i] < 3) {
-        ts = S.mass[i] * v2;
-        tc = 1.0;
+        vb = 0ull;
+      } else if ((fl & FL_THERMO) && at < 3) {
+        ts = m * v2;
+        tc = 1;
       }
     }
   }
-  unsigned long long vb = (unsigned long long)__double_as_longlong(v2);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long t = __shfl_xor_sync(0xffffffffu, vb, o);
-    vb = t > vb ? t : vb;
-  }
-  const bool thermo = __any_sync(0xffffffffu, tc > 0.0);
-  if (thermo) {
-    ts = warp_sum(ts);
-    tc = warp_sum(tc);
-  }
+  kick_combine(vb, ts, tc);
   __shared__ unsigned long long smax[kKickThreads / 32];
-  __shared__ double ssum[kKickThreads / 32], scnt[kKickThreads / 32];
+  __shared__ double ssum[kKickThreads / 32];
+  __shared__ int scnt[kKickThreads / 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
     smax[w] = vb;
-    ssum[w] = thermo ? ts : 0.0;
-    scnt[w] = thermo ? tc : 0.0;
+    ssum[w] = ts;
+    scnt[w] = tc;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  unsigned long long m = 0ull;
-  double a = 0.0, b = 0.0;
-  for (int q = 0; q < kKickThreads / 32; q++) {
-    m = smax[q] > m ? smax[q] : m;
-    a += ssum[q];
-    b += scnt[q];
-  }
-  // the replica of this block: its first atom's (blocks never straddle
-  // replicas, and a replica's padding only ends its last block)
-  const int i0 = blockIdx.x * blockDim.x;
-  const int r = i0 < P.N ? rep_of_flags(S.flags[i0]) : 0;
-  DevScalars* R = S.sc + r;
-  atomicMax(&R->acc_vmax2, m);
-  if (a != 0.0) atomicAdd(&R->acc_tsum, a);
-  if (b != 0.0) atomicAdd(&R->acc_tcnt, b);
-  // the last of the replica's blocks derives dt and the thermostat factor
-  // and clears the accumulators for the next kick
+  if (w != 0) return;
+  // warp 0: the block's partial
+  constexpr int kWarps = kKickThreads / 32;
+  unsigned long long m = lane < kWarps ? smax[lane] : 0ull;
+  int c = lane < kWarps ? scnt[lane] : 0;
+  double a = c ? ssum[lane] : 0.0;
+  kick_combine(m, a, c);
+  // the replica of this block: its first atom's, lane 0's (blocks never
+  // straddle replicas, and a replica's padding only ends its last block)
+  const int r = BATCH ? __shfl_sync(0xffffffffu, rep_of_flags(fl), 0) : 0;
   const Geo& G = S.geo[r];
+  const int nblk = G.blk_end - G.blk_begin;
+  const int grp = ((int)blockIdx.x - G.blk_begin) / kKickGroup;
+  const int gsize = min(kKickGroup, nblk - grp * kKickGroup);
+  const int ngrp = (nblk + kKickGroup - 1) / kKickGroup;
+  // group slots of different replicas never share an index
+  const int gidx = G.blk_begin / kKickGroup + r + grp;
+  const size_t gstride = (size_t)kMaxRedBlocks / kKickGroup + P.nrep + 2;
+  unsigned* gt = S.group_ticket + 8 * (size_t)gidx;
+  int st = 0;
+  if (lane == 0) {
+    S.partials[blockIdx.x] = __longlong_as_double((long long)m);
+    S.partials[kMaxRedBlocks + blockIdx.x] = a;
+    S.partials[2 * kMaxRedBlocks + blockIdx.x] = (double)c;
+    __threadfence();
+    st = atomicAdd(gt, 1u) == (unsigned)(gsize - 1);
+  }
+  if (!__shfl_sync(0xffffffffu, st, 0)) return;
+  // the group's last block: combine the group's block partials
   __threadfence();
-  const unsigned t = atomicAdd(&R->ticket[5], 1u);
-  if (t != (unsigned)(G.blk_end - G.blk_begin - 1)) return;
+  m = 0ull;
+  a = 0.0;
+  c = 0;
+  if (lane < gsize) {
+    const int b = G.blk_begin + grp * kKickGroup + lane;
+    m = (unsigned long long)__double_as_longlong(__ldcg(S.partials + b));
+    c = (int)__ldcg(S.partials + 2 * kMaxRedBlocks + b);
+    if (c) a = __ldcg(S.partials + kMaxRedBlocks + b);
+  }
+  kick_combine(m, a, c);
+  double* gp = S.group_part;
+  if (lane == 0) {
+    gp[gidx] = __longlong_as_double((long long)m);
+    gp[gstride + gidx] = a;
+    gp[2 * gstride + gidx] = (double)c;
+    *gt = 0u;  // every block of the group has counted
+    __threadfence();
+    st = atomicAdd(&S.sc[r].ticket[5], 1u) == (unsigned)(ngrp - 1);
+    if (st) S.sc[r].ticket[5] = 0u;
+  }
+  if (!__shfl_sync(0xffffffffu, st, 0)) return;
+  // the replica's last group: combine the group partials
   __threadfence();
-  volatile DevScalars* V = R;
-  const double mx = __longlong_as_double((long long)V->acc_vmax2);
-  const double tsum = V->acc_tsum, tcnt = V->acc_tcnt;
-  R->acc_vmax2 = 0ull;
-  R->acc_tsum = 0.0;
-  R->acc_tcnt = 0.0;
-  R->ticket[5] = 0u;
+  m = 0ull;
+  a = 0.0;
+  c = 0;
+  const int g0 = G.blk_begin / kKickGroup + r;
+  for (int q = lane; q < ngrp; q += 32) {
+    const unsigned long long x = (unsigned long long)__double_as_longlong(__ldcg(gp + g0 + q));
+    m = x > m ? x : m;
+    const int cq = (int)__ldcg(gp + 2 * gstride + g0 + q);
+    if (cq) a += __ldcg(gp + gstride + g0 + q);
+    c += cq;
+  }
+  kick_combine(m, a, c);
+  if (lane != 0) return;
+  const double mx = __longlong_as_double((long long)m);
+  const double tsum = a, tcnt = (double)c;
+  DevScalars* R = S.sc + r;
   R->thermo_sum = tsum;
   R->thermo_cnt = tcnt;
   R->vmax2 = mx;
@@ -531,7 +609,10 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
                              double Ttar, int apply) {
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
-  k_spec_kick<<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
+  if (P.nrep > 1)
+    k_spec_kick<1><<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
+  else
+    k_spec_kick<0><<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
   return cudaGetLastError();
 }
 

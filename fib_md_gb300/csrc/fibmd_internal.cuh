@@ -28,6 +28,7 @@ namespace fibmd {
 constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
 constexpr int kMaxRedBlocks = 16384;  // row stride of the reduction partials
+constexpr int kKickGroup = 32;     // spec kick blocks per first-level ticket
 constexpr int kKickThreads = 256;  // spec kick block; replicas start at multiples
 // Binary32 SW legs with exp(gamma/(u-a)) below this are dropped: an angle
 // term is at most lambda*eps*E_a*E_b (~45 eV E_a E_b), so such a leg moves a
@@ -135,8 +136,6 @@ struct DevScalars {
   double dt;           // spec: current step
   double half_dt;      //       dt / 2 (kick)
   double half_dt2;     //       dt^2 / 2 (drift)
-  unsigned long long acc_vmax2;   // spec kick accumulators: max |v|^2 (bits),
-  double acc_tsum, acc_tcnt;      // thermostat layer sum m v^2 and count
   double dt_next;      // spec: step chosen from this step's velocities
   double thermo_sum, thermo_cnt;  // spec thermostat layer
   double ekin, epot;   // energies (J)
@@ -207,6 +206,8 @@ struct DevState {
   double* epot;
   // reductions
   double* partials;
+  unsigned* group_ticket;  // spec kick: first-level tickets, 32 bytes apart
+  double* group_part;      //            group partials (3 rows)
   DevScalars* sc;    // one per replica; context-wide fields live in sc[0]
   // replicas
   const Geo* geo;    // nrep entries
