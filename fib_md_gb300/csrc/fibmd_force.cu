@@ -494,9 +494,13 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
 }
 
 // Centres with more than kMaxLegs active legs (compressed cascade regions):
-// one warp per centre. The lanes first compute every listed leg in binary64
-// and stage the active ones in shared memory, then split the leg pairs; leg
-// reactions are scattered with atomics, the centre's force is warp-reduced.
+// one warp per centre. The lanes first compute every listed leg (binary64,
+// or binary32 in mixed precision) and stage the active ones in shared
+// memory, then take legs as rows: a lane sums its leg's reaction over every
+// other leg in registers and scatters it once. Each angle term is evaluated
+// in both of its rows, which costs less than splitting the pairs over the
+// lanes: that needs shared-memory atomics on the leg sums, and lanes sharing
+// a leg serialise on them. The centre's force is warp-reduced.
 constexpr int kHeavyWarps = 4;
 constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
@@ -505,7 +509,6 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
   // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
   using R = typename std::conditional<MIXED, float, double>::type;
   __shared__ R sl[kHeavyWarps][6][kHeavyLegs];
-  __shared__ R sr[kHeavyWarps][4][kHeavyLegs];  // reaction x, y, z and energy per leg
   __shared__ int sj[kHeavyWarps][kHeavyLegs];
   __shared__ int snl[kHeavyWarps];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -556,59 +559,41 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     }
     __syncwarp();
     const int nl = snl[w];
-    for (int k = lane; k < nl; k += 32) sr[w][0][k] = sr[w][1][k] = sr[w][2][k] = sr[w][3][k] = 0;
-    __syncwarp();
-    // the nl(nl-1)/2 leg pairs shared out over the lanes; each leg's reaction
-    // is summed in shared memory and scattered once
+    // rows: lane sums leg a's reaction over every other leg b in registers
+    // (each term evaluated in both of its rows; no shared-memory atomics)
     R fcx = 0, fcy = 0, fcz = 0, uc = 0;
     const R thrd = (R)P.thrd;
-    const int npair = nl * (nl - 1) / 2;
-    int a = 0, a_end = nl - 1;  // pairs of leg a are [a_end - (nl - 1 - a), a_end)
-    for (int q = lane; q < npair; q += 32) {
-      while (q >= a_end) {
-        a++;
-        a_end += nl - 1 - a;
-      }
-      const int b = nl - (a_end - q);
+    for (int a = lane; a < nl; a += 32) {
       const R ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
-      const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
-      const R ar = sl[w][3][a], br = sl[w][3][b];
-      const int ja = sj[w][a], jb = sj[w][b];
-      const R cs = ax * bx + ay * by + az * bz;
-      const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
-      R lp;
-      if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-      else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-      const R pref = lp * sl[w][4][a] * sl[w][4][b];
-      const R wa = W * sl[w][5][a] - s2 * cs * ar, sa = s2 * ar;
-      const R wb = W * sl[w][5][b] - s2 * cs * br, sb = s2 * br;
-      const R Fax = pref * (wa * ax + sa * bx), Fay = pref * (wa * ay + sa * by),
-              Faz = pref * (wa * az + sa * bz);
-      const R Fbx = pref * (wb * bx + sb * ax), Fby = pref * (wb * by + sb * ay),
-              Fbz = pref * (wb * bz + sb * az);
-      atomicAdd(&sr[w][0][a], Fax);
-      atomicAdd(&sr[w][1][a], Fay);
-      atomicAdd(&sr[w][2][a], Faz);
-      atomicAdd(&sr[w][0][b], Fbx);
-      atomicAdd(&sr[w][1][b], Fby);
-      atomicAdd(&sr[w][2][b], Fbz);
-      fcx -= Fax + Fbx;
-      fcy -= Fay + Fby;
-      fcz -= Faz + Fbz;
-      if (ENERGY) {
-        const R e3 = pref * W / (R)3;
-        uc += e3;
-        atomicAdd(&sr[w][3][a], e3);
-        atomicAdd(&sr[w][3][b], e3);
+      const R ar = sl[w][3][a], aE = sl[w][4][a], ag = sl[w][5][a];
+      const int ja = sj[w][a];
+      R afx = 0, afy = 0, afz = 0, ae = 0;
+      for (int b = 0; b < nl; b++) {
+        if (b == a) continue;
+        const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
+        const int jb = sj[w][b];
+        const R cs = ax * bx + ay * by + az * bz;
+        const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
+        R lp;
+        if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+        else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+        const R pref = lp * aE * sl[w][4][b];
+        const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
+        afx += pref * (wa * ax + sa * bx);
+        afy += pref * (wa * ay + sa * by);
+        afz += pref * (wa * az + sa * bz);
+        if (ENERGY) ae += pref * W;
       }
+      const int j = ja & 0x3fffffff;
+      atomic_add3(S.frc_new, j, conv * (double)afx, conv * (double)afy, conv * (double)afz);
+      if (ENERGY && ae != (R)0) atomicAdd(&S.epot[j], econv * (double)ae / 3.0);
+      fcx -= afx;
+      fcy -= afy;
+      fcz -= afz;
+      if (ENERGY) uc += ae;
     }
-    __syncwarp();
-    for (int k = lane; k < nl; k += 32) {
-      const int j = sj[w][k] & 0x3fffffff;
-      atomic_add3(S.frc_new, j, conv * (double)sr[w][0][k], conv * (double)sr[w][1][k],
-                  conv * (double)sr[w][2][k]);
-      if (ENERGY && sr[w][3][k] != (R)0) atomicAdd(&S.epot[j], econv * (double)sr[w][3][k]);
-    }
+    // the centre's third of each term, counted in both rows
+    if (ENERGY) uc /= (R)6;
     const double dcx = warp_sum(conv * (double)fcx);
     const double dcy = warp_sum(conv * (double)fcy);
     const double dcz = warp_sum(conv * (double)fcz);

@@ -237,3 +237,47 @@ def test_mixed_precision_force_error(gpu_lib):
     rms_rel = np.sqrt(np.mean(np.sum((F - Fr) ** 2, axis=1))) / np.sqrt(np.mean(np.sum(Fr ** 2, axis=1)))
     assert rms_rel < 2e-5, rms_rel
     assert _maxrel(F, Fr) < 1e-4
+
+
+def _compressed_core(scale=0.8, radius_A=6.0):
+    """The slab with a compressed core, as in a cascade: displacements from
+    the middle of the lattice within radius_A scaled by `scale`. Second
+    neighbours move inside the SW cutoff, so the core's centres have ~16
+    legs, more than either force kernel stages per thread."""
+    o = _slab()
+    nsg = o.p.Nsg
+    X = o.X[:nsg]
+    c = np.median(X, axis=0)
+    d = X - c
+    sel = np.sqrt(np.sum(d * d, axis=1)) < radius_A * 1e-10
+    X[sel] = c + scale * d[sel]
+    assert sel.sum() > 20
+    return o
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_many_leg_centres(gpu_lib, precision):
+    """Centres with more legs than the per-thread stage (the many-leg paths:
+    the warp-per-centre kernel in binary64, the warp-cooperative epilogue of
+    the binary32 kernel) against the binary64 oracle: within 1e-10 in
+    binary64, at the crystal test's binary32 tolerances in mixed precision."""
+    import fib_md_gb300 as fm
+
+    o = _compressed_core()
+    o.si_nlist()
+    Fr = o.si_force()
+    p = o.p.copy()
+    p.precision = precision
+    g = fm.FibMD(p)
+    g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
+    g.set_impact(1)
+    g.si_nlist()
+    F = g.si_force()
+    assert g.work_counters()[5] > 0  # the many-leg path ran
+    if precision == 0:
+        assert _maxrel(F, Fr) < FORCE_RTOL
+    else:
+        rms_rel = np.sqrt(np.mean(np.sum((F - Fr) ** 2, axis=1))) / np.sqrt(
+            np.mean(np.sum(Fr ** 2, axis=1)))
+        assert rms_rel < 2e-5, rms_rel
+        assert _maxrel(F, Fr) < 1e-4
