@@ -53,8 +53,11 @@ def parse():
     ap.add_argument("--cpu-sample-steps", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--list-skin", type=float, default=0.0,
-                    help="spec-mode list skin in Angstrom (0: the reference's list radii)")
+    ap.add_argument("--list-skin", type=float, default=0.6,
+                    help="spec-mode list skin in Angstrom (0: the reference's list radii). "
+                         "The fastest atom moves dx_max per step, so the skin sets the "
+                         "rebuild interval against the list length the force kernel scans; "
+                         "0.6 A (a rebuild every ~6 steps of the cascade) measured fastest")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the step loop launch by launch (for a profiler's launch list)")
     ap.add_argument("--ensemble-replicas", type=int, default=256)
