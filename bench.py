@@ -69,6 +69,8 @@ def parse():
                     help="impacts of the cumulative-dose run (0: skip)")
     ap.add_argument("--dose-fp64-impacts", type=int, default=-1,
                     help="impacts of its binary64 counterpart (default: as many)")
+    ap.add_argument("--large-steps", type=int, default=20000,
+                    help="MD steps of the 1,048,577-atom 30 keV cascade (0: skip)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step"], default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64), "
                          "rebuild the lists 5 times (build) or run 10 mixed steps launch "
@@ -78,7 +80,8 @@ def parse():
 
 # ---------------------------------------------------------------------------
 # workload
-def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A=0.0):
+def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A=0.0,
+                  centre=False):
     import fib_md_gb300 as fm
 
     p = fm.params_default()
@@ -105,7 +108,9 @@ def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A
     th = np.deg2rad(polar_deg)
     speed = np.sqrt(2 * energy_eV * p.ec / p.massGa)
     X = s.X.copy(order="F")
-    X[nsg] = [rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1]), surf + 10e-10]
+    xy = [0.5 * p.Lb[0], 0.5 * p.Lb[1]] if centre else \
+        [rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1])]
+    X[nsg] = [xy[0], xy[1], surf + 10e-10]
     V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
     p.Ttar1 = 300.0
     p.tau_spec = 1.0e-13
@@ -410,6 +415,82 @@ def bench_ours(args, rank, world, dist):
     if e2e:
         out["e2e"] = e2e
     return out
+
+
+# ---------------------------------------------------------------------------
+# binary64 flops of one spec-mode integration step per atom: the drift's
+# c = dt^2/2m (1), x + v dt + c f (3 x 2 FMA = 12) and fixed-point shadow (3
+# FMA = 6) and removal test (2); the kick's c = dt/2m (1), f + f' (3),
+# v + c (f + f') (3 FMA = 6) and |v|^2 (5)
+INTEGRATOR_FP64_FLOPS = 36
+
+
+def bench_large(args):
+    """The large single cascade: 64x64x32 unit cells (1,048,576 Si; diamond
+    has 8 atoms per cell) and one 30 keV Ga at normal incidence on the slab
+    centre, args.large_steps variable-dt steps in mixed precision through the
+    CUDA-graph step loop, timed whole (cascade and all) with CUDA events."""
+    import torch
+
+    import fib_md_gb300 as fm
+
+    w = make_workload((64, 64, 32), seed=5001, energy_eV=30000.0, polar_deg=0.0,
+                      list_skin_A=args.list_skin, centre=True)
+    N = w["params"].Natm
+    fp64_peak, fp32_peak = fm.md.pipe_peaks()
+    g = make_ctx(w, fm.PREC_MIXED)
+    g.set_option("timers", 0)
+    stream = torch.cuda.ExternalStream(g.stream_ptr)
+    rb0 = g.work_counters()[4]
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        a.record(stream)
+        _, t_sim, _, _ = g.steps(2, args.large_steps, 0, 0.0, 300.0)
+        b.record(stream)
+        torch.cuda.synchronize()
+    secs = a.elapsed_time(b) / 1e3
+    rebuilds = g.work_counters()[4] - rb0
+    # the main force kernel timed live over a launch-by-launch segment
+    g.set_option("graph", 0)
+    g.set_option("kernel_timing", 1)
+    g.kernel_time(reset=True)
+    g.steps(2, 100, 0, t_sim, 300.0)
+    fk_total, fk_n = g.kernel_time(reset=True)
+    g.si_force()
+    counts = g.work_counters()
+    g.close()
+    fk = fk_total / max(fk_n, 1)
+    f32 = flops_per_force(counts) / fk / 1e12
+    rate = N * args.large_steps / secs
+    f64 = INTEGRATOR_FP64_FLOPS * rate / 1e12
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    return {
+        "config": "Si slab 64x64x32 unit cells (1,048,576 Si + 1 Ga), 30 keV Ga at normal "
+                  f"incidence on the slab centre, {args.large_steps} variable-dt steps, "
+                  "mixed precision, CUDA-graph step loop, list skin "
+                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+        "atoms": N, "md_steps": args.large_steps,
+        "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
+        "simulated_ps": t_sim * 1e12,
+        "rebuild_fraction": rebuilds / float(args.large_steps),
+        "fp32_pipe": {"kernel": "k_force<mixed>", "achieved_tflops": f32, "peak_tflops": fp32_peak,
+                      "frac": f32 / fp32_peak, "force_kernel_us": 1e6 * fk,
+                      "peak_source": "measured in this run (FFMA loop)"},
+        "fp64_pipe": {"what": "integration (drift + kick), INTEGRATOR_FP64_FLOPS per atom-step "
+                              "over the whole step time",
+                      "achieved_tflops": f64, "peak_tflops": fp64_peak, "frac": f64 / fp64_peak,
+                      "peak_source": "measured in this run (DFMA loop)"},
+        "hbm": {"achieved_gbs": 150.0 * rate / 1e9, "peak_gbs": hbm_peak,
+                "frac": 150.0 * rate / 1e9 / hbm_peak, "bytes_per_atom_step": 150,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs"},
+        "work_counters": {"sw_pairs": counts[0], "angle_terms": counts[1],
+                          "moliere_pairs": counts[2], "many_leg_centres": counts[5]},
+        "clocks": clk.summary(),
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -767,6 +848,8 @@ def main():
         out["ensemble"] = bench_ensemble(args)
     if args.dose_impacts > 0:
         out["dose"] = bench_dose(args)
+    if args.large_steps > 0 and rank == 0:
+        out["large"] = bench_large(args)
     if rank == 0:
         if not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(cells, args.cpu_sample_steps)
