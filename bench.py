@@ -560,7 +560,7 @@ def nve_drift(w, precision, steps=1000):
 
 # ---------------------------------------------------------------------------
 # batched ensemble: independent impacts on uneven slabs
-def make_ensemble(nrep, precision, seed0=3000):
+def make_ensemble(nrep, precision, seed0=3000, list_skin_A=0.0):
     """Slabs of U{6..12} x U{6..12} x 10 unit cells, one Ga each at
     U(0.5, 5) keV and U(0, 30) degrees off normal, seeded azimuth and impact
     point (seed 3000 + r); atoms more than 15 A above the surface leave."""
@@ -568,6 +568,7 @@ def make_ensemble(nrep, precision, seed0=3000):
 
     p = fm.params_default()
     p.precision = precision
+    p.list_skin = list_skin_A * 1e-10
     rs = np.random.default_rng(seed0)
     slabs = []
     for r in range(nrep):
@@ -662,7 +663,7 @@ def bench_ensemble(args):
     import fib_md_gb300 as fm
 
     nrep, steps = args.ensemble_replicas, args.ensemble_steps
-    slabs = make_ensemble(nrep, fm.PREC_MIXED)
+    slabs = make_ensemble(nrep, fm.PREC_MIXED, list_skin_A=args.list_skin)
     # a short warm-up batch (context set-up, graph capture, first-touch)
     run_ensemble_batch(slabs[:4], fm.PREC_MIXED, 20)
     mixed = run_ensemble_batch(slabs, fm.PREC_MIXED, steps)
@@ -678,7 +679,8 @@ def bench_ensemble(args):
     ok = all(v["p_mannwhitney"] is None or v["p_mannwhitney"] > 0.05 for v in cmp.values())
     return {
         "config": f"{nrep} impacts, U{{6..12}}^2 x 10 unit-cell slabs, U(0.5,5) keV Ga, "
-                  f"U(0,30) deg, {steps} variable-dt steps each, one batch context",
+                  f"U(0,30) deg, {steps} variable-dt steps each, one batch context, list skin "
+                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
         "impacts_per_hour": {"mixed_batched": ih(mixed), "fp64_batched": ih(fp64),
                              "fp64_plain": 3600.0 / plain_s},
         "mixed_batched_over_fp64_plain": ih(mixed) * plain_s / 3600.0,
@@ -728,8 +730,10 @@ def bench_dose(args):
 
     n = args.dose_impacts
     n64 = n if args.dose_fp64_impacts < 0 else min(n, args.dose_fp64_impacts)
+    p = fm.params_default()
+    p.list_skin = args.list_skin * 1e-10
     d = fm.dose_slab((20, 20, 12), n, seed=4001, ion_eV=2000.0, window=30e-10,
-                     remove_above=15e-10)
+                     remove_above=15e-10, params=p)
     mixed = run_dose(d, fm.PREC_MIXED, n)
     fp64 = run_dose(d, fm.PREC_FP64, n64) if n64 > 0 else None
     per = lambda r: np.diff(np.concatenate([[0], r["removed"]])).tolist()
@@ -737,7 +741,8 @@ def bench_dose(args):
         "config": f"20x20x12 unit-cell slab ({d.slab.params.Nsg} Si), {n} successive 2 keV Ga "
                   "impacts at normal incidence in a 30x30 A window (seed 4001), 3000 steps "
                   "then 2 ps relaxation each, atoms 15 A above the surface removed, one "
-                  "device-side dose call",
+                  "device-side dose call, list skin "
+                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
         "impacts": n,
         "impacts_per_hour": {"mixed": 3600.0 * n / mixed["wall_s"]},
         "wall_s": {"mixed": mixed["wall_s"]},

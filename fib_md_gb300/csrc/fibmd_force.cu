@@ -63,11 +63,10 @@ constexpr int kBlock64 = 64;
 constexpr int kLegF32 = 6;   // ux uy uz rinv E g
 constexpr int kBlock32 = 128;
 constexpr int kCandF64 = 16;  // prefiltered neighbours staged per centre (binary64 kernel)
-constexpr int kLegs32 = 6;   // staged candidates per centre (binary32 kernel);
-                             // a crystal at 300 K has 4 legs, rarely more than 6,
-                             // and more centres go to the many-leg kernel; the
-                             // smaller stage leaves more of the SM's memory to
-                             // the L1 cache the neighbour gathers hit
+constexpr int kLegs32 = 8;   // staged candidates per centre (binary32 kernel);
+                             // a crystal at 300 K has 4 legs, rarely more than 6;
+                             // the damaged slabs of a batch of small cascades
+                             // need the headroom (fewer many-leg centres)
 
 constexpr int kBatch = 8;    // neighbour gathers in flight per thread
 
