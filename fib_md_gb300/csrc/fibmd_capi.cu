@@ -81,6 +81,11 @@ struct fibmd_ctx {
   cudaStream_t cap2 = nullptr;
   double4_32a* graph_frc = nullptr;  // S.frc when the graph was captured
   int graph_nfired = -1;
+  int graph_stage = 0;               // the force stage size it was captured with
+  // binary32 force kernel: stage size, re-chosen by timing (autotune) before
+  // each chunk of kTuneSteps spec-mode steps
+  int stage = kStageSmall;
+  bool autotune = true;
   LoopCtl* d_loop = nullptr;
   // replicas: one for a single system, several for a batched ensemble
   Geo geo0;                 // the single system's geometry
@@ -125,6 +130,7 @@ static Launch launch_of(const fibmd_ctx* ctx) {
   Launch L;
   L.stream = ctx->stream;
   L.sms = ctx->sms;
+  L.stage = ctx->stage;
   return L;
 }
 
@@ -1236,6 +1242,13 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->kernel_timing = value != 0.0;
   } else if (!std::strcmp(key, "graph")) {
     ctx->use_graph = value != 0.0;
+  } else if (!std::strcmp(key, "autotune")) {
+    ctx->autotune = value != 0.0;
+  } else if (!std::strcmp(key, "stage")) {
+    if (value != kStageSmall && value != kStageLarge)
+      return fail(ctx, FIBMD_EINVAL, "stage must be %d or %d", kStageSmall, kStageLarge);
+    ctx->stage = (int)value;
+    ctx->autotune = false;
   } else {
     return fail(ctx, FIBMD_EINVAL, "unknown option '%s'", key);
   }
@@ -1384,6 +1397,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     return fail(ctx, FIBMD_ECUDA, "graph instantiate: %s", cudaGetErrorString(ei));
   }
   ctx->graph_frc = ctx->S.frc;
+  ctx->graph_stage = ctx->stage;
   ctx->graph_nfired = P.nfired;
   return FIBMD_OK;
 }
@@ -1391,8 +1405,39 @@ static int build_spec_graph(fibmd_ctx* ctx) {
 // Runs `pairs` x 2 spec-mode steps with one graph launch.
 // Enqueues `pairs` step pairs (stopping early after `relax` seconds of
 // simulated time when relax > 0); returns without waiting.
+constexpr long long kTuneSteps = 1000;  // spec-mode steps between stage re-tunings
+
+// Times the binary32 force kernel with each stage size on the current state
+// (one untimed and two timed evaluations each) and keeps the faster one. It
+// reads the lists, so it runs only once they are built; the evaluations
+// accumulate into the next-force buffer, which the caller clears.
+static int tune_stage(fibmd_ctx* ctx) {
+  if (ctx->P.precision != FIBMD_PREC_MIXED || !ctx->autotune || !ctx->lists_built)
+    return FIBMD_OK;
+  cudaEvent_t a = get_event(ctx), b = get_event(ctx);
+  const int stages[2] = {kStageSmall, kStageLarge};
+  float ms[2] = {0.f, 0.f};
+  for (int q = 0; q < 2; q++) {
+    Launch L = launch_of(ctx);
+    L.stage = stages[q];
+    CK(launch_force(L, ctx->P, ctx->S, false, false, false));
+    CK(cudaEventRecord(a, ctx->stream));
+    for (int k = 0; k < 2; k++) CK(launch_force(L, ctx->P, ctx->S, false, false, false));
+    CK(cudaEventRecord(b, ctx->stream));
+    CK(cudaEventSynchronize(b));
+    CK(cudaEventElapsedTime(&ms[q], a, b));
+  }
+  ctx->pool.push_back(a);
+  ctx->pool.push_back(b);
+  // switch only for a clear gain: a switch recaptures the step graph
+  const int cur = ctx->stage == kStageLarge ? 1 : 0;
+  if (ms[1 - cur] < 0.97f * ms[cur]) ctx->stage = stages[1 - cur];
+  return FIBMD_OK;
+}
+
 static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
-  if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired) {
+  if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
+      ctx->graph_stage != ctx->stage) {
     int rc = build_spec_graph(ctx);
     if (rc) return rc;
   }
@@ -1421,8 +1466,21 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
   CK(cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, ctx->stream));
   long long todo = max_steps;
   if (ctx->use_graph && todo >= 2) {
-    int rc = run_spec_graph(ctx, todo / 2);
-    if (rc) return rc;
+    // in chunks of kTuneSteps steps, before each of which the binary32 force
+    // kernel's stage size is re-chosen on the current state
+    const bool tune = ctx->autotune && P.precision == FIBMD_PREC_MIXED && ctx->lists_built;
+    for (long long pairs = todo / 2; pairs > 0;) {
+      const long long chunk = tune ? std::min(pairs, kTuneSteps / 2) : pairs;
+      if (tune) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        int rt = tune_stage(ctx);
+        if (rt) return rt;
+        CK(cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, ctx->stream));
+      }
+      int rc = run_spec_graph(ctx, chunk);
+      if (rc) return rc;
+      pairs -= chunk;
+    }
     *lt += 2 * (todo / 2);
     todo -= 2 * (todo / 2);
   }
@@ -1504,6 +1562,11 @@ int fibmd_gpu_dose(fibmd_ctx* ctx, int nimp, const int* ion_atoms, const double*
   const Launch L = launch_of(ctx);
   const DevParams& P = ctx->P;
   const double Ttar = ctx->p.Ttar1;
+  // the force stage size for the whole dose, chosen on the slab as it is
+  {
+    int rt = tune_stage(ctx);
+    if (rt) return done(rt);
+  }
   cudaError_t e = cudaMemcpyAsync(d_tab, tab.data(), sizeof(Impact) * (size_t)nimp,
                                   cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess)

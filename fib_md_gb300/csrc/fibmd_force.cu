@@ -63,10 +63,8 @@ constexpr int kBlock64 = 64;
 constexpr int kLegF32 = 6;   // ux uy uz rinv E g
 constexpr int kBlock32 = 128;
 constexpr int kCandF64 = 16;  // prefiltered neighbours staged per centre (binary64 kernel)
-constexpr int kLegs32 = 8;   // staged candidates per centre (binary32 kernel);
-                             // a crystal at 300 K has 4 legs, rarely more than 6;
-                             // the damaged slabs of a batch of small cascades
-                             // need the headroom (fewer many-leg centres)
+// (the binary32 kernel's stage sizes, kStageSmall and kStageLarge, are in
+// fibmd_internal.cuh: the context chooses between them)
 
 constexpr int kBatch = 8;    // neighbour gathers in flight per thread
 
@@ -263,7 +261,7 @@ __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevSta
 // ions (an ion has a few dozen listed pairs, both orders), at least two
 inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P.nion + 1) / 2)); }
 
-template <bool ENERGY, bool COUNT>
+template <bool ENERGY, bool COUNT, int LEGS>
 __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
   // the last mol_blocks blocks evaluate the Moliere list (a few dozen pairs
   // per ion), which saves a launch per step
@@ -278,8 +276,8 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
   // of a leg; B = (1/r, g) of a leg; I = neighbour index | type << 30. Vector
   // accesses keep the shared-memory instruction count low.
   float4* sA = reinterpret_cast<float4*>(smem_raw);
-  float2* sB = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * kLegs32 * kBlock32);
-  int* sI = reinterpret_cast<int*>(smem_raw + (sizeof(float4) + sizeof(float2)) * kLegs32 *
+  float2* sB = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * LEGS * kBlock32);
+  int* sI = reinterpret_cast<int*>(smem_raw + (sizeof(float4) + sizeof(float2)) * LEGS *
                                                   kBlock32);
   const int t = threadIdx.x;
 
@@ -349,7 +347,7 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
       if (r2f > P.pre3mA2) continue;
       const int tb = (qq[u].w & 0xff) - 1;
-      if (r2f <= P.pre3lA2 && nc < kLegs32) {
+      if (r2f <= P.pre3lA2 && nc < LEGS) {
         sA[nc * kBlock32 + t] = make_float4(dq.x, dq.y, dq.z, r2f);
         sI[nc * kBlock32 + t] = jj[u] | (tb << 30);
         nc++;
@@ -753,13 +751,15 @@ __global__ void k_force_begin(DevState S) {
   if (threadIdx.x < 4) S.sc->counters[threadIdx.x] = 0ull;
 }
 
-template <bool MIXED, bool ENERGY, bool COUNT>
+template <bool MIXED, bool ENERGY, bool COUNT, int LEGS>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
   constexpr int BLOCK = MIXED ? kBlock32 : kBlock64;
-  const size_t smem = MIXED ? (sizeof(float) * kLegs32 * kLegF32 + sizeof(int) * kLegs32) * BLOCK
+  const size_t smem = MIXED ? (sizeof(float) * LEGS * kLegF32 + sizeof(int) * LEGS) * BLOCK
                             : (sizeof(double) * kMaxLegs * kLegF64 +
                                sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
-  auto kern = MIXED ? k_force_mixed<ENERGY, COUNT> : k_force_fp64<ENERGY, COUNT>;
+  void (*kern)(DevParams, DevState) = nullptr;
+  if constexpr (MIXED) kern = k_force_mixed<ENERGY, COUNT, LEGS>;
+  else kern = k_force_fp64<ENERGY, COUNT>;
   // the dynamic shared-memory limit is a per-device attribute of the kernel:
   // set it once on each device that launches it
   static std::atomic<unsigned long long> attr_devices{0};
@@ -800,11 +800,22 @@ cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
   if (!spec_step) k_force_begin<<<1, 32, 0, L.stream>>>(S);
   const bool mixed = P.precision == FIBMD_PREC_MIXED;
   if (mixed) {
-    if (energy) return count ? force_impl<true, true, true>(L, P, S) : force_impl<true, true, false>(L, P, S);
-    return count ? force_impl<true, false, true>(L, P, S) : force_impl<true, false, false>(L, P, S);
+    if (L.stage == kStageLarge) {
+      if (energy)
+        return count ? force_impl<true, true, true, kStageLarge>(L, P, S)
+                     : force_impl<true, true, false, kStageLarge>(L, P, S);
+      return count ? force_impl<true, false, true, kStageLarge>(L, P, S)
+                   : force_impl<true, false, false, kStageLarge>(L, P, S);
+    }
+    if (energy)
+      return count ? force_impl<true, true, true, kStageSmall>(L, P, S)
+                   : force_impl<true, true, false, kStageSmall>(L, P, S);
+    return count ? force_impl<true, false, true, kStageSmall>(L, P, S)
+                 : force_impl<true, false, false, kStageSmall>(L, P, S);
   }
-  if (energy) return count ? force_impl<false, true, true>(L, P, S) : force_impl<false, true, false>(L, P, S);
-  return count ? force_impl<false, false, true>(L, P, S) : force_impl<false, false, false>(L, P, S);
+  if (energy)
+    return count ? force_impl<false, true, true, 0>(L, P, S) : force_impl<false, true, false, 0>(L, P, S);
+  return count ? force_impl<false, false, true, 0>(L, P, S) : force_impl<false, false, false, 0>(L, P, S);
 }
 
 }  // namespace fibmd

@@ -384,11 +384,22 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
                       DevParams& P, Geo& G, char* err, int errlen);
 
 // ---- launchers (defined in the .cu files) --------------------------------
+// Staged candidates per centre in the binary32 force kernel, one of two
+// stage sizes chosen per context at run time by timing both on the current
+// state: a crystal at 300 K has 4 legs, rarely more than 6, and the small
+// stage leaves more resident warps; damaged slabs (a batch of small
+// cascades) have many centres beyond it, which the many-leg kernel then
+// takes.
+constexpr int kStageSmall = 8;
+constexpr int kStageLarge = 10;
+
 struct Launch {
   cudaStream_t stream;
   int sms;
   cudaEvent_t force_a = nullptr;  // recorded around the main force kernel
   cudaEvent_t force_b = nullptr;  // when kernel timing is on
+  int stage = kStageSmall;        // binary32 force kernel: staged candidates
+                                  // per centre (kStageSmall or kStageLarge)
 };
 
 // fibmd_nlist.cu

@@ -273,9 +273,13 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
 
 /* Options: "timers" (phase timers of fibmd_gpu_timers, default 1),
    "kernel_timing" (CUDA events around every launch of the main force
-   kernel, default 0) and "graph" (spec mode runs step pairs as one CUDA
+   kernel, default 0), "graph" (spec mode runs step pairs as one CUDA
    graph launch with device-side rebuild decisions, default 1; phase and
-   kernel timers see only the steps run outside the graph). */
+   kernel timers see only the steps run outside the graph), "autotune"
+   (mixed precision: before every 1000 spec-mode steps of a graph run, and
+   before a dose, time the binary32 force kernel's two stage sizes on the
+   current state and keep the faster, default 1) and "stage" (8 or 10
+   staged leg candidates per centre, which also turns "autotune" off). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
 
 /* Total device time (s) and number of launches of the main force kernel

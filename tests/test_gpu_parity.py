@@ -219,7 +219,8 @@ def test_regime_switch_and_parking(gpu_lib):
     assert np.abs(X - o.X).max() < TRAJ_ATOL_M
 
 
-def test_mixed_precision_force_error(gpu_lib):
+@pytest.mark.parametrize("stage", [8, 10])
+def test_mixed_precision_force_error(gpu_lib, stage):
     """binary32 force arithmetic (reduced units) against the binary64 oracle;
     the 2-body term is analytic in binary32, tabulated in the reference."""
     o = _slab()
@@ -230,6 +231,7 @@ def test_mixed_precision_force_error(gpu_lib):
     import fib_md_gb300 as fm
 
     g = fm.FibMD(p)
+    g.set_option("stage", stage)
     g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
     g.set_impact(1)
     g.si_nlist()
@@ -255,8 +257,8 @@ def _compressed_core(scale=0.8, radius_A=6.0):
     return o
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_many_leg_centres(gpu_lib, precision):
+@pytest.mark.parametrize("precision,stage", [(0, 8), (1, 8), (1, 10)])
+def test_many_leg_centres(gpu_lib, precision, stage):
     """Centres with more legs than the per-thread stage (the many-leg paths:
     the warp-per-centre kernel in binary64, the warp-cooperative epilogue of
     the binary32 kernel) against the binary64 oracle: within 1e-10 in
@@ -269,6 +271,7 @@ def test_many_leg_centres(gpu_lib, precision):
     p = o.p.copy()
     p.precision = precision
     g = fm.FibMD(p)
+    g.set_option("stage", stage)
     g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
     g.set_impact(1)
     g.si_nlist()
