@@ -259,6 +259,7 @@ def bench_ours(args, rank, world, dist):
         barrier()
         wall = time.perf_counter() - w0
     rebuilds = g.work_counters()[4] - rb0
+    stage_end = int(g.get_option("stage"))
     X_end, _, _ = g.download()
     value, t_dev, atom_steps = replica_rate(dist, float(N) * args.md_steps * args.steps,
                                             sum(times), "cuda")
@@ -370,6 +371,8 @@ def bench_ours(args, rank, world, dist):
             "atoms": N, "md_steps_per_step": args.md_steps, "mode": "spec",
             "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
             "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
+            "force_stage": "autotuned every 1000 steps between 8 and 10 staged legs; "
+                           f"{stage_end} at the end of the timed run",
             "parallelism": f"replicas x{world}", "l2": "flushed between timed steps",
         },
         "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
@@ -452,6 +455,7 @@ def bench_large(args):
         torch.cuda.synchronize()
     secs = a.elapsed_time(b) / 1e3
     rebuilds = g.work_counters()[4] - rb0
+    stage_end = int(g.get_option("stage"))
     # the main force kernel timed live over a launch-by-launch segment
     g.set_option("graph", 0)
     g.set_option("kernel_timing", 1)
@@ -477,6 +481,8 @@ def bench_large(args):
         "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
         "simulated_ps": t_sim * 1e12,
         "rebuild_fraction": rebuilds / float(args.large_steps),
+        "force_stage": "autotuned every 1000 steps between 8 and 10 staged legs; "
+                       f"{stage_end} at the end",
         "fp32_pipe": {"kernel": "k_force<mixed>", "achieved_tflops": f32, "peak_tflops": fp32_peak,
                       "frac": f32 / fp32_peak, "force_kernel_us": 1e6 * fk,
                       "peak_source": "measured in this run (FFMA loop)"},
@@ -615,9 +621,11 @@ def run_ensemble_batch(slabs, precision, steps):
     sp, dc, dp = b.impact_stats([s.surface_z for s in slabs])
     stats = [(int(sp[r]), float(dp[r]), int(dc[r])) for r in range(len(slabs))]
     atoms = int(b.natm.sum())
+    stage = int(b.get_option("stage"))
     b.close()
     return {"wall_s": wall, "atoms": atoms, "padded_atoms": int(b.N), "rebuilds": int(rebuilds),
-            "removed": removed.tolist(), "sim_time_s": t_sim.tolist(), "stats": stats}
+            "removed": removed.tolist(), "sim_time_s": t_sim.tolist(), "stats": stats,
+            "force_stage": stage}
 
 
 def run_plain(slab, steps):
@@ -691,6 +699,7 @@ def bench_ensemble(args):
                    "fp64_plain_per_impact": plain_s, "fp64_plain_sample": k},
         "atoms": mixed["atoms"], "padded_atoms": mixed["padded_atoms"],
         "rebuild_fraction": {"mixed": mixed["rebuilds"] / steps, "fp64": fp64["rebuilds"] / steps},
+        "mixed_force_stage_at_end": mixed["force_stage"],
         "mixed_vs_fp64_two_sample": cmp,
         "statistically_consistent_95": ok,
         "timing": "wall clock from upload of the initial states to the downloaded final states",

@@ -115,6 +115,7 @@ SIGNATURES = {
     "fibmd_gpu_work_counters": (_I, [_VP, _LLP]),
     "fibmd_gpu_stream": (_VP, [_VP]),
     "fibmd_gpu_set_option": (_I, [_VP, C.c_char_p, _D]),
+    "fibmd_gpu_get_option": (_I, [_VP, C.c_char_p, _DP]),
     "fibmd_gpu_kernel_time": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_phase_times": (_I, [_VP, _DP, _LLP, _I]),
     "fibmd_gpu_pipe_peaks": (_I, [_DP, _DP]),

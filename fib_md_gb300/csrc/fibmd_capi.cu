@@ -1255,6 +1255,24 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
   return FIBMD_OK;
 }
 
+int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
+  if (!ctx || !key || !value) return FIBMD_EINVAL;
+  if (!std::strcmp(key, "timers")) {
+    *value = ctx->timers_on ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "kernel_timing")) {
+    *value = ctx->kernel_timing ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "graph")) {
+    *value = ctx->use_graph ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "autotune")) {
+    *value = ctx->autotune ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "stage")) {
+    *value = (double)ctx->stage;
+  } else {
+    return fail(ctx, FIBMD_EINVAL, "unknown option '%s'", key);
+  }
+  return FIBMD_OK;
+}
+
 int fibmd_gpu_kernel_time(fibmd_ctx* ctx, double* force_kernel_s, long long* launches,
                           int reset) {
   if (!ctx) return FIBMD_EINVAL;

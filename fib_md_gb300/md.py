@@ -485,6 +485,11 @@ class FibMD:
     def set_option(self, key: str, value: float):
         self._check(self.lib.fibmd_gpu_set_option(self.h, key.encode(), float(value)), "set_option")
 
+    def get_option(self, key: str) -> float:
+        v = C.c_double()
+        self._check(self.lib.fibmd_gpu_get_option(self.h, key.encode(), C.byref(v)), "get_option")
+        return v.value
+
     def kernel_time(self, reset: bool = False):
         t = C.c_double()
         n = C.c_longlong()

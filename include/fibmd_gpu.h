@@ -281,6 +281,9 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    current state and keep the faster, default 1) and "stage" (8 or 10
    staged leg candidates per centre, which also turns "autotune" off). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
+/* The current value of an option ("stage" reads the stage size in use,
+   which "autotune" changes as the run goes). */
+int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value);
 
 /* Total device time (s) and number of launches of the main force kernel
    since the last reset, from the events of the "kernel_timing" option. */
