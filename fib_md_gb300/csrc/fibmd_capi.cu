@@ -217,6 +217,8 @@ static void list_radii(const fibmd_params& p, double* rc, double* rclj) {
   }
 }
 
+constexpr double kRemoveBelow = 10.0e-10;  // m below the lowest plane
+
 int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& G, char* err,
                int errlen) {
   std::memset(&G, 0, sizeof G);
@@ -238,6 +240,7 @@ int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& 
     G.qinvA[d] = (float)(Lb[d] * 1.0e10 / 4294967296.0);
   }
   G.remove_z = remove_z;
+  G.remove_zlo = -1.0e300;
   G.mol_reach = 1;
   if (spec) {
     // atoms above remove_z are removed, so the grid need not cover the
@@ -250,6 +253,11 @@ int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& 
       G.inv_hz = 1.0 / G.hcell[2];
       G.zcompact = 1;
       G.wrap[2] = 0;
+      // an atom that leaves through the bottom (a transmitted ion) is
+      // removed once it is beyond every interaction range of the lowest
+      // plane (z = 0), as the reference's periodic z sends it into the
+      // vacuum bands where frzsptrdatms parks it
+      G.remove_zlo = -kRemoveBelow;
     }
     const double hmin = std::min(G.hcell[0], std::min(G.hcell[1], G.hcell[2]));
     G.mol_reach = (int)std::ceil(rclj / hmin);

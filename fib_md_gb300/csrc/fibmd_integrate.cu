@@ -328,7 +328,8 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
-// remove_z, and the rebuild trigger at half the list skin.
+// remove_z (and, with an open z axis, of atoms 10 A below the lowest plane),
+// and the rebuild trigger at half the list skin.
 template <int BATCH>
 __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -366,7 +367,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
       }
       // removal looks at the unwrapped height, so an atom leaving through
       // the bottom of a periodic box is not taken for a sputtered one
-      const bool removed = G.remove_z > 0.0 && x.z > G.remove_z;
+      const bool removed = (G.remove_z > 0.0 && x.z > G.remove_z) || x.z < G.remove_zlo;
       // spec mode has no bit-compatibility constraint with the reference's
       // MOD(X + 2Lb, Lb): only atoms that left the box are wrapped, found
       // from the integer part of the fixed-point shadow (one binary64 FMA

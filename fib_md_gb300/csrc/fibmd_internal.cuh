@@ -52,6 +52,7 @@ struct Geo {
   double qscale[3];   // 2^32 / Lb
   double inv_hz;      // 1 / cell height in z (open z axis)
   double remove_z;    // spec mode: atoms above are removed (<= 0: never)
+  double remove_zlo;  // spec mode, open z axis: atoms below are removed too
   float qinvA[3];     // Lb / 2^32 in Angstrom
   int nc[3];
   int wrap[3];        // periodic cell stencil per axis (the reference: Nc > 2)

@@ -136,8 +136,10 @@ typedef struct fibmd_params {
      keeps the reference's radii (listfac 1.1). Spec mode always finds every
      Moliere pair (the reference's 27-cell stencil misses those beyond one
      cell). With remove_z > 0 (and remove_z + list radius < Lb(3)) spec mode
-     treats z as an open axis: positions are not wrapped in z and the cell
-     grid covers [0, remove_z + list radius) only. */
+     treats z as an open axis: positions are not wrapped in z, the cell
+     grid covers [0, remove_z + list radius) only, and an atom more than
+     10 A below z = 0 (a transmitted ion) is removed like one above
+     remove_z. */
   double list_skin;
 
   /* capacities; 0 = defaults */

@@ -208,3 +208,32 @@ def test_nonfinite_state_is_reported(gpu_lib, mode):
     g.si_force()
     g.steps(2, 4, 0, 0.0, 300.0)
     g.close()
+
+
+def test_transmitted_ion_is_removed(gpu_lib):
+    """With an open z axis an ion that leaves through the bottom of the slab
+    is removed once it is 10 A below the lowest plane (z = 0), as an atom
+    above remove_z is: its depth below the surface turns from a number to
+    NaN (fibmd_gpu_impact_stats)."""
+    import fib_md_gb300 as fm
+
+    s, X, V = _spec_system(nc=(4, 4, 3), seed=21)
+    nsg = s.params.Nsg
+    p = _spec_params(s, 0.3, 12.0)
+    # the ion 2 A below the lowest plane, moving down at 5 km/s: the step is
+    # capped at 1 fs, 0.05 A per step, so it passes -10 A after ~160 steps
+    X[nsg] = [0.5 * p.Lb[0], 0.5 * p.Lb[1], -2.0e-10]
+    V[nsg] = [0.0, 0.0, -5.0e3]
+    g = fm.FibMD(p)
+    g.upload(X, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
+    surf = float(X[:nsg, 2].max())
+    _, _, depth = g.impact_stats([surf])
+    assert np.isfinite(depth[0]) and depth[0] > surf
+    g.steps(2, 300, 0, 0.0, 300.0)
+    _, _, depth = g.impact_stats([surf])
+    assert np.isnan(depth[0])
+    Xf, _, _ = g.download()
+    assert (Xf[:nsg, 2] > -10e-10).all()  # the lattice stays
