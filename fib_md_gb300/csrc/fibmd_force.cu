@@ -160,7 +160,9 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
       if (k0 + u >= n) break;
       const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-      if (r2f > P.pre3A2) continue;  // beyond the table support and 3-body cutoff
+      // beyond the table support and 3-body cutoff, or removed (spec mode:
+      // a removed atom acts on nothing from the step it leaves)
+      if (r2f > P.pre3A2 || ((qq[u].w >> 8) & FL_REMOVED)) continue;
       const int tb = (qq[u].w & 0xff) - 1;
       if (nc < kCandF64) cand[nc++ * kBlock64 + threadIdx.x] = jj[u] | (tb << 30);
       else neighbour(jj[u], tb);
@@ -345,7 +347,7 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
       if (k0 + u >= n) break;
       const float3 dq = qsep(qi, qq[u], qinvA);
       const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-      if (r2f > P.pre3mA2) continue;
+      if (r2f > P.pre3mA2 || ((qq[u].w >> 8) & FL_REMOVED)) continue;
       const int tb = (qq[u].w & 0xff) - 1;
       if (r2f <= P.pre3lA2 && nc < LEGS) {
         sA[nc * kBlock32 + t] = make_float4(dq.x, dq.y, dq.z, r2f);
@@ -525,6 +527,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     for (int k = lane; k < n; k += 32) {
       const int j = S.nbr_sw[(size_t)k * P.N + c];
       const int tj = S.atype[j];
+      if (S.flags[j] & FL_REMOVED) continue;
       if constexpr (MIXED) {
         const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
         const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
@@ -696,6 +699,7 @@ __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevSta
     // si_force skips unfired ions (si.f90:428); si_potential does not
     const bool fired = i < P.nfired && j < P.nfired;
     if (!ENERGY && !fired) continue;
+    if ((S.flags[i] | S.flags[j]) & FL_REMOVED) continue;
     const int ti = S.atype[i] - 1, tj = S.atype[j] - 1;
     const double4_32a pi = S.pos[i], pj = S.pos[j];
     const Geo& G = S.geo[rep_of_flags(S.flags[i])];

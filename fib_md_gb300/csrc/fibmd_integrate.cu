@@ -384,10 +384,11 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
         }
       }
       if (removed) {
+        // the force kernels skip removed neighbours, so the lists need no
+        // rebuild for it
         fl |= FL_REMOVED;
         S.flags[i] = fl;
         v.x = v.y = v.z = 0.0;
-        trig = true;
         atomicAdd(at < 3 ? &R->removed_count : &R->ions_removed, 1);
       }
       S.pos[i] = x;
@@ -396,7 +397,7 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
                                posq_w(at, fl));
       S.posq[i] = q;
       const float3 d = qsep(q, qb, G.qinvA);
-      if (d.x * d.x + d.y * d.y + d.z * d.z >= P.disp_fastA2) trig = true;
+      if (!removed && d.x * d.x + d.y * d.y + d.z * d.z >= P.disp_fastA2) trig = true;
     }
   }
   const bool any = __syncthreads_or(trig);

@@ -237,3 +237,57 @@ def test_transmitted_ion_is_removed(gpu_lib):
     assert np.isnan(depth[0])
     Xf, _, _ = g.download()
     assert (Xf[:nsg, 2] > -10e-10).all()  # the lattice stays
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("which", ["lattice", "ion"])
+def test_removed_neighbour_exerts_no_force(gpu_lib, precision, which):
+    """An atom removed while it is still in its neighbours' lists (tagged
+    after the list build) acts on nothing: the other atoms' forces equal
+    those with the atom far away before the lists are built. A lattice atom
+    inside the slab (SW pairs and angle terms), or the ion next to the
+    surface (Moliere pairs)."""
+    import fib_md_gb300 as fm
+
+    s, X, V = _spec_system(nc=(4, 4, 3), seed=23)
+    nsg = s.params.Nsg
+    rs = np.random.default_rng(5)
+    X[:nsg] += rs.normal(scale=0.08e-10, size=(nsg, 3))
+    p = _spec_params(s, 0.3, 12.0)
+    p.precision = precision
+    surf = float(X[:nsg, 2].max())
+    if which == "lattice":
+        mid = np.array([0.5 * p.Lb[0], 0.5 * p.Lb[1], 0.5 * surf])
+        k = int(np.argmin(np.sum((X[:nsg] - mid) ** 2, axis=1)))
+    else:
+        k = nsg
+        top = np.argmax(X[:nsg, 2])
+        X[k] = X[top] + np.array([0.4e-10, 0.3e-10, 1.4e-10])
+    tags = np.zeros(p.Natm, dtype=np.uint32)
+    tags[k] = fm.TAG_REMOVED
+    forces = []
+    for far in (False, True):
+        Xc = X.copy(order="F")
+        if far:
+            Xc[k] = [0.5 * p.Lb[0], 0.5 * p.Lb[1], surf + 10e-10]
+        g = fm.FibMD(p)
+        g.upload(Xc, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+        g.set_impact(1)
+        if far:
+            g.set_tags(tags)
+        g.si_nlist()
+        if not far:
+            assert g.list_counts()[0] > 0
+            g.set_tags(tags)  # removed after the lists were built
+        forces.append(g.si_force())
+    keep = np.arange(p.Natm) != k
+    FA, FB = forces[0][keep], forces[1][keep]
+    tol = 1e-10 if precision == 0 else 1e-5
+    assert np.abs(FA - FB).max() <= tol * np.abs(FB).max()
+    # and the removed atom did act before its removal
+    g = fm.FibMD(p)
+    g.upload(X, V, None, s.Xi, s.mass, s.atype, np.zeros_like(s.xsides))
+    g.set_impact(1)
+    g.si_nlist()
+    F0 = g.si_force()[keep]
+    assert np.abs(F0 - FB).max() > 1e3 * tol * np.abs(FB).max()
