@@ -495,14 +495,17 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
   return true;
 }
 
-// Centres with more than kMaxLegs active legs (compressed cascade regions):
-// one warp per centre. The lanes first compute every listed leg (binary64,
-// or binary32 in mixed precision) and stage the active ones in shared
-// memory, then take legs as rows: a lane sums its leg's reaction over every
-// other leg in registers and scatters it once. Each angle term is evaluated
-// in both of its rows, which costs less than splitting the pairs over the
-// lanes: that needs shared-memory atomics on the leg sums, and lanes sharing
-// a leg serialise on them. The centre's force is warp-reduced.
+// Centres with more than kMaxLegs active legs (compressed cascade regions,
+// damaged slabs): a group of lanes per centre, 8 in binary32 (four centres
+// per warp) and the whole warp in binary64 (whose leg stage is twice the
+// size). The group first computes every listed leg and stages the active
+// ones in shared memory, then takes legs as rows: a lane sums its leg's
+// reaction over every other leg in registers and scatters it once. Each
+// angle term is evaluated in both of its rows, which costs less than
+// splitting the pairs over the lanes (shared-memory atomics on the leg sums,
+// on which lanes sharing a leg serialise). A centre has ~10-30 legs, so 8
+// lanes keep busy where a warp would leave most of its lanes idle; the
+// centre's force is reduced over the group.
 constexpr int kHeavyWarps = 4;
 constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
@@ -510,77 +513,87 @@ template <bool MIXED, bool ENERGY>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
   // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
   using R = typename std::conditional<MIXED, float, double>::type;
-  __shared__ R sl[kHeavyWarps][6][kHeavyLegs];
-  __shared__ int sj[kHeavyWarps][kHeavyLegs];
-  __shared__ int snl[kHeavyWarps];
+  constexpr int GROUP = MIXED ? 8 : 32;  // lanes per centre
+  constexpr int GPW = 32 / GROUP;        // centres per warp
+  constexpr int NG = kHeavyWarps * GPW;  // centres per block
+  __shared__ R sl[NG][6][kHeavyLegs];
+  __shared__ int sj[NG][kHeavyLegs];
+  __shared__ int snl[NG];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gl = lane % GROUP;               // lane within the group
+  const int sg = w * GPW + lane / GROUP;     // the group's stage
   const int cnt = *((volatile int*)&S.sc->heavy_count);
   const double conv = MIXED ? P.f_evA_to_N : 1.0;
   const double econv = MIXED ? P.e_eV_to_J : 1.0;
-  for (int h = blockIdx.x * kHeavyWarps + w; h < cnt; h += gridDim.x * kHeavyWarps) {
-    const int c = S.heavy_list[h];
-    const int tc = S.atype[c];
-    const int n = S.n_sw[c];
-    const Geo& G = S.geo[rep_of_flags(S.flags[c])];
-    if (lane == 0) snl[w] = 0;
+  // warp-uniform loop: every lane takes part in the group reductions
+  for (int base = (blockIdx.x * kHeavyWarps + w) * GPW; base < cnt;
+       base += gridDim.x * kHeavyWarps * GPW) {
+    const int h = base + lane / GROUP;
+    const int c = h < cnt ? S.heavy_list[h] : -1;
+    if (gl == 0) snl[sg] = 0;
     __syncwarp();
-    for (int k = lane; k < n; k += 32) {
-      const int j = S.nbr_sw[(size_t)k * P.N + c];
-      const int tj = S.atype[j];
-      if (S.flags[j] & FL_REMOVED) continue;
-      if constexpr (MIXED) {
-        const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
-        const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-        const float rinv = rsqrtf(r2);
-        const float is = P.isigA[tc - 1][tj - 1];
-        const float u = r2 * rinv * is;
-        if (!(u < (float)P.cut3)) continue;
-        const float ia = __frcp_rn(u - (float)P.al);
-        const float E = expf((float)P.gam * ia);
-        if (!(E > kLegEmin)) continue;
-        const int q = atomicAdd(&snl[w], 1);
-        sl[w][0][q] = dq.x * rinv;
-        sl[w][1][q] = dq.y * rinv;
-        sl[w][2][q] = dq.z * rinv;
-        sl[w][3][q] = rinv;
-        sl[w][4][q] = E;
-        sl[w][5][q] = -(float)P.gam * ia * ia * is;
-        sj[w][q] = j | ((tj - 1) << 30);
-      } else {
-        const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);
-        if (!(L.u < P.cut3)) continue;
-        const int q = atomicAdd(&snl[w], 1);
-        const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
-        sl[w][0][q] = L.dx * ra;
-        sl[w][1][q] = L.dy * ra;
-        sl[w][2][q] = L.dz * ra;
-        sl[w][3][q] = ra;
-        sl[w][4][q] = exp(P.gam * ia);
-        sl[w][5][q] = -P.gam * ia * ia * L.isig;
-        sj[w][q] = j | (L.t << 30);
+    int tc = 1;
+    if (c >= 0) {
+      tc = S.atype[c];
+      const int n = S.n_sw[c];
+      const Geo& G = S.geo[rep_of_flags(S.flags[c])];
+      for (int k = gl; k < n; k += GROUP) {
+        const int j = S.nbr_sw[(size_t)k * P.N + c];
+        const int tj = S.atype[j];
+        if (S.flags[j] & FL_REMOVED) continue;
+        if constexpr (MIXED) {
+          const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
+          const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+          const float rinv = rsqrtf(r2);
+          const float is = P.isigA[tc - 1][tj - 1];
+          const float u = r2 * rinv * is;
+          if (!(u < (float)P.cut3)) continue;
+          const float ia = __frcp_rn(u - (float)P.al);
+          const float E = expf((float)P.gam * ia);
+          if (!(E > kLegEmin)) continue;
+          const int q = atomicAdd(&snl[sg], 1);
+          sl[sg][0][q] = dq.x * rinv;
+          sl[sg][1][q] = dq.y * rinv;
+          sl[sg][2][q] = dq.z * rinv;
+          sl[sg][3][q] = rinv;
+          sl[sg][4][q] = E;
+          sl[sg][5][q] = -(float)P.gam * ia * ia * is;
+          sj[sg][q] = j | ((tj - 1) << 30);
+        } else {
+          const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);
+          if (!(L.u < P.cut3)) continue;
+          const int q = atomicAdd(&snl[sg], 1);
+          const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
+          sl[sg][0][q] = L.dx * ra;
+          sl[sg][1][q] = L.dy * ra;
+          sl[sg][2][q] = L.dz * ra;
+          sl[sg][3][q] = ra;
+          sl[sg][4][q] = exp(P.gam * ia);
+          sl[sg][5][q] = -P.gam * ia * ia * L.isig;
+          sj[sg][q] = j | (L.t << 30);
+        }
       }
     }
     __syncwarp();
-    const int nl = snl[w];
+    const int nl = snl[sg];
     // rows: lane sums leg a's reaction over every other leg b in registers
-    // (each term evaluated in both of its rows; no shared-memory atomics)
     R fcx = 0, fcy = 0, fcz = 0, uc = 0;
     const R thrd = (R)P.thrd;
-    for (int a = lane; a < nl; a += 32) {
-      const R ax = sl[w][0][a], ay = sl[w][1][a], az = sl[w][2][a];
-      const R ar = sl[w][3][a], aE = sl[w][4][a], ag = sl[w][5][a];
-      const int ja = sj[w][a];
+    for (int a = gl; a < nl; a += GROUP) {
+      const R ax = sl[sg][0][a], ay = sl[sg][1][a], az = sl[sg][2][a];
+      const R ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
+      const int ja = sj[sg][a];
       R afx = 0, afy = 0, afz = 0, ae = 0;
       for (int b = 0; b < nl; b++) {
         if (b == a) continue;
-        const R bx = sl[w][0][b], by = sl[w][1][b], bz = sl[w][2][b];
-        const int jb = sj[w][b];
+        const R bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
+        const int jb = sj[sg][b];
         const R cs = ax * bx + ay * by + az * bz;
         const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
         R lp;
         if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-        const R pref = lp * aE * sl[w][4][b];
+        const R pref = lp * aE * sl[sg][4][b];
         const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
         afx += pref * (wa * ax + sa * bx);
         afy += pref * (wa * ay + sa * by);
@@ -597,11 +610,17 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     }
     // the centre's third of each term, counted in both rows
     if (ENERGY) uc /= (R)6;
-    const double dcx = warp_sum(conv * (double)fcx);
-    const double dcy = warp_sum(conv * (double)fcy);
-    const double dcz = warp_sum(conv * (double)fcz);
-    const double duc = ENERGY ? warp_sum(econv * (double)uc) : 0.0;
-    if (lane == 0) {
+    __syncwarp();
+    double dcx = conv * (double)fcx, dcy = conv * (double)fcy, dcz = conv * (double)fcz;
+    double duc = ENERGY ? econv * (double)uc : 0.0;
+#pragma unroll
+    for (int o = GROUP / 2; o > 0; o >>= 1) {
+      dcx += __shfl_xor_sync(0xffffffffu, dcx, o);
+      dcy += __shfl_xor_sync(0xffffffffu, dcy, o);
+      dcz += __shfl_xor_sync(0xffffffffu, dcz, o);
+      if (ENERGY) duc += __shfl_xor_sync(0xffffffffu, duc, o);
+    }
+    if (gl == 0 && c >= 0) {
       atomic_add3(S.frc_new, c, dcx, dcy, dcz);
       if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
     }
@@ -781,9 +800,9 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   if (!MIXED) k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
-  // one warp per many-leg centre; the count is known only on the device, so
-  // the grid covers thousands of centres (cascade cores of a batch) in one
-  // round and idle warps return at once
+  // a group of lanes per many-leg centre; the count is known only on the
+  // device, so the grid covers thousands of centres (cascade cores of a
+  // batch) in one round and idle warps return at once
   const int heavy_blocks = std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
   k_force_heavy<MIXED, ENERGY><<<heavy_blocks, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
