@@ -291,3 +291,32 @@ def test_removed_neighbour_exerts_no_force(gpu_lib, precision, which):
     g.si_nlist()
     F0 = g.si_force()[keep]
     assert np.abs(F0 - FB).max() > 1e3 * tol * np.abs(FB).max()
+
+
+def test_force_stage_switch_and_autotune(gpu_lib):
+    """Mixed precision: the force kernel's stage size (8 or 10 staged legs)
+    changed between graph runs recaptures the step graph; the run matches
+    one at a fixed stage (the stage only moves centres between the main and
+    the many-leg kernel: binary32 sums in another order). With autotune on,
+    the stage in use is one of the two."""
+    s, X, V = _spec_system(precision=1)
+    a = _ctx(s, X, V, 1)
+    b = _ctx(s, X, V, 1)
+    a.set_option("stage", 8)
+    b.set_option("stage", 8)
+    a.steps(2, 60, 0, 0.0, 300.0)
+    b.steps(2, 60, 0, 0.0, 300.0)
+    a.set_option("stage", 10)
+    assert a.get_option("stage") == 10 and a.get_option("autotune") == 0
+    la, ta, _, _ = a.steps(2, 60, 60, 0.0, 300.0)
+    lb, tb, _, _ = b.steps(2, 60, 60, 0.0, 300.0)
+    assert la == lb == 120
+    Xa, _, _ = a.download()
+    Xb, _, _ = b.download()
+    assert np.isfinite(Xa).all()
+    assert np.abs(Xa - Xb).max() < 1e-15  # 1e-5 A after 120 steps of a 2 keV cascade
+    c = _ctx(s, X, V, 1)
+    c.set_option("autotune", 1)
+    c.steps(2, 1200, 0, 0.0, 300.0)  # tunes before each 1000 steps
+    assert c.get_option("stage") in (8, 10)
+    assert c.get_option("autotune") == 1
