@@ -71,10 +71,12 @@ def parse():
                     help="impacts of its binary64 counterpart (default: as many)")
     ap.add_argument("--large-steps", type=int, default=20000,
                     help="MD steps of the 1,048,577-atom 30 keV cascade (0: skip)")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step"], default=None,
+    ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step", "ensemble"],
+                    default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64), "
-                         "rebuild the lists 5 times (build) or run 10 mixed steps launch "
-                         "by launch (step), exit (for ncu)")
+                         "rebuild the lists 5 times (build), run 10 mixed steps launch "
+                         "by launch (step), or run the 256-impact ensemble 1000 steps as "
+                         "graphs and 20 launch by launch (ensemble), exit (for ncu)")
     return ap.parse_args()
 
 
@@ -831,6 +833,25 @@ def main():
                "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
+        return 0
+
+    if args.profile == "ensemble":
+        import fib_md_gb300 as fm
+
+        slabs = make_ensemble(256, fm.PREC_MIXED, list_skin_A=args.list_skin)
+        p = slabs[0].params.copy()
+        reps = [(s.params.Natm, s.params.Nsg, list(s.params.Lb), s.params.remove_z) for s in slabs]
+        b = fm.FibMDBatch(p, reps)
+        b.upload(b.pad([s.X for s in slabs]), b.pad([s.V for s in slabs]), None,
+                 b.pad([s.Xi for s in slabs]), b.pad([s.mass for s in slabs], fill=1.0),
+                 b.pad([s.atype for s in slabs], fill=1, dtype=np.int32), np.zeros(b.N, np.int32))
+        b.set_tags(b.pad([s.tags for s in slabs], fill=0, dtype=np.uint32))
+        b.si_nlist()
+        b.si_force()
+        lt, t, _, _ = b.steps(2, 1000, 0, 0.0, 300.0)
+        b.set_option("graph", 0)
+        b.steps(2, 20, lt, t, 300.0)
+        b.close()
         return 0
 
     if args.profile:
