@@ -224,14 +224,15 @@ __device__ __forceinline__ bool exact_in(const Geo& G, const DevState& S, int i,
 // both atoms' lists. The lanes of a warp hold the atoms of a few x-adjacent
 // cells and walk nearly the same rows; a row of x-adjacent cells is one run
 // of the cell-sorted arrays (two where it wraps in x). Candidates are tested
-// in binary32 on the fixed-point separations; within 1e-4 of a radius the
-// reference's binary64 test decides. Accepted pairs are buffered in shared
-// memory and entered afterwards: the centre's own entries with one atomic
-// reservation, each partner's with one atomic slot. A pair with an ion goes
+// in binary32 on the fixed-point separations; those inside the prefilter
+// are buffered in shared memory and resolved after the scan (within 1e-4
+// of a radius the reference's binary64 test decides), and the accepted
+// pairs entered: the centre's own entries with one atomic reservation, each
+// partner's with one atomic slot. A pair with an ion goes
 // to the Moliere pair list in both orders; with WIDE (spec mode) the ion
 // scan below lists those and ions are skipped here.
 constexpr int kBuildThreads = 128;
-constexpr int kBuildBuf = 24;  // buffered pairs per atom
+constexpr int kBuildBuf = 24;  // buffered candidates per atom
 
 // A slot in atom x's list, or -1 (counted) when the list is full; the count
 // ends at min(entries, max_sw) whatever the order of the atomics.
@@ -247,7 +248,8 @@ template <bool WIDE>
 __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, DevState S,
                                                                    int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  __shared__ int buf[kBuildBuf][kBuildThreads];
+  __shared__ int buf[kBuildBuf][kBuildThreads];     // candidate slots, then partners
+  __shared__ float bufr[kBuildBuf][kBuildThreads];  // their binary32 r^2 (A^2)
   const int t = threadIdx.x;
   const int h = blockIdx.x * kBuildThreads + t;
   if (h >= S.cell_start[P.ncell]) return;
@@ -255,7 +257,7 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
   const int4 qi = S.posq_cell[h];
   const int ti = qi.w & 0xff;
   const size_t stride = (size_t)P.N;
-  int n = 0;  // accepted SW pairs
+  int n = 0;  // buffered candidates, then accepted SW partners
   if (!(WIDE && ti == 3)) {
     const Geo& G = S.geo[rep_of_w(qi.w)];
     const int c = S.atom_cell[i] - G.cell_off;
@@ -276,11 +278,47 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
       xa0 = max(cx - 1, 0);
       xa1 = min(cx + 1, nx - 1);
     }
-    const float thr_sw = P.pre_sw2A;
     // binary32 bound of any listed pair of this atom
     const float thr = WIDE ? P.pre_sw2A : fmaxf(P.pre_sw2A, P.pre_mol2A);
     const int4* __restrict__ qc = S.posq_cell;
-    // candidate runs: [b, e) of the cell-sorted arrays
+    // The buffered candidates: the exact test where the prefilter is not
+    // conclusive, Moliere pairs (reference mode) to their list, accepted SW
+    // partners compacted to the front of buf as atom indices (direct:
+    // entered at once instead). Returns the number compacted.
+    auto resolve = [&](int nc, bool direct) -> int {
+      int na = 0;
+      for (int k = 0; k < nc; k++) {
+        const int p = buf[k][t];
+        const float r2f = bufr[k][t];
+        const int j = __ldg(&S.cell_atoms[p]);
+        bool sw = true;
+        if (!WIDE) {
+          const int tj = __ldg(&qc[p].w) & 0xff;
+          sw = (ti > tj ? ti : tj) < 3;
+          if (sw && r2f > P.pre_sw2A) continue;
+        }
+        if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) && !exact_in(G, S, i, j, sw ? P.rv2 : P.rv2lj))
+          continue;
+        if (!sw) {
+          const int slot = atomicAdd(&S.sc->mol_count, 2);
+          if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
+          if (slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
+        } else if (direct) {
+          const int si = list_slot(P, S, i);
+          if (si >= 0) S.nbr_sw[(size_t)si * stride + i] = j;
+          const int sj = list_slot(P, S, j);
+          if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
+        } else {
+          buf[na][t] = j;
+          na++;
+        }
+      }
+      return na;
+    };
+    // candidate runs: [b, e) of the cell-sorted arrays. Candidates inside
+    // the prefilter are buffered by predicated stores, so the lanes of a
+    // warp stay converged through the scan (about one candidate in eight
+    // passes it); a nearly full buffer is resolved at once.
     auto scan = [&](int b, int e) {
       for (int p0 = b; p0 < e; p0 += 4) {
         int4 qq[4];
@@ -288,39 +326,18 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
         for (int u = 0; u < 4; u++) qq[u] = __ldg(&qc[min(p0 + u, e - 1)]);
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-          const int p = p0 + u;
-          if (p >= e) break;
-          const int4 qj = qq[u];
-          const float3 d = qsep(qi, qj, qinvA);
+          const float3 d = qsep(qi, qq[u], qinvA);
           const float r2f = fmaf(d.z, d.z, fmaf(d.y, d.y, d.x * d.x));
-          if (r2f > thr) continue;
-          // rare from here on: inside the larger prefilter sphere
-          bool sw = true;
-          if (!WIDE) {
-            const int tj = qj.w & 0xff;
-            sw = (ti > tj ? ti : tj) < 3;
-            if (sw && r2f > thr_sw) continue;
+          const bool in = r2f <= thr && p0 + u < e;
+          if (in) {
+            buf[n][t] = p0 + u;
+            bufr[n][t] = r2f;
           }
-          if (r2f >= (sw ? P.acc_sw2A : P.acc_mol2A) &&
-              !exact_in(G, S, i, __ldg(&S.cell_atoms[p]), sw ? P.rv2 : P.rv2lj))
-            continue;
-          if (sw) {
-            if (n < kBuildBuf) {
-              buf[n][t] = p;
-            } else {
-              const int j = __ldg(&S.cell_atoms[p]);
-              const int si = list_slot(P, S, i);
-              if (si >= 0) S.nbr_sw[(size_t)si * stride + i] = j;
-              const int sj = list_slot(P, S, j);
-              if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
-            }
-            n++;
-          } else {
-            const int j = __ldg(&S.cell_atoms[p]);
-            const int slot = atomicAdd(&S.sc->mol_count, 2);
-            if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
-            if (slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
-          }
+          n += in;
+        }
+        if (n > kBuildBuf - 4) {  // room for the next four
+          resolve(n, true);
+          n = 0;
         }
       }
     };
@@ -346,10 +363,11 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
       scan(S.cell_start[row + xa0], S.cell_start[row + xa1 + 1]);
       if (xb1 >= xb0) scan(S.cell_start[row + xb0], S.cell_start[row + xb1 + 1]);
     }
+    n = resolve(n, false);
   }
-  // enter the buffered pairs: the centre's entries in one reservation, then
-  // the partners' (independent atomics, several in flight)
-  const int nb = min(n, kBuildBuf);
+  // enter the accepted partners: the centre's entries in one reservation,
+  // then the partners' (independent atomics, several in flight)
+  const int nb = n;
   if (nb > 0) {
     int base = atomicAdd(&S.n_sw[i], nb);
     int keep = min(nb, max(0, P.max_sw - base));
@@ -358,7 +376,7 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
       atomicAdd(&S.sc->overflow_sw, 1);
     }
     for (int k = 0; k < nb; k++) {
-      const int j = S.cell_atoms[buf[k][t]];
+      const int j = buf[k][t];
       if (k < keep) S.nbr_sw[(size_t)(base + k) * stride + i] = j;
       const int sj = list_slot(P, S, j);
       if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
