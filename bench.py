@@ -373,7 +373,8 @@ def bench_ours(args, rank, world, dist):
             "atoms": N, "md_steps_per_step": args.md_steps, "mode": "spec",
             "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
             "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
-            "force_stage": "autotuned every 1000 steps between 8 and 10 staged legs; "
+            "force_stage": "autotuned every 1000 steps among 8 or 10 staged legs per "
+                           "thread and 8 lanes per centre (1); "
                            f"{stage_end} at the end of the timed run",
             "parallelism": f"replicas x{world}", "l2": "flushed between timed steps",
         },
@@ -407,12 +408,15 @@ def bench_ours(args, rank, world, dist):
                           "moliere_pairs": counts[2], "stale_terms": counts[3],
                           "many_leg_centres": counts[5]},
         # per MD step: drift, rebuild condition, force (main with the Moliere
-        # blocks, many-leg), kick, kick reduction = 6; per step pair the loop
-        # control; 9 kernels per list rebuild; the loop set-up per bench step.
-        # Launch by launch: the 9 list kernels every step (they return at once
-        # when no rebuild is due), no condition or loop kernels
-        "gpu_launches": int(14 * args.md_steps * args.steps if args.no_graph else
-                            6.5 * args.md_steps * args.steps + 9 * rebuilds + args.steps),
+        # blocks, many-leg; one kernel on the 8-lanes-per-centre path), kick,
+        # kick reduction = 6; per step pair the loop control; 9 kernels per
+        # list rebuild; the loop set-up per bench step. Launch by launch: the
+        # 9 list kernels every step (they return at once when no rebuild is
+        # due), no condition or loop kernels
+        "gpu_launches": int((14 if stage_end != 1 else 13) * args.md_steps * args.steps
+                            if args.no_graph else
+                            (6.5 if stage_end != 1 else 5.5) * args.md_steps * args.steps +
+                            9 * rebuilds + args.steps),
         "rebuild_fraction": rebuilds / float(args.md_steps * args.steps),
         "wall_s_timed": wall,
         "clocks": clk.summary(),
@@ -483,7 +487,8 @@ def bench_large(args):
         "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
         "simulated_ps": t_sim * 1e12,
         "rebuild_fraction": rebuilds / float(args.large_steps),
-        "force_stage": "autotuned every 1000 steps between 8 and 10 staged legs; "
+        "force_stage": "autotuned every 1000 steps among 8 or 10 staged legs per thread "
+                       "and 8 lanes per centre (1); "
                        f"{stage_end} at the end",
         "fp32_pipe": {"kernel": "k_force<mixed>", "achieved_tflops": f32, "peak_tflops": fp32_peak,
                       "frac": f32 / fp32_peak, "force_kernel_us": 1e6 * fk,

@@ -1253,8 +1253,9 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
   } else if (!std::strcmp(key, "autotune")) {
     ctx->autotune = value != 0.0;
   } else if (!std::strcmp(key, "stage")) {
-    if (value != kStageSmall && value != kStageLarge)
-      return fail(ctx, FIBMD_EINVAL, "stage must be %d or %d", kStageSmall, kStageLarge);
+    if (value != kStageSmall && value != kStageLarge && value != kStageGroup)
+      return fail(ctx, FIBMD_EINVAL, "stage must be %d, %d or %d", kStageSmall, kStageLarge,
+                  kStageGroup);
     ctx->stage = (int)value;
     ctx->autotune = false;
   } else {
@@ -1441,9 +1442,9 @@ static int tune_stage(fibmd_ctx* ctx) {
   if (ctx->P.precision != FIBMD_PREC_MIXED || !ctx->autotune || !ctx->lists_built)
     return FIBMD_OK;
   cudaEvent_t a = get_event(ctx), b = get_event(ctx);
-  const int stages[2] = {kStageSmall, kStageLarge};
-  float ms[2] = {0.f, 0.f};
-  for (int q = 0; q < 2; q++) {
+  const int stages[3] = {kStageSmall, kStageLarge, kStageGroup};
+  float ms[3] = {0.f, 0.f, 0.f};
+  for (int q = 0; q < 3; q++) {
     Launch L = launch_of(ctx);
     L.stage = stages[q];
     CK(launch_force(L, ctx->P, ctx->S, false, false, false));
@@ -1456,8 +1457,12 @@ static int tune_stage(fibmd_ctx* ctx) {
   ctx->pool.push_back(a);
   ctx->pool.push_back(b);
   // switch only for a clear gain: a switch recaptures the step graph
-  const int cur = ctx->stage == kStageLarge ? 1 : 0;
-  if (ms[1 - cur] < 0.97f * ms[cur]) ctx->stage = stages[1 - cur];
+  int cur = 0, best = 0;
+  for (int q = 0; q < 3; q++) {
+    if (stages[q] == ctx->stage) cur = q;
+    if (ms[q] < ms[best]) best = q;
+  }
+  if (ms[best] < 0.97f * ms[cur]) ctx->stage = stages[best];
   return FIBMD_OK;
 }
 

@@ -537,40 +537,56 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
       tc = S.atype[c];
       const int n = S.n_sw[c];
       const Geo& G = S.geo[rep_of_flags(S.flags[c])];
-      for (int k = gl; k < n; k += GROUP) {
-        const int j = S.nbr_sw[(size_t)k * P.N + c];
-        const int tj = S.atype[j];
-        if (S.flags[j] & FL_REMOVED) continue;
-        if constexpr (MIXED) {
-          const float3 dq = qsep(S.posq[c], S.posq[j], G.qinvA);
-          const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
-          const float rinv = rsqrtf(r2);
-          const float is = P.isigA[tc - 1][tj - 1];
-          const float u = r2 * rinv * is;
-          if (!(u < (float)P.cut3)) continue;
-          const float ia = __frcp_rn(u - (float)P.al);
-          const float E = expf((float)P.gam * ia);
-          if (!(E > kLegEmin)) continue;
-          const int q = atomicAdd(&snl[sg], 1);
-          sl[sg][0][q] = dq.x * rinv;
-          sl[sg][1][q] = dq.y * rinv;
-          sl[sg][2][q] = dq.z * rinv;
-          sl[sg][3][q] = rinv;
-          sl[sg][4][q] = E;
-          sl[sg][5][q] = -(float)P.gam * ia * ia * is;
-          sj[sg][q] = j | ((tj - 1) << 30);
-        } else {
-          const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);
-          if (!(L.u < P.cut3)) continue;
-          const int q = atomicAdd(&snl[sg], 1);
-          const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
-          sl[sg][0][q] = L.dx * ra;
-          sl[sg][1][q] = L.dy * ra;
-          sl[sg][2][q] = L.dz * ra;
-          sl[sg][3][q] = ra;
-          sl[sg][4][q] = exp(P.gam * ia);
-          sl[sg][5][q] = -P.gam * ia * ia * L.isig;
-          sj[sg][q] = j | (L.t << 30);
+      const int4 qc = S.posq[c];
+      // three neighbours per lane in flight
+      constexpr int kG = 3;
+      for (int k0 = gl; k0 < n; k0 += kG * GROUP) {
+        int jj[kG];
+        int4 qq[kG];
+#pragma unroll
+        for (int u = 0; u < kG; u++) {
+          const int k = k0 + u * GROUP;
+          jj[u] = k < n ? S.nbr_sw[(size_t)k * P.N + c] : c;
+        }
+#pragma unroll
+        for (int u = 0; u < kG; u++) qq[u] = S.posq[jj[u]];
+#pragma unroll
+        for (int u = 0; u < kG; u++) {
+          if (k0 + u * GROUP >= n) break;
+          const int j = jj[u];
+          const int tj = qq[u].w & 0xff;
+          if ((qq[u].w >> 8) & FL_REMOVED) continue;
+          if constexpr (MIXED) {
+            const float3 dq = qsep(qc, qq[u], G.qinvA);
+            const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+            const float rinv = rsqrtf(r2);
+            const float is = P.isigA[tc - 1][tj - 1];
+            const float ue = r2 * rinv * is;
+            if (!(ue < (float)P.cut3)) continue;
+            const float ia = __frcp_rn(ue - (float)P.al);
+            const float E = expf((float)P.gam * ia);
+            if (!(E > kLegEmin)) continue;
+            const int q = atomicAdd(&snl[sg], 1);
+            sl[sg][0][q] = dq.x * rinv;
+            sl[sg][1][q] = dq.y * rinv;
+            sl[sg][2][q] = dq.z * rinv;
+            sl[sg][3][q] = rinv;
+            sl[sg][4][q] = E;
+            sl[sg][5][q] = -(float)P.gam * ia * ia * is;
+            sj[sg][q] = j | ((tj - 1) << 30);
+          } else {
+            const Leg64 L = make_leg(P, G, S.pos[c], S.pos[j], tc, tj);
+            if (!(L.u < P.cut3)) continue;
+            const int q = atomicAdd(&snl[sg], 1);
+            const double ra = 1.0 / L.r, ia = 1.0 / (L.u - P.al);
+            sl[sg][0][q] = L.dx * ra;
+            sl[sg][1][q] = L.dy * ra;
+            sl[sg][2][q] = L.dz * ra;
+            sl[sg][3][q] = ra;
+            sl[sg][4][q] = exp(P.gam * ia);
+            sl[sg][5][q] = -P.gam * ia * ia * L.isig;
+            sj[sg][q] = j | (L.t << 30);
+          }
         }
       }
     }
@@ -625,6 +641,158 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
       if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
     }
     __syncwarp();
+  }
+}
+
+// Binary32 force with eight lanes per centre for every centre (four centres
+// per warp), for systems too small to fill the GPU one thread per centre:
+// each lane takes every eighth listed neighbour (2-body force on the centre
+// and the leg parameters, active legs staged in shared memory), then legs
+// as rows as in the many-leg kernel, and the group reduces the centre's
+// force. Twice the warps of a one-thread-per-centre pass per eight atoms and
+// a fraction of its dependent chain; chosen by the force-stage autotune
+// where it is faster (tens of thousands of atoms).
+template <bool ENERGY, bool COUNT>
+__global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, DevState S) {
+  constexpr int GROUP = 8;
+  constexpr int GPW = 32 / GROUP;
+  constexpr int NG = kHeavyWarps * GPW;
+  const int nbg = (P.N + NG - 1) / NG;
+  // the last mol_blocks blocks evaluate the Moliere list
+  if ((int)blockIdx.x >= nbg) {
+    moliere_entries<true, ENERGY>(P, S, ((int)blockIdx.x - nbg) * (32 * kHeavyWarps) + threadIdx.x,
+                                  ((int)gridDim.x - nbg) * (32 * kHeavyWarps));
+    return;
+  }
+  __shared__ float sl[NG][6][kHeavyLegs];
+  __shared__ int sj[NG][kHeavyLegs];
+  __shared__ int snl[NG];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gl = lane % GROUP;            // lane within the group
+  const int sg = w * GPW + lane / GROUP;  // the group's stage
+  const int c = blockIdx.x * NG + sg;
+  if (gl == 0) snl[sg] = 0;
+  __syncwarp();
+  int tc = 1, n = 0;
+  int4 qc = make_int4(0, 0, 0, 0);
+  if (c < P.N) {
+    qc = S.posq[c];
+    tc = qc.w & 0xff;
+    if (tc < 3 && !((qc.w >> 8) & FL_REMOVED)) n = S.n_sw[c];
+  }
+  const int ta = tc - 1;
+  float fx = 0.f, fy = 0.f, fz = 0.f, ui = 0.f;
+  unsigned cnt_pairs = 0, cnt_ang = 0;
+  if (n > 0) {
+    const Geo& G = S.geo[rep_of_w(qc.w)];
+    const float al = (float)P.al, cut = (float)P.cut3, gm = (float)P.gam;
+    const float Bc = (float)P.B, Ac = (float)P.A;
+    // three neighbours per lane in flight (a crystal lists 16)
+    constexpr int kG = 3;
+    for (int k0 = gl; k0 < n; k0 += kG * GROUP) {
+      int jj[kG];
+      int4 qq[kG];
+#pragma unroll
+      for (int u = 0; u < kG; u++) {
+        const int k = k0 + u * GROUP;
+        jj[u] = k < n ? S.nbr_sw[(size_t)k * P.N + c] : c;
+      }
+#pragma unroll
+      for (int u = 0; u < kG; u++) qq[u] = S.posq[jj[u]];
+#pragma unroll
+      for (int u = 0; u < kG; u++) {
+        if (k0 + u * GROUP >= n) break;
+        const int j = jj[u];
+        const int4 qj = qq[u];
+        const float3 dq = qsep(qc, qj, G.qinvA);
+        const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
+        if (r2f > P.pre3mA2 || ((qj.w >> 8) & FL_REMOVED)) continue;
+        const int tb = (qj.w & 0xff) - 1;
+        const float rinv = rsqrtf(r2f);
+        const float is = P.isigA[ta][tb];
+        const float ue = r2f * rinv * is;
+        if (!(ue < cut)) continue;
+        const float inv = __frcp_rn(ue - al);
+        const float ex = expf(inv);
+        const float iu = P.sigA[ta][tb] * rinv;  // 1/u
+        const float u2 = iu * iu;
+        const float u4 = u2 * u2;
+        // psi = 4, qsi = 0: dphi/du = A e^{1/(u-a)} [ -4 B u^-5 - (B u^-4 - 1)/(u-a)^2 ]
+        const float dphi = Ac * ex * (-4.0f * Bc * u4 * iu - (Bc * u4 - 1.0f) * inv * inv);
+        const float cf = -(dphi * rinv * P.epssigA[ta][tb]);
+        fx += cf * dq.x;
+        fy += cf * dq.y;
+        fz += cf * dq.z;
+        if (COUNT) cnt_pairs++;
+        if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
+        const float E = expf(gm * inv);
+        if (!(E > kLegEmin)) continue;
+        const int q = atomicAdd(&snl[sg], 1);
+        sl[sg][0][q] = dq.x * rinv;
+        sl[sg][1][q] = dq.y * rinv;
+        sl[sg][2][q] = dq.z * rinv;
+        sl[sg][3][q] = rinv;
+        sl[sg][4][q] = E;
+        sl[sg][5][q] = -gm * inv * inv * is;
+        sj[sg][q] = j | (tb << 30);
+      }
+    }
+  }
+  __syncwarp();
+  const int nl = snl[sg];
+  const float thrd = (float)P.thrd;
+  const float conv = (float)P.f_evA_to_N;
+  float uc = 0.f;
+  for (int a = gl; a < nl; a += GROUP) {
+    const float ax = sl[sg][0][a], ay = sl[sg][1][a], az = sl[sg][2][a];
+    const float ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
+    const int ja = sj[sg][a];
+    float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+    for (int b = 0; b < nl; b++) {
+      if (b == a) continue;
+      const float bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
+      const float cs = ax * bx + ay * by + az * bz;
+      const float c3 = cs + thrd, W = c3 * c3, s2 = 2.0f * c3;
+      const float pref =
+          P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30] * aE * sl[sg][4][b];
+      const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
+      afx += pref * (wa * ax + sa * bx);
+      afy += pref * (wa * ay + sa * by);
+      afz += pref * (wa * az + sa * bz);
+      if (ENERGY) ae += pref * W;
+      if (COUNT && b > a && pref != 0.f) cnt_ang++;
+    }
+    const int j = ja & 0x3fffffff;
+    atomic_add3(S.frc_new, j, (double)(conv * afx), (double)(conv * afy), (double)(conv * afz));
+    if (ENERGY && ae != 0.f) atomicAdd(&S.epot[j], P.e_eV_to_J * (double)ae / 3.0);
+    fx -= afx;
+    fy -= afy;
+    fz -= afz;
+    if (ENERGY) uc += ae;
+  }
+  // the centre's force over the group: binary64 sums of the lanes' shares
+  double dcx = (double)(conv * fx), dcy = (double)(conv * fy), dcz = (double)(conv * fz);
+  // the centre's half of each pair, and a third of each angle term (counted
+  // in both of its rows)
+  double duc = ENERGY ? P.e_eV_to_J * ((double)ui + (double)uc / 6.0) : 0.0;
+#pragma unroll
+  for (int o = GROUP / 2; o > 0; o >>= 1) {
+    dcx += __shfl_xor_sync(0xffffffffu, dcx, o);
+    dcy += __shfl_xor_sync(0xffffffffu, dcy, o);
+    dcz += __shfl_xor_sync(0xffffffffu, dcz, o);
+    if (ENERGY) duc += __shfl_xor_sync(0xffffffffu, duc, o);
+  }
+  if (gl == 0 && n > 0) {
+    atomic_add3(S.frc_new, c, dcx, dcy, dcz);
+    if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
+  }
+  if (COUNT) {
+    const unsigned sp = __reduce_add_sync(0xffffffffu, cnt_pairs);
+    const unsigned sa = __reduce_add_sync(0xffffffffu, cnt_ang);
+    if (lane == 0) {
+      if (sp) atomicAdd(&S.sc->counters[0], (unsigned long long)sp);
+      if (sa) atomicAdd(&S.sc->counters[1], (unsigned long long)sa);
+    }
   }
 }
 
@@ -809,6 +977,22 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
   return cudaGetLastError();
 }
 
+// The eight-lanes-per-centre path: one kernel for the SW terms of every
+// centre and the Moliere list.
+template <bool ENERGY, bool COUNT>
+static cudaError_t group_impl(const Launch& L, const DevParams& P, const DevState& S) {
+  constexpr int NG = kHeavyWarps * 4;  // centres per block
+  if (L.force_a) cudaEventRecord(L.force_a, L.stream);
+  k_force_group<ENERGY, COUNT>
+      <<<(P.N + NG - 1) / NG + mol_blocks(P), 32 * kHeavyWarps, 0, L.stream>>>(P, S);
+  if (L.force_b) cudaEventRecord(L.force_b, L.stream);
+  if (P.mode == FIBMD_MODE_REF) {
+    const int side = L.sms > 0 ? L.sms : 152;
+    k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S, bool energy,
                          bool count, bool spec_step) {
   cudaError_t e = cudaSuccess;
@@ -823,6 +1007,10 @@ cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
   if (!spec_step) k_force_begin<<<1, 32, 0, L.stream>>>(S);
   const bool mixed = P.precision == FIBMD_PREC_MIXED;
   if (mixed) {
+    if (L.stage == kStageGroup) {
+      if (energy) return count ? group_impl<true, true>(L, P, S) : group_impl<true, false>(L, P, S);
+      return count ? group_impl<false, true>(L, P, S) : group_impl<false, false>(L, P, S);
+    }
     if (L.stage == kStageLarge) {
       if (energy)
         return count ? force_impl<true, true, true, kStageLarge>(L, P, S)

@@ -393,6 +393,9 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
 // takes.
 constexpr int kStageSmall = 8;
 constexpr int kStageLarge = 10;
+// A third choice for small systems: eight lanes per centre for every centre
+// (the "stage" value 1).
+constexpr int kStageGroup = 1;
 
 struct Launch {
   cudaStream_t stream;

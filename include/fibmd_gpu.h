@@ -279,11 +279,13 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    graph launch with device-side rebuild decisions, default 1; phase and
    kernel timers see only the steps run outside the graph), "autotune"
    (mixed precision: before every 1000 spec-mode steps of a graph run, and
-   before a dose, time the binary32 force kernel's two stage sizes on the
-   current state and keep the faster, default 1) and "stage" (8 or 10
-   staged leg candidates per centre, which also turns "autotune" off). */
+   before a dose, time the binary32 force paths on the current state and
+   keep the fastest, default 1) and "stage" (the binary32 force path: 8 or
+   10 staged leg candidates per centre with one thread per centre, or 1 for
+   eight lanes per centre, the faster on small systems; setting it turns
+   "autotune" off). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
-/* The current value of an option ("stage" reads the stage size in use,
+/* The current value of an option ("stage" reads the force path in use,
    which "autotune" changes as the run goes). */
 int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value);
 

@@ -219,10 +219,11 @@ def test_regime_switch_and_parking(gpu_lib):
     assert np.abs(X - o.X).max() < TRAJ_ATOL_M
 
 
-@pytest.mark.parametrize("stage", [8, 10])
+@pytest.mark.parametrize("stage", [8, 10, 1])
 def test_mixed_precision_force_error(gpu_lib, stage):
     """binary32 force arithmetic (reduced units) against the binary64 oracle;
-    the 2-body term is analytic in binary32, tabulated in the reference."""
+    the 2-body term is analytic in binary32, tabulated in the reference.
+    Stages 8 and 10: one thread per centre; 1: eight lanes per centre."""
     o = _slab()
     o.si_nlist()
     Fr = o.si_force()
@@ -257,12 +258,13 @@ def _compressed_core(scale=0.8, radius_A=6.0):
     return o
 
 
-@pytest.mark.parametrize("precision,stage", [(0, 8), (1, 8), (1, 10)])
+@pytest.mark.parametrize("precision,stage", [(0, 8), (1, 8), (1, 10), (1, 1)])
 def test_many_leg_centres(gpu_lib, precision, stage):
     """Centres with more legs than the per-thread stage (the many-leg paths:
-    the warp-per-centre kernel in binary64, the warp-cooperative epilogue of
-    the binary32 kernel) against the binary64 oracle: within 1e-10 in
-    binary64, at the crystal test's binary32 tolerances in mixed precision."""
+    the warp-per-centre kernel in binary64, the eight-lane groups of the
+    binary32 many-leg kernel; stage 1 takes every centre in eight-lane
+    groups) against the binary64 oracle: within 1e-10 in binary64, at the
+    crystal test's binary32 tolerances in mixed precision."""
     import fib_md_gb300 as fm
 
     o = _compressed_core()
@@ -276,7 +278,8 @@ def test_many_leg_centres(gpu_lib, precision, stage):
     g.set_impact(1)
     g.si_nlist()
     F = g.si_force()
-    assert g.work_counters()[5] > 0  # the many-leg path ran
+    # the many-leg kernel ran (stage 1 has no separate many-leg pass)
+    assert (g.work_counters()[5] > 0) == (stage != 1)
     if precision == 0:
         assert _maxrel(F, Fr) < FORCE_RTOL
     else:

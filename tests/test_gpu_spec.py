@@ -294,11 +294,11 @@ def test_removed_neighbour_exerts_no_force(gpu_lib, precision, which):
 
 
 def test_force_stage_switch_and_autotune(gpu_lib):
-    """Mixed precision: the force kernel's stage size (8 or 10 staged legs)
-    changed between graph runs recaptures the step graph; the run matches
-    one at a fixed stage (the stage only moves centres between the main and
-    the many-leg kernel: binary32 sums in another order). With autotune on,
-    the stage in use is one of the two."""
+    """Mixed precision: the binary32 force path (8 or 10 staged legs per
+    thread, or 1: eight lanes per centre) changed between graph runs
+    recaptures the step graph; the run matches one at a fixed stage (the
+    paths differ only in the order of binary32 sums). With autotune on, the
+    stage in use is one of the three."""
     s, X, V = _spec_system(precision=1)
     a = _ctx(s, X, V, 1)
     b = _ctx(s, X, V, 1)
@@ -309,14 +309,18 @@ def test_force_stage_switch_and_autotune(gpu_lib):
     a.set_option("stage", 10)
     assert a.get_option("stage") == 10 and a.get_option("autotune") == 0
     la, ta, _, _ = a.steps(2, 60, 60, 0.0, 300.0)
+    a.set_option("stage", 1)
+    assert a.get_option("stage") == 1
+    la, ta, _, _ = a.steps(2, 60, la, ta, 300.0)
     lb, tb, _, _ = b.steps(2, 60, 60, 0.0, 300.0)
-    assert la == lb == 120
+    lb, tb, _, _ = b.steps(2, 60, lb, tb, 300.0)
+    assert la == lb == 180
     Xa, _, _ = a.download()
     Xb, _, _ = b.download()
     assert np.isfinite(Xa).all()
-    assert np.abs(Xa - Xb).max() < 1e-15  # 1e-5 A after 120 steps of a 2 keV cascade
+    assert np.abs(Xa - Xb).max() < 1e-15  # 1e-5 A after 180 steps of a 2 keV cascade
     c = _ctx(s, X, V, 1)
     c.set_option("autotune", 1)
     c.steps(2, 1200, 0, 0.0, 300.0)  # tunes before each 1000 steps
-    assert c.get_option("stage") in (8, 10)
+    assert c.get_option("stage") in (8, 10, 1)
     assert c.get_option("autotune") == 1
