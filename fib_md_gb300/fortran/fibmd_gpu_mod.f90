@@ -63,6 +63,14 @@ module fibmd_gpu_mod
      integer(c_int) :: reserved(8)
   end type fibmd_params
 
+  ! one replica of a batched ensemble (fibmd_gpu_batch_create)
+  type, bind(C) :: fibmd_replica
+     integer(c_int) :: natm, nsg
+     real(c_double) :: Lb(3)
+     real(c_double) :: remove_z
+     integer(c_int) :: reserved(4)
+  end type fibmd_replica
+
   interface
      integer(c_int) function fibmd_gpu_abi_version() bind(C)
        import
@@ -183,6 +191,123 @@ module fibmd_gpu_mod
        character(kind=c_char) :: key(*)
        real(c_double), value :: value
      end function fibmd_gpu_set_option
+
+     integer(c_int) function fibmd_gpu_get_option(ctx, key, value) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       character(kind=c_char) :: key(*)
+       real(c_double) :: value
+     end function fibmd_gpu_get_option
+
+     integer(c_int) function fibmd_gpu_regime(ctx, Ts, tic) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: Ts
+       integer(c_int) :: tic
+     end function fibmd_gpu_regime
+
+     integer(c_int) function fibmd_gpu_xyz_frame(ctx, xyz_A, ke_eV) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: xyz_A(*), ke_eV(*)
+     end function fibmd_gpu_xyz_frame
+
+     integer(c_int) function fibmd_gpu_list_counts(ctx, n_sw_full, n_mol_full, n_triplets) &
+          bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_long_long) :: n_sw_full, n_mol_full, n_triplets
+     end function fibmd_gpu_list_counts
+
+     integer(c_int) function fibmd_gpu_get_pairs(ctx, kind, n, ij, cap) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: kind, cap
+       integer(c_int) :: n
+       integer(c_int) :: ij(*)
+     end function fibmd_gpu_get_pairs
+
+     integer(c_int) function fibmd_gpu_get_triplets(ctx, n, ijk, cap) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_long_long) :: n
+       integer(c_int) :: ijk(*)
+       integer(c_long_long), value :: cap
+     end function fibmd_gpu_get_triplets
+
+     integer(c_int) function fibmd_gpu_phase_times(ctx, seconds7, counts7, reset) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: seconds7(7)
+       integer(c_long_long) :: counts7(7)
+       integer(c_int), value :: reset
+     end function fibmd_gpu_phase_times
+
+     integer(c_int) function fibmd_gpu_kernel_time(ctx, force_kernel_s, launches, reset) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: force_kernel_s
+       integer(c_long_long) :: launches
+       integer(c_int), value :: reset
+     end function fibmd_gpu_kernel_time
+
+     integer(c_int) function fibmd_gpu_pipe_peaks(fp64_tflops, fp32_tflops) bind(C)
+       import
+       real(c_double) :: fp64_tflops, fp32_tflops
+     end function fibmd_gpu_pipe_peaks
+
+     integer(c_int) function fibmd_gpu_work_counters(ctx, counts) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_long_long) :: counts(6)
+     end function fibmd_gpu_work_counters
+
+     ! successive impacts on the device: ion_atoms 1-based, x/v (nimp,3)
+     integer(c_int) function fibmd_gpu_dose(ctx, nimp, ion_atoms, x, v, steps, relax_s, &
+          removed_after, ions_removed_after, time_after, steps_after) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int), value :: nimp
+       integer(c_int) :: ion_atoms(*)
+       real(c_double) :: x(*), v(*)
+       integer(c_long_long), value :: steps
+       real(c_double), value :: relax_s
+       integer(c_int), optional :: removed_after(*), ions_removed_after(*)
+       real(c_double), optional :: time_after(*)
+       integer(c_long_long), optional :: steps_after(*)
+     end function fibmd_gpu_dose
+
+     integer(c_int) function fibmd_gpu_batch_create(p, nrep, reps, ctx) bind(C)
+       import
+       type(fibmd_params) :: p
+       integer(c_int), value :: nrep
+       type(fibmd_replica) :: reps(*)
+       type(c_ptr) :: ctx
+     end function fibmd_gpu_batch_create
+
+     integer(c_int) function fibmd_gpu_batch_layout(ctx, nrep, offsets) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int) :: nrep
+       integer(c_int) :: offsets(*)
+     end function fibmd_gpu_batch_layout
+
+     integer(c_int) function fibmd_gpu_batch_scalars(ctx, time, dt, removed) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: time(*), dt(*)
+       integer(c_int) :: removed(*)
+     end function fibmd_gpu_batch_scalars
+
+     integer(c_int) function fibmd_gpu_impact_stats(ctx, surface_z, displaced_m, sputtered, &
+          displaced, ion_depth) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: surface_z(*)
+       real(c_double), value :: displaced_m
+       integer(c_int) :: sputtered(*), displaced(*)
+       real(c_double) :: ion_depth(*)
+     end function fibmd_gpu_impact_stats
   end interface
 
 contains
