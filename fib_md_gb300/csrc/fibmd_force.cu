@@ -600,8 +600,10 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
       const R ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
       const int ja = sj[sg][a];
       R afx = 0, afy = 0, afz = 0, ae = 0;
+      // unrolled for independent shared-memory loads; leg a itself enters
+      // with a zero weight (its terms are finite)
+#pragma unroll 4
       for (int b = 0; b < nl; b++) {
-        if (b == a) continue;
         const R bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
         const int jb = sj[sg][b];
         const R cs = ax * bx + ay * by + az * bz;
@@ -609,7 +611,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
         R lp;
         if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
-        const R pref = lp * aE * sl[sg][4][b];
+        const R pref = b == a ? (R)0 : lp * aE * sl[sg][4][b];
         const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
         afx += pref * (wa * ax + sa * bx);
         afy += pref * (wa * ay + sa * by);
@@ -748,13 +750,16 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
     const float ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
     const int ja = sj[sg][a];
     float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+    // unrolled for independent shared-memory loads; leg a itself enters
+    // with a zero weight (its terms are finite)
+#pragma unroll 4
     for (int b = 0; b < nl; b++) {
-      if (b == a) continue;
       const float bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
       const float cs = ax * bx + ay * by + az * bz;
       const float c3 = cs + thrd, W = c3 * c3, s2 = 2.0f * c3;
       const float pref =
-          P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30] * aE * sl[sg][4][b];
+          b == a ? 0.f
+                 : P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30] * aE * sl[sg][4][b];
       const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
       afx += pref * (wa * ax + sa * bx);
       afy += pref * (wa * ay + sa * by);
