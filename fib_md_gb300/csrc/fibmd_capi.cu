@@ -1438,24 +1438,47 @@ constexpr long long kTuneSteps = 1000;  // spec-mode steps between stage re-tuni
 // (one untimed and two timed evaluations each) and keeps the faster one. It
 // reads the lists, so it runs only once they are built; the evaluations
 // accumulate into the next-force buffer, which the caller clears.
+// Device time (ms) of three force evaluations with the given stage, each a
+// launch of a captured graph as the step loop runs it, so that a path of
+// fewer kernels is credited with the launch gaps it saves.
+static int time_force_graph(fibmd_ctx* ctx, int stage, cudaEvent_t a, cudaEvent_t b, float* ms) {
+  Launch L = launch_of(ctx);
+  L.stage = stage;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const cudaError_t e = launch_force(L, ctx->P, ctx->S, false, false, false);
+  const cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+  if (e != cudaSuccess || ee != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return fail(ctx, FIBMD_ECUDA, "force-stage timing capture: %s",
+                cudaGetErrorString(e != cudaSuccess ? e : ee));
+  }
+  cudaGraphExec_t x = nullptr;
+  cudaError_t r = cudaGraphInstantiate(&x, g, 0);
+  cudaGraphDestroy(g);
+  if (r == cudaSuccess) r = cudaGraphLaunch(x, ctx->stream);
+  if (r == cudaSuccess) r = cudaEventRecord(a, ctx->stream);
+  for (int k = 0; k < 3 && r == cudaSuccess; k++) r = cudaGraphLaunch(x, ctx->stream);
+  if (r == cudaSuccess) r = cudaEventRecord(b, ctx->stream);
+  if (r == cudaSuccess) r = cudaEventSynchronize(b);
+  if (r == cudaSuccess) r = cudaEventElapsedTime(ms, a, b);
+  if (x) cudaGraphExecDestroy(x);
+  if (r != cudaSuccess)
+    return fail(ctx, FIBMD_ECUDA, "force-stage timing: %s", cudaGetErrorString(r));
+  return FIBMD_OK;
+}
+
 static int tune_stage(fibmd_ctx* ctx) {
   if (ctx->P.precision != FIBMD_PREC_MIXED || !ctx->autotune || !ctx->lists_built)
     return FIBMD_OK;
   cudaEvent_t a = get_event(ctx), b = get_event(ctx);
   const int stages[3] = {kStageSmall, kStageLarge, kStageGroup};
   float ms[3] = {0.f, 0.f, 0.f};
-  for (int q = 0; q < 3; q++) {
-    Launch L = launch_of(ctx);
-    L.stage = stages[q];
-    CK(launch_force(L, ctx->P, ctx->S, false, false, false));
-    CK(cudaEventRecord(a, ctx->stream));
-    for (int k = 0; k < 2; k++) CK(launch_force(L, ctx->P, ctx->S, false, false, false));
-    CK(cudaEventRecord(b, ctx->stream));
-    CK(cudaEventSynchronize(b));
-    CK(cudaEventElapsedTime(&ms[q], a, b));
-  }
+  int rc = FIBMD_OK;
+  for (int q = 0; q < 3 && rc == FIBMD_OK; q++) rc = time_force_graph(ctx, stages[q], a, b, &ms[q]);
   ctx->pool.push_back(a);
   ctx->pool.push_back(b);
+  if (rc) return rc;
   // switch only for a clear gain: a switch recaptures the step graph
   int cur = 0, best = 0;
   for (int q = 0; q < 3; q++) {
