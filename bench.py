@@ -71,12 +71,14 @@ def parse():
                     help="impacts of its binary64 counterpart (default: as many)")
     ap.add_argument("--large-steps", type=int, default=20000,
                     help="MD steps of the 1,048,577-atom 30 keV cascade (0: skip)")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step", "ensemble"],
+    ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step", "ensemble", "dose"],
                     default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64), "
                          "rebuild the lists 5 times (build), run 10 mixed steps launch "
-                         "by launch (step), or run the 256-impact ensemble 1000 steps as "
-                         "graphs and 20 launch by launch (ensemble), exit (for ncu)")
+                         "by launch (step), run the 256-impact ensemble 1000 steps as "
+                         "graphs and 20 launch by launch (ensemble), or run the dose slab's "
+                         "first impact 300 steps as graphs and 20 launch by launch on the "
+                         "8-lanes-per-centre force path (dose), exit (for ncu)")
     return ap.parse_args()
 
 
@@ -857,6 +859,30 @@ def main():
         b.set_option("graph", 0)
         b.steps(2, 20, lt, t, 300.0)
         b.close()
+        return 0
+
+    if args.profile == "dose":
+        import fib_md_gb300 as fm
+
+        p = fm.params_default()
+        p.list_skin = args.list_skin * 1e-10
+        d = fm.dose_slab((20, 20, 12), 1, seed=4001, ion_eV=2000.0, window=30e-10,
+                         remove_above=15e-10, params=p)
+        sl = d.slab
+        q = sl.params.copy()
+        q.precision = fm.PREC_MIXED
+        g = fm.FibMD(q)
+        g.upload(sl.X, sl.V, None, sl.Xi, sl.mass, sl.atype, np.zeros(q.Natm, np.int32))
+        g.set_tags(sl.tags)
+        g.set_impact(len(d.ion_atoms))
+        g.si_nlist()
+        g.si_force()
+        g.set_option("stage", 1)
+        g.set_atom(int(d.ion_atoms[0]), d.X0[0], d.V0[0])
+        lt, t, _, _ = g.steps(2, 300, 0, 0.0, 300.0)
+        g.set_option("graph", 0)
+        g.steps(2, 20, lt, t, 300.0)
+        g.close()
         return 0
 
     if args.profile:
