@@ -1,8 +1,8 @@
 #!/usr/bin/env python
 """Throughput of the FIB_MD hot path on GB300: atom-steps/s.
 
-Workload (BASELINE config 2): a diamond-cubic Si slab of 40 x 40 x 20 unit
-cells (256,000 Si; the named atom count) plus one Ga ion at
+Workload: a diamond-cubic Si slab of 40 x 40 x 20 unit cells (256,000 Si,
+eight atoms per cubic unit cell) plus one Ga ion at
 5 keV, 7 degrees off normal, seeded azimuth and impact point 10 A above the
 surface; Maxwell-Boltzmann velocities at 300 K (seeded); bottom 2 atomic
 layers fixed, next 4 Berendsen-thermostatted at 300 K; variable dt
