@@ -258,6 +258,32 @@ def _compressed_core(scale=0.8, radius_A=6.0):
     return o
 
 
+def test_group_path_energies(gpu_lib):
+    """Mixed precision: forces and per-atom energies of the eight-lanes-per-
+    centre path (stage 1) against the one-thread-per-centre path with its
+    many-leg kernel (stage 8) on the compressed-core slab: the same terms
+    summed in another order, so equal to binary32 rounding."""
+    import fib_md_gb300 as fm
+
+    o = _compressed_core()
+    p = o.p.copy()
+    p.precision = 1
+    out = {}
+    for stage in (8, 1):
+        g = fm.FibMD(p)
+        g.set_option("stage", stage)
+        g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
+        g.set_impact(1)
+        g.si_nlist()
+        out[stage] = g.si_force_energy()
+        g.close()
+    (F8, u8, U8), (F1, u1, U1) = out[8], out[1]
+    assert np.isfinite(u1).all() and np.abs(u8).max() > 0
+    assert _maxrel(F1, F8) < 1e-5
+    assert _maxrel(u1, u8) < 1e-5
+    assert abs(U1 - U8) < 1e-6 * abs(U8)
+
+
 @pytest.mark.parametrize("precision,stage", [(0, 8), (1, 8), (1, 10), (1, 1)])
 def test_many_leg_centres(gpu_lib, precision, stage):
     """Centres with more legs than the per-thread stage (the many-leg paths:
