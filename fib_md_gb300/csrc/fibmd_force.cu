@@ -63,8 +63,8 @@ constexpr int kBlock64 = 64;
 constexpr int kLegF32 = 6;   // ux uy uz rinv E g
 constexpr int kBlock32 = 128;
 constexpr int kCandF64 = 16;  // prefiltered neighbours staged per centre (binary64 kernel)
-// (the binary32 kernel's stage sizes, kStageSmall and kStageLarge, are in
-// fibmd_internal.cuh: the context chooses between them)
+// (the binary32 paths, kStageSmall, kStageLarge and kStageGroup, are in
+// fibmd_internal.cuh: the context chooses among them)
 
 constexpr int kBatch = 8;    // neighbour gathers in flight per thread
 

@@ -385,16 +385,16 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
                       DevParams& P, Geo& G, char* err, int errlen);
 
 // ---- launchers (defined in the .cu files) --------------------------------
-// Staged candidates per centre in the binary32 force kernel, one of two
-// stage sizes chosen per context at run time by timing both on the current
-// state: a crystal at 300 K has 4 legs, rarely more than 6, and the small
-// stage leaves more resident warps; damaged slabs (a batch of small
-// cascades) have many centres beyond it, which the many-leg kernel then
-// takes.
+// The binary32 force path, chosen per context at run time by timing each
+// on the current state: one thread per centre with kStageSmall or
+// kStageLarge staged candidates (a crystal at 300 K has 4 legs, rarely more
+// than 6, and the small stage leaves more resident warps; damaged slabs, a
+// batch of small cascades, have many centres beyond it, which the many-leg
+// kernel then takes), or eight lanes per centre for every centre
+// (kStageGroup, the "stage" value 1: one kernel, faster on systems too
+// small to fill the GPU one thread per centre).
 constexpr int kStageSmall = 8;
 constexpr int kStageLarge = 10;
-// A third choice for small systems: eight lanes per centre for every centre
-// (the "stage" value 1).
 constexpr int kStageGroup = 1;
 
 struct Launch {
