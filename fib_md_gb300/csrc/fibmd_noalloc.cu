@@ -80,13 +80,18 @@ constexpr Layout kLayout = make_layout();
 // for cudaGetSymbolAddress, never a device address.
 __device__ __align__(256) unsigned char g_noalloc_scratch[kLayout.total];
 
-// Per-device set-up: the array's device address and the parameters of the
-// 2-body table currently loaded into it.
+// Per-device set-up: the array's device address, the parameters of the
+// 2-body table currently loaded into it, and that table's extent (umax and
+// the last non-zero entry). The key, the device table and the extent change
+// together, inside one critical section, so they always describe the same
+// table.
 struct DeviceSlot {
   bool ready = false;
   unsigned char* base = nullptr;
   bool table_loaded = false;
   double tab_key[7] = {};
+  double umax = 0.0;
+  int tab_last = 0;
 };
 constexpr int kMaxDevices = 64;
 DeviceSlot g_slots[kMaxDevices];
@@ -158,25 +163,13 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
     return fail_na(FIBMD_ECUDA, "force_noalloc: no usable current device");
   cudaStream_t s = (cudaStream_t)stream;
 
-  // derived constants (the table itself goes to the device below)
+  // per-device set-up on the first call (the device address of the array),
+  // then the 2-body table: its key is compared, and on a change the table is
+  // built, uploaded and recorded with its extent, all under one lock, so a
+  // thread calling with other parameters cannot slip its table in between
+  DeviceSlot& slot = g_slots[dev];
   double umax = 0.0;
   int last = 0;
-  DevParams P;
-  Geo G;
-  {
-    std::lock_guard<std::mutex> lock(g_slots_mutex);
-    build_ref_table(q, g_tab_host, g_tabu_host, &umax, &last);
-  }
-  const int rc = derive_dev_params(q, impact, umax, last, P, G, msg, sizeof msg);
-  if (rc) return fail_na(rc, msg);
-  if (P.ncell > kNaCells) {
-    std::snprintf(msg, sizeof msg, "force_noalloc: %d cells in the reference grid, the limit is %d",
-                  P.ncell, kNaCells);
-    return fail_na(FIBMD_EINVAL, msg);
-  }
-
-  // per-device set-up on the first call: the device address of the array
-  DeviceSlot& slot = g_slots[dev];
   {
     std::lock_guard<std::mutex> lock(g_slots_mutex);
     if (!slot.ready) {
@@ -192,6 +185,10 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
     }
     const double key[7] = {q.A, q.B, q.psi, q.qsi, q.al, q.listfac, (double)q.Ntable};
     if (!slot.table_loaded || std::memcmp(key, slot.tab_key, sizeof key) != 0) {
+      slot.table_loaded = false;
+      double um = 0.0;
+      int lz = 0;
+      build_ref_table(q, g_tab_host, g_tabu_host, &um, &lz);
       const size_t tb = sizeof(double) * (size_t)(q.Ntable + 2);
       cudaError_t e1 = cudaMemcpyAsync(slot.base + kLayout.tab, g_tab_host, tb,
                                        cudaMemcpyHostToDevice, s);
@@ -201,8 +198,21 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
       if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess)
         return fail_na(FIBMD_ECUDA, "force_noalloc: table upload failed");
       std::memcpy(slot.tab_key, key, sizeof key);
+      slot.umax = um;
+      slot.tab_last = lz;
       slot.table_loaded = true;
     }
+    umax = slot.umax;
+    last = slot.tab_last;
+  }
+  DevParams P;
+  Geo G;
+  const int rc = derive_dev_params(q, impact, umax, last, P, G, msg, sizeof msg);
+  if (rc) return fail_na(rc, msg);
+  if (P.ncell > kNaCells) {
+    std::snprintf(msg, sizeof msg, "force_noalloc: %d cells in the reference grid, the limit is %d",
+                  P.ncell, kNaCells);
+    return fail_na(FIBMD_EINVAL, msg);
   }
   unsigned char* b = slot.base;
   DevState S;

@@ -7,9 +7,9 @@
  * The reference (nanoMFG/FIB_MD, Fortran 90 + MPI) has no plugin API: the hot
  * path is a set of module subroutines called from `onestep`
  * (src/timeint.f90:158-242). Each entry point below names the routine(s) it
- * replaces. A Fortran host binds them with ISO_C_BINDING (see the binding
- * module shown in INTEGRATION.md); the C++ host driver and the Python package
- * `fib_md_gb300` bind the same symbols.
+ * replaces. A Fortran host binds them with ISO_C_BINDING (the interface
+ * module fib_md_gb300/fortran/fibmd_gpu_mod.f90 declares every one); the C++
+ * host driver and the Python package `fib_md_gb300` bind the same symbols.
  *
  * Conventions (mirroring the reference's):
  *   - Every real is IEEE binary64 (the reference builds with -fdefault-real-8,
