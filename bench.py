@@ -1,23 +1,27 @@
 #!/usr/bin/env python
 """Throughput of the FIB_MD hot path on GB300: atom-steps/s.
 
-Workload: a diamond-cubic Si slab of 40 x 40 x 20 unit cells (256,000 Si,
-eight atoms per cubic unit cell) plus one Ga ion at
-5 keV, 7 degrees off normal, seeded azimuth and impact point 10 A above the
-surface; Maxwell-Boltzmann velocities at 300 K (seeded); bottom 2 atomic
-layers fixed, next 4 Berendsen-thermostatted at 300 K; variable dt
-= min(1 fs, 0.05 A / max|v|); lists rebuilt at half the skin. Synthetic data.
+Workload (the single-cascade configuration): a diamond-cubic Si slab of
+40 x 40 x 20 unit cells (256,000 Si, eight atoms per cubic unit cell) plus
+one Ga ion at 5 keV, 7 degrees off normal, seeded azimuth and impact point
+10 A above the surface; Maxwell-Boltzmann velocities at 300 K (seeded);
+bottom 2 atomic layers fixed, next 4 Berendsen-thermostatted at 300 K;
+variable dt = min(1 fs, 0.05 A / max|v|); lists rebuilt at half the skin.
+Synthetic data, seeded (spec_slab, seed 2001).
 
-One bench step = `--md-steps` (default 1000) MD steps through fibmd_gpu_steps.
+One bench step = MD steps 1..`--md-steps` (default 5000) of that cascade,
+from a fresh upload of the seeded initial state, through fibmd_gpu_steps.
 `value` is the mixed-precision path (binary32 force arithmetic, binary64
-accumulation/integration) with the state resident in HBM; `fp64` is the
-plain binary64 path on the same workload. L2 (129 MB) is flushed between
-timed steps (the resident working set is ~70 MB). `e2e` times the C-ABI
-calls a host makes with host buffers: upload (pinned) -> steps -> download.
+accumulation/integration) with the upload, list build and first force
+outside the timed region; `fp64` is the plain binary64 path on the same
+window. L2 (129 MB) is flushed before every timed step. `e2e` times what a
+host does per cascade through the C-ABI with pinned host buffers: upload of
+the initial state -> tags -> si_nlist -> si_force -> steps -> download.
 
 --impl reference times the CPU oracle (the binary64 restatement of the
-reference's onestep, OpenMP over all host cores) on a bounded sample of the
-same slab.
+reference's si_nlist/si_force with the spec-mode step, its force OpenMP over
+all host cores) on a bounded sample of the same window of the same cascade,
+set up from the oracle's restatements alone.
 """
 from __future__ import annotations
 
@@ -39,6 +43,7 @@ sys.path.insert(0, str(ROOT))
 
 KB = 1.381e-23
 A_LAT = 5.431073e-10
+METRIC = "atom-steps/s (256k-atom Si slab, 5 keV Ga cascade from the ion's start)"
 
 
 def parse():
@@ -47,10 +52,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--md-steps", type=int, default=1000)
+    ap.add_argument("--md-steps", type=int, default=5000,
+                    help="MD steps of the cascade per bench step, from the ion's start")
     ap.add_argument("--cells", default="40,40,20")
-    ap.add_argument("--fp64-steps", type=int, default=-1)
-    ap.add_argument("--cpu-sample-steps", type=int, default=12)
+    ap.add_argument("--fp64-steps", type=int, default=2,
+                    help="timed bench steps of the binary64 arm (after one untimed)")
+    ap.add_argument("--cpu-sample-steps", type=int, default=12,
+                    help="spec-mode oracle steps of the CPU baseline's timed sample")
+    ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--list-skin", type=float, default=0.6,
@@ -84,44 +93,54 @@ def parse():
 
 # ---------------------------------------------------------------------------
 # workload
+def _impact_xy(cells, centre):
+    return (0.5 * A_LAT * cells[0], 0.5 * A_LAT * cells[1]) if centre else None
+
+
+def _as_workload(params, X, V, Xi, mass, atype, tags):
+    N = params.Natm
+    return dict(params=params, X=X, V=V, Xi=Xi, mass=mass, atype=atype,
+                xsides=np.zeros(N, dtype=np.int32), tags=tags)
+
+
 def make_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A=0.0,
                   centre=False):
+    """The spec-mode cascade slab (fib_md_gb300.spec_slab): 300 K
+    Maxwell-Boltzmann velocities, bottom 2 planes fixed, next 4
+    thermostatted, the ion 10 A above the surface (at a seeded point, or the
+    slab centre), atoms 35 A above the surface removed."""
     import fib_md_gb300 as fm
 
     p = fm.params_default()
-    p.mode = fm.MODE_SPEC
-    s = fm.crystal_system(cells, 1, -seed, params=p)
-    p = s.params
-    N, nsg = p.Natm, p.Nsg
-    rs = np.random.default_rng(seed)
-    # Maxwell-Boltzmann at 300 K, zero net momentum
-    V = np.zeros((N, 3), order="F")
-    sd = np.sqrt(KB * 300.0 / s.mass[:nsg])
-    V[:nsg] = rs.normal(size=(nsg, 3)) * sd[:, None]
-    V[:nsg] -= (s.mass[:nsg, None] * V[:nsg]).sum(0) / s.mass[:nsg].sum()
-    # layers: (001) planes are a/4 apart; bottom 2 fixed, next 4 thermostatted
-    z = s.X[:nsg, 2]
-    tags = np.zeros(N, dtype=np.uint32)
-    layer = np.rint(z / (A_LAT / 4)).astype(int)
-    tags[:nsg][layer < 2] = fm.TAG_FROZEN
-    tags[:nsg][(layer >= 2) & (layer < 6)] = fm.TAG_THERMO
-    V[:nsg][layer < 2] = 0.0
-    # the ion: 10 A above the surface, seeded point and azimuth
-    surf = z.max()
-    az = rs.uniform(0.0, 2 * np.pi)
-    th = np.deg2rad(polar_deg)
-    speed = np.sqrt(2 * energy_eV * p.ec / p.massGa)
-    X = s.X.copy(order="F")
-    xy = [0.5 * p.Lb[0], 0.5 * p.Lb[1]] if centre else \
-        [rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1])]
-    X[nsg] = [xy[0], xy[1], surf + 10e-10]
-    V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
-    p.Ttar1 = 300.0
-    p.tau_spec = 1.0e-13
-    p.remove_z = surf + 15e-10 + 20e-10  # sputtered atoms well above the surface leave
     p.list_skin = list_skin_A * 1e-10
-    return dict(params=p, X=X, V=V, Xi=s.Xi.copy(order="F"), mass=s.mass.copy(),
-                atype=s.atype.copy(), xsides=np.zeros(N, dtype=np.int32), tags=tags)
+    s = fm.spec_slab(cells, seed, energy_eV, polar_deg, ion_height=10e-10,
+                     remove_above=35e-10, params=p, impact_xy=_impact_xy(cells, centre))
+    return _as_workload(s.params, s.X, s.V, s.Xi, s.mass, s.atype, s.tags)
+
+
+def oracle_workload(cells, seed=2001, energy_eV=5000.0, polar_deg=7.0, list_skin_A=0.0,
+                    centre=False):
+    """The same slab from the oracle's restatements alone (oracle_ffi.spec_slab
+    draws the same numbers in the same order): the reference arm and the CPU
+    baseline load nothing of the GPU package."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_ffi as of
+
+    p = of.params_default()
+    p.list_skin = list_skin_A * 1e-10
+    s = of.spec_slab(cells, seed, energy_eV, polar_deg, ion_height=10e-10,
+                     remove_above=35e-10, params=p, impact_xy=_impact_xy(cells, centre))
+    return _as_workload(s["params"], s["X"], s["V"], s["Xi"], s["mass"], s["atype"], s["tags"])
+
+
+def fresh_state(g, w):
+    """A cascade's start on context g: upload of the seeded initial state,
+    tags, the ion fired, lists built, the first force."""
+    g.upload(w["X"], w["V"], None, w["Xi"], w["mass"], w["atype"], w["xsides"])
+    g.set_tags(w["tags"])
+    g.set_impact(1)
+    g.si_nlist()
+    g.si_force()
 
 
 def make_ctx(w, precision):
@@ -130,12 +149,24 @@ def make_ctx(w, precision):
     p = w["params"].copy()
     p.precision = precision
     g = fm.FibMD(p)
-    g.upload(w["X"], w["V"], None, w["Xi"], w["mass"], w["atype"], w["xsides"])
-    g.set_tags(w["tags"])
-    g.set_impact(1)
-    g.si_nlist()
-    g.si_force()
+    fresh_state(g, w)
     return g
+
+
+def workload_config(args, cells, N):
+    """The `config` object of both arms' JSON lines (static: what is run)."""
+    return {
+        "workload": f"Si slab {cells[0]}x{cells[1]}x{cells[2]} unit cells ({N - 1} Si + 1 Ga), "
+                    "5 keV Ga at 7 deg, 10 A above the surface, 300 K, spec mode",
+        "atoms": N,
+        "window": f"MD steps 1-{args.md_steps} of the cascade from the ion's start; every "
+                  "bench step starts from the seeded initial state",
+        "md_steps_per_step": args.md_steps, "mode": "spec",
+        "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
+        "seed": 2001,
+        "parallelism": "replicas (one cascade per GPU)",
+        "l2": "flushed before every timed step",
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -191,21 +222,26 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-def run_device(g, torch, stream, steps, md_steps, flush):
-    """Times `steps` bench steps on the device; returns per-step seconds."""
-    times = []
-    lt, t, T = 0, 0.0, 300.0
+def run_windows(g, w, torch, stream, steps, md_steps, flush):
+    """`steps` bench steps on the device: each a fresh start of the cascade
+    (untimed: upload, tags, lists, first force), an L2 flush, then MD steps
+    1..md_steps timed with CUDA events on the library's stream. Returns the
+    per-step seconds and the list rebuilds inside the timed steps."""
+    times, rebuilds = [], 0
     for _ in range(steps):
+        fresh_state(g, w)
+        rb0 = g.work_counters()[4]
         flush.zero_()
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        lt, t, T, _ = g.steps(2, md_steps, lt, t, T)
+        g.steps(2, md_steps, 0, 0.0, 300.0)
         e1.record(stream)
         e1.synchronize()
         times.append(e0.elapsed_time(e1) * 1e-3)
-    return times
+        rebuilds += g.work_counters()[4] - rb0
+    return times, rebuilds
 
 
 def flops_per_force(counts):
@@ -254,26 +290,25 @@ def bench_ours(args, rank, world, dist):
     g.set_option("timers", 0)
     g.set_option("graph", 0 if args.no_graph else 1)
     stream = torch.cuda.ExternalStream(g.stream_ptr)
-    run_device(g, torch, stream, args.warmup, args.md_steps, flush)
+    run_windows(g, w, torch, stream, args.warmup, args.md_steps, flush)
     barrier()
-    rb0 = g.work_counters()[4]
     with ClockSampler(dev) as clk:
         w0 = time.perf_counter()
-        times = run_device(g, torch, stream, args.steps, args.md_steps, flush)
+        times, rebuilds = run_windows(g, w, torch, stream, args.steps, args.md_steps, flush)
         barrier()
         wall = time.perf_counter() - w0
-    rebuilds = g.work_counters()[4] - rb0
     stage_end = int(g.get_option("stage"))
     X_end, _, _ = g.download()
     value, t_dev, atom_steps = replica_rate(dist, float(N) * args.md_steps * args.steps,
                                             sum(times), "cuda")
     # the main force kernel, timed live with CUDA events on the library's
-    # stream over a segment run launch by launch (events cannot sit inside
-    # the graph's conditional bodies)
+    # stream over the window's first steps run launch by launch (events
+    # cannot sit inside the graph's conditional bodies), from a fresh start
     g.set_option("graph", 0)
     g.set_option("kernel_timing", 1)
+    fresh_state(g, w)
     g.kernel_time(reset=True)
-    run_device(g, torch, stream, 1, min(args.md_steps, 200), flush)
+    g.steps(2, min(args.md_steps, 1000), 0, 0.0, 300.0)
     fk_total, fk_n = g.kernel_time(reset=True)
     g.set_option("kernel_timing", 0)
     g.set_option("graph", 0 if args.no_graph else 1)
@@ -283,53 +318,73 @@ def bench_ours(args, rank, world, dist):
     fk_avg = fk_total / max(fk_n, 1)
     achieved = flops / fk_avg / 1e12
 
-    # ---- end to end through the C-ABI with pinned host buffers
+    # ---- end to end through the C-ABI with pinned host buffers: per step
+    # the initial state goes up, the cascade runs, the final state comes down
     e2e = None
     if not args.no_e2e:
-        def pinned(shape_fortran):
-            n = int(np.prod(shape_fortran))
-            t = torch.empty(n, dtype=torch.float64, pin_memory=True)
-            a = t.numpy()
-            return a.reshape(shape_fortran[::-1]).T if len(shape_fortran) > 1 else a
+        import ctypes as C
 
-        X, V, F = g.download()
-        hX, hV, hF, hXi = (pinned((N, 3)) for _ in range(4))
-        hX[:], hV[:], hF[:], hXi[:] = X, V, F, w["Xi"]
+        def pinned(shape, dtype=torch.float64):
+            n = int(np.prod(shape))
+            a = torch.empty(n, dtype=dtype, pin_memory=True).numpy()
+            return a.reshape(shape[::-1]).T if len(shape) > 1 else a
+
+        hX, hV, hXi = (pinned((N, 3)) for _ in range(3))
+        hX[:], hV[:], hXi[:] = w["X"], w["V"], w["Xi"]
         hm = pinned((N,))
         hm[:] = w["mass"]
-        ha = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+        ha = pinned((N,), torch.int32)
         ha[:] = w["atype"]
-        hs = torch.empty(N, dtype=torch.int32, pin_memory=True).numpy()
+        hs = pinned((N,), torch.int32)
         hs[:] = w["xsides"]
-        lt, tm, T = 0, 0.0, 300.0
+        ht = pinned((N,), torch.int32)
+        ht[:] = w["tags"].astype(np.int32)
+        oX, oV, oF = (pinned((N, 3)) for _ in range(3))
+        lib, h = g.lib, g.h
+        dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        tp = ht.ctypes.data_as(C.POINTER(C.c_uint32))
+
+        def cascade():
+            for rc in (lib.fibmd_gpu_upload(h, dp(hX), dp(hV), None, dp(hXi), dp(hm), ip(ha),
+                                            ip(hs)),
+                       lib.fibmd_gpu_set_tags(h, tp),
+                       lib.fibmd_gpu_set_impact(h, 1),
+                       lib.fibmd_gpu_nlist(h),
+                       lib.fibmd_gpu_force(h, None, None, None)):
+                g._check(rc, "e2e set-up")
+            g.steps(2, args.md_steps, 0, 0.0, 300.0)
+            g._check(lib.fibmd_gpu_download(h, dp(oX), dp(oV), dp(oF)), "e2e download")
+
+        cascade()
         barrier()
         w0 = time.perf_counter()
         for _ in range(args.steps):
-            g.upload(hX, hV, hF, hXi, hm, ha, hs)
-            lt, tm, T, _ = g.steps(2, args.md_steps, lt, tm, T)
-            X, V, F = g.download()
-            hX[:], hV[:], hF[:] = X, V, F
+            cascade()
         barrier()
         t_e2e = time.perf_counter() - w0
         e2e_value, _, _ = replica_rate(dist, float(N) * args.md_steps * args.steps, t_e2e, "cuda")
         e2e = {"value": e2e_value, "unit": "atom-steps/s",
-               "h2d_bytes_per_step": N * (4 * 24 + 8 + 4 + 4),
-               "d2h_bytes_per_step": N * 3 * 24}
+               "h2d_bytes_per_step": N * (3 * 24 + 8 + 4 + 4 + 4),
+               "d2h_bytes_per_step": N * 3 * 24,
+               "what": "per step: upload of the initial state (X, V, Xi, mass, atype, xsides) "
+                       "and the tags from pinned host memory, si_nlist, si_force, the "
+                       f"{args.md_steps} MD steps, download of X, V, F to pinned host memory"}
     g.close()
 
-    # ---- plain binary64 on the same workload
+    # ---- plain binary64 on the same window
     g64 = make_ctx(w, fm.PREC_FP64)
     g64.set_option("timers", 0)
     s64 = torch.cuda.ExternalStream(g64.stream_ptr)
-
-    n64 = args.fp64_steps if args.fp64_steps > 0 else max(2, args.steps // 2)
-    run_device(g64, torch, s64, max(1, args.warmup - 1), args.md_steps, flush)
+    n64 = max(1, args.fp64_steps)
+    run_windows(g64, w, torch, s64, 1, args.md_steps, flush)
     barrier()
-    t64 = run_device(g64, torch, s64, n64, args.md_steps, flush)
+    t64, rb64 = run_windows(g64, w, torch, s64, n64, args.md_steps, flush)
     g64.set_option("graph", 0)
     g64.set_option("kernel_timing", 1)
+    fresh_state(g64, w)
     g64.kernel_time(reset=True)
-    run_device(g64, torch, s64, 1, min(args.md_steps, 50), flush)
+    g64.steps(2, min(args.md_steps, 200), 0, 0.0, 300.0)
     f64_total, f64_n = g64.kernel_time(reset=True)
     g64.si_force()
     c64 = g64.work_counters()
@@ -356,7 +411,7 @@ def bench_ours(args, rank, world, dist):
         if bpa > 0:
             traffic = bpa * N
     out = {
-        "metric": "atom-steps/s (256k-atom Si slab, 5 keV Ga, mixed precision)",
+        "metric": METRIC,
         "value": value,
         "unit": "atom-steps/s",
         "n_gpus": world,
@@ -367,22 +422,17 @@ def bench_ours(args, rank, world, dist):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 force arithmetic, f64 accumulation/positions/VV",
-        "data": "synthetic",
-        "config": {
-            "workload": f"Si slab {cells[0]}x{cells[1]}x{cells[2]} unit cells "
-                        f"({N - 1} Si + 1 Ga), 5 keV Ga at 7 deg, variable dt, "
-                        f"{args.md_steps} MD steps per bench step",
-            "atoms": N, "md_steps_per_step": args.md_steps, "mode": "spec",
-            "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
-            "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
-            "force_stage": "autotuned every 1000 steps among 8 or 10 staged legs per "
-                           "thread and 8 lanes per centre (1); "
-                           f"{stage_end} at the end of the timed run",
-            "parallelism": f"replicas x{world}", "l2": "flushed between timed steps",
-        },
+        "data": "synthetic (seeded)",
+        "config": workload_config(args, cells, N),
+        "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
+        "force_stage": {"autotune": "before every 1000 steps among 8 or 10 staged legs per "
+                                    "thread and 8 lanes per centre (1)",
+                        "at_end": stage_end},
         "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
-                 "mixed_over_fp64": value / value64,
+                 "window": "the same", "mixed_over_fp64": value / value64,
+                 "ms_per_step": 1e3 * sum(t64) / n64,
                  "force_kernel_ms": 1e3 * f64_avg,
+                 "rebuild_fraction": rb64 / float(args.md_steps * n64),
                  "roofline": {"bound": "fp64", "achieved": flops_per_force(c64) / f64_avg / 1e12,
                               "peak": fp64_peak, "unit": "TFLOP/s",
                               "frac": flops_per_force(c64) / f64_avg / 1e12 / fp64_peak,
@@ -392,6 +442,8 @@ def bench_ours(args, rank, world, dist):
                      "traffic": traffic, "flops_per_launch": flops,
                      "bytes_per_launch_algorithmic": 56 * N,
                      "force_kernel_ms": 1e3 * fk_avg, "launches": fk_n,
+                     "timed_over": f"the window's first {min(args.md_steps, 1000)} steps, "
+                                   "launch by launch",
                      "peak_source": "measured in this run (FFMA loop)"},
         "roofline_hbm": {"bound": "hbm", "achieved": step_bytes / md_step_s / 1e9,
                          "peak": hbm_peak, "unit": "GB/s",
@@ -412,13 +464,13 @@ def bench_ours(args, rank, world, dist):
         # per MD step: drift, rebuild condition, force (main with the Moliere
         # blocks, many-leg; one kernel on the 8-lanes-per-centre path), kick,
         # kick reduction = 6; per step pair the loop control; 9 kernels per
-        # list rebuild; the loop set-up per bench step. Launch by launch: the
-        # 9 list kernels every step (they return at once when no rebuild is
-        # due), no condition or loop kernels
+        # list rebuild; the loop set-up per 1000-step chunk. Launch by launch:
+        # the 9 list kernels every step (they return at once when no rebuild
+        # is due), no condition or loop kernels
         "gpu_launches": int((14 if stage_end != 1 else 13) * args.md_steps * args.steps
                             if args.no_graph else
                             (6.5 if stage_end != 1 else 5.5) * args.md_steps * args.steps +
-                            9 * rebuilds + args.steps),
+                            9 * rebuilds + args.steps * ((args.md_steps + 999) // 1000)),
         "rebuild_fraction": rebuilds / float(args.md_steps * args.steps),
         "wall_s_timed": wall,
         "clocks": clk.summary(),
@@ -784,72 +836,143 @@ def bench_dose(args):
 
 
 # ---------------------------------------------------------------------------
-def _oracle_slab(cells, nthreads):
-    """The bench slab in the oracle (binary64, the reference's algorithm):
-    lists built (timed) and the first force evaluated."""
+# config 1: the small slab in plain binary64 on the GPU beside the oracle
+def bench_config1(args, repeats=3, cpu_sample=200):
+    """8x8x8 unit cells (4096 Si + 1 Ga), 500 eV Ga at normal incidence 10 A
+    above the surface (seed 1001), 300 K, the 2000 variable-dt steps from the
+    ion's start on the GPU in binary64 (and in mixed precision), each run
+    from a fresh upload, timed with CUDA events (median of `repeats`); the
+    oracle's spec-mode step on the same slab over all host cores, a sample
+    of `cpu_sample` steps after an untimed tenth."""
+    import torch
+
+    import fib_md_gb300 as fm
+
+    cells, steps = (8, 8, 8), 2000
+    w = make_workload(cells, seed=1001, energy_eV=500.0, polar_deg=0.0,
+                      list_skin_A=args.list_skin)
+    N = w["params"].Natm
+    res = {}
+    for name, prec in (("gpu_fp64", fm.PREC_FP64), ("gpu_mixed", fm.PREC_MIXED)):
+        g = make_ctx(w, prec)
+        g.set_option("timers", 0)
+        stream = torch.cuda.ExternalStream(g.stream_ptr)
+        ts = []
+        for r in range(repeats + 1):
+            fresh_state(g, w)
+            torch.cuda.synchronize()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            _, t_sim, _, _ = g.steps(2, steps, 0, 0.0, 300.0)
+            b.record(stream)
+            b.synchronize()
+            if r > 0:
+                ts.append(a.elapsed_time(b) / 1e3)
+        g.close()
+        sec = statistics.median(ts)
+        res[name] = {"atom_steps_per_s": N * steps / sec, "ms_per_run": 1e3 * sec,
+                     "simulated_ps": t_sim * 1e12}
+    nthreads = os.cpu_count() or 1
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_ffi as of
 
-    o, rng, Xr = of.crystal(cells, 1, -2001)
-    w = make_workload(cells)
-    o.X[:] = w["X"]
-    o.V[:] = w["V"]
+    ow = oracle_workload(cells, seed=1001, energy_eV=500.0, polar_deg=0.0,
+                         list_skin_A=args.list_skin)
+    p = ow["params"].copy()
+    o = of.Oracle(p)
+    o.load(ow["X"], ow["V"], ow["Xi"], ow["mass"], ow["atype"], ow["xsides"])
     o.set_impact(1)
-    t0 = time.perf_counter()
+    o.spec_init(ow["tags"], 0.0)
     o.si_nlist()
-    t_nl = time.perf_counter() - t0
     o.F[:] = o.si_force(nthreads=nthreads)
-    return o, t_nl
+    _oracle_sample(o, cpu_sample // 10, nthreads)
+    cpu = _oracle_sample(o, cpu_sample, nthreads)
+    o.close()
+    return {
+        "config": f"8x8x8 unit cells ({N - 1} Si + 1 Ga), 500 eV Ga at normal incidence 10 A "
+                  f"above the surface, seed 1001, 300 K, {steps} variable-dt steps from the "
+                  "ion's start, spec mode, list skin "
+                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+        **res,
+        "cpu_oracle": {"atom_steps_per_s": cpu, "cores": nthreads, "kind": "port",
+                       "algorithm": CPU_ALGORITHM,
+                       "sample": f"MD steps {cpu_sample // 10 + 1}-{cpu_sample // 10 + cpu_sample}"
+                                 f" of the same cascade after {cpu_sample // 10} untimed"},
+        "gpu_fp64_over_cpu": res["gpu_fp64"]["atom_steps_per_s"] / cpu,
+    }
 
 
-def _oracle_sample(o, t_nl, first, sample_steps, nthreads, state):
-    """Atom-steps/s of sample_steps onestep calls from step `first` on,
-    with one list build per 50 steps (ntlist_i) charged at its measured
-    cost; state = (time, temperature), advanced."""
-    tm, T = state
+# ---------------------------------------------------------------------------
+# the CPU side: the oracle (binary64, the reference's si_nlist/si_force with
+# the spec-mode step) on the same cascade, set up without the GPU package
+def _oracle_cascade(cells, list_skin_A, nthreads):
+    """The oracle at the cascade's start: the seeded slab, spec-mode lists
+    built, the first force evaluated (all host threads for the force)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    import oracle_ffi as of
+
+    w = oracle_workload(cells, list_skin_A=list_skin_A)
+    p = w["params"].copy()
+    p.mode = 1
+    o = of.Oracle(p)
+    o.load(w["X"], w["V"], w["Xi"], w["mass"], w["atype"], w["xsides"])
+    o.set_impact(1)
+    o.spec_init(w["tags"], 0.0)
+    o.si_nlist()
+    o.F[:] = o.si_force(nthreads=nthreads)
+    return o
+
+
+def _oracle_sample(o, sample_steps, nthreads):
+    """Atom-steps/s of the next sample_steps spec-mode steps (rebuilds
+    included as they fall due)."""
     t0 = time.perf_counter()
-    for k in range(sample_steps):
-        tm, T = o.onestep(2, first + k + 1, tm, T, nthreads)
-    t_st = time.perf_counter() - t0
-    return o.N / (t_st / sample_steps + t_nl / 50.0), (tm, T)
+    for _ in range(sample_steps):
+        o.spec_step(nthreads)
+    return o.N * sample_steps / (time.perf_counter() - t0)
 
 
-def cpu_baseline(cells, sample_steps, nthreads=None):
-    """The oracle's onestep (binary64, the reference's algorithm) on the same
-    slab over all host cores; one list build per 50 steps as ntlist_i; one
-    untimed sample first (first touch of the slab's pages)."""
+CPU_ALGORITHM = ("the oracle: binary64 restatement of the reference's si_nlist (cell lists) "
+                 "and si_force (table SW 2-body, Moliere, connected-triplet SW 3-body) with "
+                 "the spec-mode step; its force OpenMP over all host threads")
+
+
+def cpu_baseline(cells, list_skin_A, sample_steps, nthreads=None):
+    """The oracle on the cascade's first steps over all host cores: an
+    untimed sample of a third of the steps, then sample_steps timed."""
     nthreads = nthreads or os.cpu_count() or 1
-    o, t_nl = _oracle_slab(cells, nthreads)
-    _, state = _oracle_sample(o, t_nl, 0, sample_steps, nthreads, (0.0, 300.0))
-    value, _ = _oracle_sample(o, t_nl, sample_steps, sample_steps, nthreads, state)
+    o = _oracle_cascade(cells, list_skin_A, nthreads)
+    _oracle_sample(o, max(1, sample_steps // 3), nthreads)
+    value = _oracle_sample(o, sample_steps, nthreads)
+    first = max(1, sample_steps // 3) + 1
     N = o.N
     o.close()
     return {"value": value, "unit": "atom-steps/s", "cores": nthreads, "kind": "port",
-            "sample": f"{sample_steps} onestep calls + 1 si_nlist (weighted 1/50) on the "
-                      f"{N}-atom slab after {sample_steps} untimed, OpenMP over "
-                      f"{nthreads} threads"}
+            "algorithm": CPU_ALGORITHM,
+            "sample": f"MD steps {first}-{first + sample_steps - 1} of the {N}-atom cascade "
+                      f"(after {first - 1} untimed), {nthreads} threads"}
 
 
-def cpu_reference_run(cells, warmup, steps, sample_steps, nthreads=None):
-    """The reference arm: the oracle slab set up once, `warmup` untimed
-    samples, then `steps` timed samples of sample_steps onestep calls each
-    (a bounded sample of the workload per step); the median rate."""
+def cpu_reference_run(cells, list_skin_A, warmup, steps, sample_steps, nthreads=None):
+    """The reference arm: the oracle's cascade set up once, `warmup` untimed
+    samples, then `steps` timed samples of sample_steps spec-mode steps each
+    (the cascade goes on from sample to sample); the median rate."""
     nthreads = nthreads or os.cpu_count() or 1
-    o, t_nl = _oracle_slab(cells, nthreads)
-    state, first, vals = (0.0, 300.0), 0, []
+    o = _oracle_cascade(cells, list_skin_A, nthreads)
+    vals = []
     for n in range(warmup + steps):
-        v, state = _oracle_sample(o, t_nl, first, sample_steps, nthreads, state)
-        first += sample_steps
+        v = _oracle_sample(o, sample_steps, nthreads)
         if n >= warmup:
             vals.append(v)
     N = o.N
     o.close()
     return statistics.median(vals), {
         "value": statistics.median(vals), "unit": "atom-steps/s", "cores": nthreads,
-        "kind": "port",
-        "sample": f"per step {sample_steps} onestep calls + 1 si_nlist (weighted 1/50) on the "
-                  f"{N}-atom slab, OpenMP over {nthreads} threads; median of {steps} steps "
-                  f"after {warmup} untimed"}
+        "kind": "port", "algorithm": CPU_ALGORITHM,
+        "sample": f"per step {sample_steps} MD steps of the {N}-atom cascade, continuing from "
+                  f"step to step over steps 1-{(warmup + steps) * sample_steps} of the window "
+                  f"({warmup} untimed samples first), {nthreads} threads; median of {steps}"}
 
 
 def main():
@@ -861,13 +984,15 @@ def main():
         if rank != 0:
             return 0
         steps, warmup = max(1, args.steps), max(0, args.warmup)
-        v, cb = cpu_reference_run(cells, warmup, steps, max(2, args.cpu_sample_steps // 2))
-        out = {"impl": "reference", "metric": "atom-steps/s (256k-atom Si slab, 5 keV Ga, mixed precision)",
+        v, cb = cpu_reference_run(cells, args.list_skin, warmup, steps,
+                                  max(2, args.cpu_sample_steps // 4))
+        N = 8 * cells[0] * cells[1] * cells[2] + 1
+        out = {"impl": "reference", "metric": METRIC,
                "value": v, "unit": "atom-steps/s", "n_gpus": 0, "steps": steps,
                "warmup": warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "f64", "data": "synthetic",
-               "config": {"workload": f"Si slab {cells[0]}x{cells[1]}x{cells[2]} unit cells, "
-                                      "reference onestep (CPU oracle port)"},
+               "dtype": "f64", "data": "synthetic (seeded)",
+               "config": workload_config(args, cells, N),
+               "cpu_algorithm": CPU_ALGORITHM,
                "cpu_baseline": cb,
                "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
@@ -948,9 +1073,11 @@ def main():
         out["dose"] = bench_dose(args)
     if args.large_steps > 0 and rank == 0:
         out["large"] = bench_large(args)
+    if not args.no_config1 and rank == 0:
+        out["config1"] = bench_config1(args)
     if rank == 0:
         if not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(cells, args.cpu_sample_steps)
+            out["cpu_baseline"] = cpu_baseline(cells, args.list_skin, args.cpu_sample_steps)
         print(json.dumps(out))
     if dist is not None:
         dist.destroy_process_group()

@@ -99,6 +99,7 @@ SIGNATURES = {
     "fibmd_gpu_upload": (_I, [_VP, _DP, _DP, _DP, _DP, _DP, _IP, _IP]),
     "fibmd_gpu_download": (_I, [_VP, _DP, _DP, _DP]),
     "fibmd_gpu_set_tags": (_I, [_VP, C.POINTER(C.c_uint32)]),
+    "fibmd_gpu_get_tags": (_I, [_VP, C.POINTER(C.c_uint32)]),
     "fibmd_gpu_set_atom": (_I, [_VP, _I, _DP, _DP]),
     "fibmd_gpu_set_impact": (_I, [_VP, _I]),
     "fibmd_gpu_ionrun": (_I, [_VP, _I]),
@@ -140,6 +141,7 @@ SIGNATURES = {
     "fibmd_host_initranions": (None, [C.POINTER(Rng), _I, _D, _DP]),
     "fibmd_host_init_state": (_I, [C.POINTER(Params), C.POINTER(Rng), _D, _DP, _DP, _DP, _DP, _IP]),
     "fibmd_host_knock": (_I, [C.POINTER(Params), C.POINTER(Rng), _I, _D, _D, _D, _DP, _I, _DP, _DP]),
+    "fibmd_host_maxwell": (None, [C.POINTER(Rng), _I, _I, _DP, _D, _D, _DP]),
 }
 
 _lib: C.CDLL | None = None

@@ -968,6 +968,18 @@ int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags) {
   return FIBMD_OK;
 }
 
+int fibmd_gpu_get_tags(fibmd_ctx* ctx, uint32_t* tags) {
+  if (!ctx || !tags) return FIBMD_EINVAL;
+  if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "get_tags before upload");
+  const int N = ctx->P.N;
+  std::vector<uint32_t> fl((size_t)N);
+  CK(cudaMemcpyAsync(fl.data(), ctx->S.flags, sizeof(uint32_t) * (size_t)N,
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < N; i++) tags[i] = fl[(size_t)i] & 0xffu;
+  return FIBMD_OK;
+}
+
 int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F) {
   if (!ctx) return FIBMD_EINVAL;
   if (!ctx->uploaded) return fail(ctx, FIBMD_ESTATE, "download before upload");

@@ -123,6 +123,12 @@ module fibmd_gpu_mod
        integer(c_int32_t) :: tags(*)
      end function fibmd_gpu_set_tags
 
+     integer(c_int) function fibmd_gpu_get_tags(ctx, tags) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       integer(c_int32_t) :: tags(*)
+     end function fibmd_gpu_get_tags
+
      integer(c_int) function fibmd_gpu_set_atom(ctx, i, x, v) bind(C)
        import
        type(c_ptr), value :: ctx

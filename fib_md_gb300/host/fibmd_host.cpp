@@ -292,6 +292,33 @@ int fibmd_host_init_state(const fibmd_params* p, fibmd_rng* r, double Uo, double
   return FIBMD_OK;
 }
 
+void fibmd_host_maxwell(fibmd_rng* r, int n, int N, const double* mass, double T, double kB,
+                        double* V) {
+  // Box-Muller (Box and Muller, 1958) on consecutive ran1 pairs, the method
+  // initranions uses for its impact table (data.f90:263-285)
+  const double Pi = 4. * std::atan(1.0);
+  const long long nv = 3 * (long long)n;
+  for (long long m = 0; m < nv; m += 2) {
+    const double u1 = fibmd_host_ran1(r);
+    const double u2 = fibmd_host_ran1(r);
+    const double rad = std::sqrt(-2. * std::log(u1));
+    const double z[2] = {rad * std::cos(2. * Pi * u2), rad * std::sin(2. * Pi * u2)};
+    for (int q = 0; q < 2 && m + q < nv; q++) {
+      const long long e = m + q;
+      const int i = (int)(e / 3), d = (int)(e % 3);
+      V[(size_t)d * (size_t)N + (size_t)i] = z[q] * std::sqrt(kB * T / mass[i]);
+    }
+  }
+  double P[3] = {0.0, 0.0, 0.0}, M = 0.0;
+  for (int i = 0; i < n; i++) {
+    M = M + mass[i];
+    for (int d = 0; d < 3; d++) P[d] = P[d] + mass[i] * V[(size_t)d * (size_t)N + (size_t)i];
+  }
+  for (int i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++)
+      V[(size_t)d * (size_t)N + (size_t)i] = V[(size_t)d * (size_t)N + (size_t)i] - P[d] / M;
+}
+
 int fibmd_host_knock(const fibmd_params* p, fibmd_rng* r, int knc, double eV, double phiz,
                      double phixy, const double* Xrand, int Nrand, double x[3], double v[3]) {
   const double Pi = 4. * std::atan(1.0);

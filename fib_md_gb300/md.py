@@ -35,6 +35,16 @@ def _fortran(a, dtype=np.float64) -> np.ndarray:
     return np.asfortranarray(np.asarray(a, dtype=dtype))
 
 
+def as_params(p) -> Params:
+    """A copy of p as this package's Params: p may be any ctypes mirror of
+    fibmd_params with the same layout (the oracle harness keeps its own)."""
+    if C.sizeof(type(p)) != C.sizeof(Params):
+        raise TypeError(f"{type(p).__name__} is not a fibmd_params mirror")
+    q = Params()
+    C.memmove(C.byref(q), C.byref(p), C.sizeof(Params))
+    return q
+
+
 def params_default() -> Params:
     """prms.f90's constants and the reference's shipped siga.in."""
     p = Params()
@@ -45,7 +55,7 @@ def params_default() -> Params:
 def read_siga(path: str, p: Params | None = None) -> tuple[Params, Siga]:
     """Read siga.in's 45 values (prms.f90:221-275) into a Params/Siga pair."""
     lib = _abi.load()
-    p = params_default() if p is None else p.copy()
+    p = params_default() if p is None else as_params(p)
     s = Siga()
     msg = C.create_string_buffer(512)
     rc = lib.fibmd_host_read_siga(str(path).encode(), C.byref(p), C.byref(s), msg, 512)
@@ -96,7 +106,7 @@ def crystal_system(nc=(8, 8, 8), nlj: int = 1, seed: int = -1001, params: Params
     crystalline target with an explicit ran1 seed (the reference seeds from
     the wall clock, prms.f90:220,296)."""
     lib = _abi.load()
-    p = params_default() if params is None else params.copy()
+    p = params_default() if params is None else as_params(params)
     XX, xs, Lb = pureepi(*nc)
     nsg = XX.shape[0]
     p.Nsg, p.Nlj, p.Natm = nsg, nlj, nsg + nlj
@@ -151,17 +161,20 @@ def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.
     thermostat (TAG_THERMO). The ion starts ion_height above the top plane
     at a seeded (or given) point, with ion_eV along a direction polar_deg off
     the inward normal at a seeded (or given) azimuth. Atoms higher than
-    remove_above over the surface are removed during the run."""
-    p = params_default() if params is None else params.copy()
+    remove_above over the surface are removed during the run.
+
+    Every random draw continues the ran1 stream of the reference's set-up
+    (crystal_system, seed -|seed|-1): Maxwell-Boltzmann velocities by the
+    Box-Muller method (fibmd_host_maxwell), then the azimuth and the impact
+    point."""
+    p = params_default() if params is None else as_params(params)
     p.mode = _abi.MODE_SPEC
     s = crystal_system(tuple(cells), 1, -abs(int(seed)) - 1, params=p)
     p = s.params
     N, nsg = p.Natm, p.Nsg
-    rs = np.random.default_rng(int(seed))
     V = np.zeros((N, 3), order="F")
-    sd = np.sqrt(KB_SI * T / s.mass[:nsg])
-    V[:nsg] = rs.normal(size=(nsg, 3)) * sd[:, None]
-    V[:nsg] -= (s.mass[:nsg, None] * V[:nsg]).sum(0) / s.mass[:nsg].sum()
+    _abi.load().fibmd_host_maxwell(C.byref(s.rng.state), nsg, N, _dp(s.mass), float(T), p.kB,
+                                   _dp(V))
     z = s.X[:nsg, 2]
     layer = np.rint(z / (A_LATTICE / 4)).astype(int)
     tags = np.zeros(N, dtype=np.uint32)
@@ -169,11 +182,16 @@ def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.
     tags[:nsg][(layer >= fixed_layers) & (layer < fixed_layers + thermo_layers)] = _abi.TAG_THERMO
     V[:nsg][layer < fixed_layers] = 0.0
     surf = float(z.max())
-    az = rs.uniform(0.0, 2 * np.pi) if azimuth is None else float(azimuth)
+    az = 2 * np.pi * s.rng() if azimuth is None else float(azimuth)
     th = np.deg2rad(polar_deg)
     speed = np.sqrt(2 * ion_eV * p.ec / p.massGa)
     X = s.X.copy(order="F")
-    xy = (rs.uniform(0, p.Lb[0]), rs.uniform(0, p.Lb[1])) if impact_xy is None else impact_xy
+    if impact_xy is None:
+        xr = s.rng()
+        yr = s.rng()
+        xy = (xr * p.Lb[0], yr * p.Lb[1])
+    else:
+        xy = impact_xy
     X[nsg] = [xy[0], xy[1], surf + ion_height]
     V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
     p.remove_z = surf + remove_above
@@ -198,7 +216,7 @@ def dose_slab(cells, nimp: int, seed: int, ion_eV: float = 2000.0, window: float
     """A slab (spec_slab's layers, tags and 300 K velocities) with nimp ions
     for successive impacts at normal incidence, each at a seeded uniform
     point of a window x window square centred on the slab."""
-    p = params_default() if params is None else params.copy()
+    p = params_default() if params is None else as_params(params)
     p.mode = _abi.MODE_SPEC
     base = spec_slab(cells, seed, ion_eV, 0.0, ion_height=ion_height, remove_above=remove_above,
                      params=p)
@@ -301,7 +319,7 @@ class FibMD:
 
     def __init__(self, params: Params):
         self.lib = _abi.load()
-        self.params = params.copy()
+        self.params = as_params(params)
         self.N = params.Natm
         h = C.c_void_p()
         rc = self.lib.fibmd_gpu_create(C.byref(self.params), C.byref(h))
@@ -360,6 +378,23 @@ class FibMD:
         t = np.ascontiguousarray(tags, dtype=np.uint32)
         self._check(self.lib.fibmd_gpu_set_tags(self.h, t.ctypes.data_as(C.POINTER(C.c_uint32))),
                     "set_tags")
+
+    def get_tags(self) -> np.ndarray:
+        """The per-atom tags as the device holds them (TAG_REMOVED set by
+        spec-mode removal)."""
+        t = np.zeros(self.N, dtype=np.uint32)
+        self._check(self.lib.fibmd_gpu_get_tags(self.h, t.ctypes.data_as(C.POINTER(C.c_uint32))),
+                    "get_tags")
+        return t
+
+    def spec_scalars(self):
+        """(time, dt, removed lattice atoms) of the system (replica 0)."""
+        t = np.zeros(1)
+        dt = np.zeros(1)
+        rm = np.zeros(1, dtype=np.int32)
+        self._check(self.lib.fibmd_gpu_batch_scalars(self.h, _dp(t), _dp(dt), _ip(rm)),
+                    "batch_scalars")
+        return float(t[0]), float(dt[0]), int(rm[0])
 
     def set_atom(self, i: int, x, v):
         x = np.ascontiguousarray(x, dtype=np.float64)
@@ -525,7 +560,7 @@ class FibMDBatch(FibMD):
     def __init__(self, params: Params, replicas):
         """replicas: sequence of (natm, nsg, Lb[3], remove_z)."""
         self.lib = _abi.load()
-        self.params = params.copy()
+        self.params = as_params(params)
         R = len(replicas)
         arr = (Replica * R)()
         for r, (natm, nsg, Lb, rz) in enumerate(replicas):

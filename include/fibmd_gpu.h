@@ -184,6 +184,12 @@ int fibmd_gpu_download(fibmd_ctx* ctx, double* X, double* V, double* F);
 
 /* Spec-mode per-atom tags (FIBMD_TAG_* bits), (Natm) entries. */
 int fibmd_gpu_set_tags(fibmd_ctx* ctx, const uint32_t* tags);
+/* The current tags, (Natm) entries: spec mode sets FIBMD_TAG_REMOVED on the
+   device when an atom is removed (the reference's counterpart is the
+   parking of sputtered atoms in frzsptrdatms, src/temp.f90:99-127, which
+   leaves no mark); ref mode reports FIBMD_TAG_FROZEN for atoms pinned by
+   xsides. */
+int fibmd_gpu_get_tags(fibmd_ctx* ctx, uint32_t* tags);
 
 /* The device side of writeatoms (src/out.f90:62-100): the columns of an
    extended-xyz frame computed on the GPU — x y z in Angstrom ((Natm,3)

@@ -66,6 +66,16 @@ void fibmd_host_initranions(fibmd_rng* r, int Nrand, double fwhm, double* Xrand)
 int fibmd_host_init_state(const fibmd_params* p, fibmd_rng* r, double Uo, double* X,
                           double* Xi, double* V, double* mass, int* atype);
 
+/* Maxwell-Boltzmann velocities at temperature T (K) for rows 0..n-1 of V
+   ((N,3) column-major; mass in kg, kB in J/K): normal deviates by the
+   Box-Muller method from consecutive ran1 pairs, filled atom by atom
+   (x, y, z), scaled by sqrt(kB T / m), then the mass-weighted mean velocity
+   removed. The reference starts from uniform velocities (randvel,
+   src/data.f90:169-204) and a warm-up; this is the spec-mode set-up's
+   thermal start, which has no counterpart there. */
+void fibmd_host_maxwell(fibmd_rng* r, int n, int N, const double* mass, double T, double kB,
+                        double* V);
+
 /* knock (src/knock.f90:21-55): start point and velocity of ion knc.
    NINT(ran1*Nrand) may be 0 in the reference (an out-of-bounds read); here
    index 0 is taken as 1. Returns the 1-based atom index (Nsg + knc). */

@@ -183,13 +183,19 @@ int orc_init(orc_sys* s, const fibmd_params* p) {
   s->ML2 = Nl * 40;
   double sigmax = p->sigmaGe > p->sigmaSi ? p->sigmaGe : p->sigmaSi;
   s->rc = p->listfac * p->al * sigmax;
+  double rlj2 = 2.5 * sigmax;
+  s->rclj = p->listfac * rlj2;
+  s->rlj2 = rlj2 * rlj2;
+  s->spec = p->mode == FIBMD_MODE_SPEC;
+  if (s->spec && p->list_skin > 0.0) {
+    /* spec mode: interaction cutoff + skin */
+    s->rc = 0.999 * p->al * sigmax + p->list_skin;
+    s->rclj = rlj2 + p->list_skin;
+  }
   for (int d = 0; d < 3; d++) {
     int n = f_int(s->Lb[d] / s->rc);
     s->Nc[d] = n > 1 ? n : 1;
   }
-  double rlj2 = 2.5 * sigmax;
-  s->rclj = p->listfac * rlj2;
-  s->rlj2 = rlj2 * rlj2;
 
   s->cap2 = s->ML2 > 64 ? s->ML2 : 64;
   s->cap3 = s->ML3 > 64 ? s->ML3 : 64;
@@ -210,6 +216,18 @@ int orc_init(orc_sys* s, const fibmd_params* p) {
   s->mass = (double*)calloc(N, sizeof(double));
   s->atype = (int*)calloc(N, sizeof(int));
   s->xsides = (int*)calloc(N, sizeof(int));
+  if (s->spec) {
+    s->tags = (unsigned*)calloc(N, sizeof(unsigned));
+    s->Xb = (double*)calloc(N * 3, sizeof(double));
+    /* the half skin, the smaller of the two lists' skins (1 % margin) */
+    double skin = s->rc - 0.999 * p->al * sigmax;
+    if (s->rclj - rlj2 < skin) skin = s->rclj - rlj2;
+    double half = 0.5 * skin * 0.99;
+    s->sp_trig2 = half * half;
+    s->sp_zopen = p->remove_z > 0.0 && p->remove_z + s->rc < s->Lb[2];
+    s->sp_remove_zlo = s->sp_zopen ? -10.0e-10 : -1.0e300;
+    s->sp_thermo_s = 1.0;
+  }
   orc_ionrun(s, 1);
   s->impact = 0;
   s->atom_is_fast = 1;
@@ -232,6 +250,8 @@ void orc_free(orc_sys* s) {
   free(s->mass);
   free(s->atype);
   free(s->xsides);
+  free(s->tags);
+  free(s->Xb);
   memset(s, 0, sizeof(*s));
 }
 
@@ -244,6 +264,12 @@ static void chainlist(orc_sys* s, int* LL, int* HOC, const double* X) {
   for (int d = 0; d < 3; d++) HMf[d] = s->Lb[d] / (double)s->Nc[d];
   memset(HOC, 0, sizeof(int) * (size_t)s1 * s2 * s3);
   for (int i = 1; i <= N; i++) {
+    /* spec mode bins the lattice atoms still in the run; pairs with an ion
+       are found by the ion scan of spec_moliere_pairs */
+    if (s->spec && (s->atype[i - 1] >= 3 || (s->tags[i - 1] & FIBMD_TAG_REMOVED))) {
+      LL[i - 1] = 0;
+      continue;
+    }
     int ic[3];
     for (int d = 0; d < 3; d++) {
       double x = CM(X, N, i, d);
@@ -311,6 +337,48 @@ static inline void min_image(const orc_sys* s, const double* X, int i, int j,
     double dd = CM(X, N, i, d) - CM(X, N, j, d);
     xx[d] = dd - f_nint(dd * s->iLb[d]) * s->Lb[d];
   }
+}
+
+/* Spec mode: every pair with an ion closer than the Moliere list radius (no
+   stencil limit), each once as (i, j), i < j, in i's half list, by a direct
+   scan over the atoms for each ion; removed atoms take no part. */
+static int cmp_pair(const void* a, const void* b);
+static void spec_moliere_pairs(orc_sys* s, const double* X) {
+  int N = s->Natm;
+  double rv2lj = s->rclj * s->rclj;
+  int cap = 64, n = 0;
+  int* pr = (int*)malloc(sizeof(int) * 2 * (size_t)cap);
+  for (int a = 1; a <= N; a++) {
+    if (s->atype[a - 1] != 3 || (s->tags[a - 1] & FIBMD_TAG_REMOVED)) continue;
+    for (int b = 1; b <= N; b++) {
+      if (b == a || (s->tags[b - 1] & FIBMD_TAG_REMOVED)) continue;
+      if (s->atype[b - 1] == 3 && b < a) continue; /* an ion pair once */
+      double xx[3];
+      min_image(s, X, a, b, xx);
+      double rij2 = xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2];
+      if (!(rij2 < rv2lj)) continue;
+      if (n == cap) {
+        cap *= 2;
+        pr = (int*)realloc(pr, sizeof(int) * 2 * (size_t)cap);
+      }
+      pr[2 * n] = a < b ? a : b;
+      pr[2 * n + 1] = a < b ? b : a;
+      n++;
+    }
+  }
+  qsort(pr, (size_t)n, 2 * sizeof(int), cmp_pair);
+  grow_int(&s->nlistlj, &s->caplj, n + 1, 1);
+  int l = 0;
+  for (int i = 1; i <= N; i++) {
+    NSSLJ1(s, i) = l + 1;
+    while (l < n && pr[2 * l] == i) {
+      s->nlistlj[l] = pr[2 * l + 1];
+      l++;
+    }
+    NSSLJ2(s, i) = l;
+  }
+  s->nbr_cntlj_full = 2 * (long long)n;
+  free(pr);
 }
 
 /* ---- si_nlistG, si.f90:102-276 (one domain: P_big(i) == myid for all) --- */
@@ -451,6 +519,10 @@ void orc_si_nlist(orc_sys* s, const double* X) {
   if (nbr_cntlj >= s->MLlj) s->overflow |= 4;
   free(LL);
   free(HOC);
+  if (s->spec) {
+    spec_moliere_pairs(s, X);
+    memcpy(s->Xb, X, sizeof(double) * 3 * (size_t)N);
+  }
 }
 
 /* ---- itable2bd, si.f90:554-573 ------------------------------------------- */
@@ -582,15 +654,22 @@ static inline void triplet_force(const orc_sys* s, const double* Xp, int i,
   for (int d = 0; d < 3; d++) fk[d] = -fi[d] - fj[d];
 }
 
+/* Spec mode: an atom removed since the last list build acts on nothing
+   (its pairs and triplets are skipped until the lists drop it). */
+static inline int gone(const orc_sys* s, int i) {
+  return s->spec && (s->tags[i - 1] & FIBMD_TAG_REMOVED);
+}
+
 /* ---- si_force, si.f90:384-552 -------------------------------------------- */
 void orc_si_force(orc_sys* s, const double* Xp, double* F) {
   int N = s->Natm;
   int lim = s->Nsg + s->impact;
   memset(F, 0, sizeof(double) * 3 * (size_t)N);
   for (int i = 1; i <= N; i++) {
+    if (gone(s, i)) continue;
     for (int l = NSS1(s, i); l <= NSS2(s, i); l++) {
       int j = s->nlist2[l - 1];
-      if (i > lim || j > lim) continue;
+      if (i > lim || j > lim || gone(s, j)) continue;
       double fi[3];
       pair_sw_force(s, Xp, i, j, fi);
       for (int d = 0; d < 3; d++) {
@@ -600,7 +679,7 @@ void orc_si_force(orc_sys* s, const double* Xp, double* F) {
     }
     for (int l = NSSLJ1(s, i); l <= NSSLJ2(s, i); l++) {
       int j = s->nlistlj[l - 1];
-      if (i > lim || j > lim) continue;
+      if (i > lim || j > lim || gone(s, j)) continue;
       double fi[3];
       if (pair_mol_force(s, Xp, i, j, fi)) {
         for (int d = 0; d < 3; d++) {
@@ -615,6 +694,7 @@ void orc_si_force(orc_sys* s, const double* Xp, double* F) {
     int j = s->nlist3[(size_t)s->cap3 + l - 1];
     int k = s->nlist3[2 * (size_t)s->cap3 + l - 1];
     if (i > lim || j > lim || k > lim) continue;
+    if (gone(s, i) || gone(s, j) || gone(s, k)) continue;
     double fi[3], fj[3], fk[3];
     triplet_force(s, Xp, i, j, k, fi, fj, fk);
     for (int d = 0; d < 3; d++) {
@@ -643,9 +723,10 @@ void orc_si_force_omp(orc_sys* s, const double* Xp, double* F, int nthreads) {
     local.table_err = 0;
 #pragma omp for schedule(dynamic, 256)
     for (int i = 1; i <= N; i++) {
+      if (gone(s, i)) continue;
       for (int l = NSS1(s, i); l <= NSS2(s, i); l++) {
         int j = s->nlist2[l - 1];
-        if (i > lim || j > lim) continue;
+        if (i > lim || j > lim || gone(s, j)) continue;
         double fi[3];
         pair_sw_force(&local, Xp, i, j, fi);
         for (int d = 0; d < 3; d++) {
@@ -655,7 +736,7 @@ void orc_si_force_omp(orc_sys* s, const double* Xp, double* F, int nthreads) {
       }
       for (int l = NSSLJ1(s, i); l <= NSSLJ2(s, i); l++) {
         int j = s->nlistlj[l - 1];
-        if (i > lim || j > lim) continue;
+        if (i > lim || j > lim || gone(s, j)) continue;
         double fi[3];
         if (pair_mol_force(s, Xp, i, j, fi))
           for (int d = 0; d < 3; d++) {
@@ -670,6 +751,7 @@ void orc_si_force_omp(orc_sys* s, const double* Xp, double* F, int nthreads) {
       int j = s->nlist3[(size_t)s->cap3 + l - 1];
       int k = s->nlist3[2 * (size_t)s->cap3 + l - 1];
       if (i > lim || j > lim || k > lim) continue;
+      if (gone(s, i) || gone(s, j) || gone(s, k)) continue;
       double fi[3], fj[3], fk[3];
       triplet_force(s, Xp, i, j, k, fi, fj, fk);
       for (int d = 0; d < 3; d++) {
@@ -708,8 +790,10 @@ void orc_si_potential(orc_sys* s, const double* X, double* Utot_out, double* u) 
   double Utot = 0.;
   memset(u, 0, sizeof(double) * (size_t)N);
   for (int i = 1; i <= N; i++) {
+    if (gone(s, i)) continue;
     for (int l = NSS1(s, i); l <= NSS2(s, i); l++) {
       int j = s->nlist2[l - 1];
+      if (gone(s, j)) continue;
       double xx[3];
       min_image(s, X, i, j, xx);
       double rij = sqrt(xx[0] * xx[0] + xx[1] * xx[1] + xx[2] * xx[2]);
@@ -725,6 +809,7 @@ void orc_si_potential(orc_sys* s, const double* X, double* Utot_out, double* u) 
     }
     for (int l = NSSLJ1(s, i); l <= NSSLJ2(s, i); l++) {
       int j = s->nlistlj[l - 1];
+      if (gone(s, j)) continue;
       double xx[3];
       min_image(s, X, i, j, xx);
       double rij2 = 0.0;
@@ -749,6 +834,7 @@ void orc_si_potential(orc_sys* s, const double* X, double* Utot_out, double* u) 
     int i = s->nlist3[l - 1];
     int j = s->nlist3[(size_t)s->cap3 + l - 1];
     int k = s->nlist3[2 * (size_t)s->cap3 + l - 1];
+    if (gone(s, i) || gone(s, j) || gone(s, k)) continue;
     int ti = s->atype[i - 1] - 1, tj = s->atype[j - 1] - 1, tk = s->atype[k - 1] - 1;
     double xxij[3], xxik[3], xxjk[3];
     min_image(s, X, i, j, xxij);
@@ -1154,6 +1240,173 @@ void orc_knock(orc_sys* s, orc_rng* r, int knc, double eV, double phiz,
   CM(s->X, N, ion, 0) = CM(Xrand, Nrand, ri, 0) + s->Lb[0] / 2.0 - dx;
   CM(s->X, N, ion, 1) = CM(Xrand, Nrand, ri, 1) + s->Lb[1] / 2.0 - dy;
   CM(s->X, N, ion, 2) = s->p.knockz * L3 / 10.0;
+}
+
+/* ---- spec mode ------------------------------------------------------------
+   The specified set-up of the benchmark slabs (the reference has none of
+   it): each function restates the step of the GPU library's spec mode in
+   plain binary64 with the order of operations written out. */
+
+/* the next step and the thermostat factor from the current velocities
+   (after a kick): dt = min(dt_max, dx_max / max|v|) over the atoms in the
+   run; the Berendsen factor sqrt(1 + dt/tau (Ttar/T - 1)) of the tagged
+   layer's lattice atoms, T from their sum of m v^2 */
+static void spec_reduce(orc_sys* s) {
+  int N = s->Natm;
+  const fibmd_params* p = &s->p;
+  double vmax2 = 0.0, tsum = 0.0;
+  int tcnt = 0;
+  for (int i = 1; i <= N; i++) {
+    if (s->tags[i - 1] & FIBMD_TAG_REMOVED) continue;
+    double v1 = CM(s->V, N, i, 0), v2 = CM(s->V, N, i, 1), v3 = CM(s->V, N, i, 2);
+    double vv = v1 * v1 + v2 * v2 + v3 * v3;
+    if (vv > vmax2) vmax2 = vv;
+    if ((s->tags[i - 1] & FIBMD_TAG_THERMO) && s->atype[i - 1] < 3) {
+      tsum = tsum + s->mass[i - 1] * vv;
+      tcnt++;
+    }
+  }
+  s->sp_vmax2 = vmax2;
+  double vm = sqrt(vmax2);
+  double nd = p->dt_max;
+  if (vm > 0.0 && p->dx_max / vm < nd) nd = p->dx_max / vm;
+  s->sp_dt = nd;
+  double sf = 1.0;
+  if (tcnt > 0) {
+    double T = tsum / 3. / (double)tcnt / p->kB;
+    if (T > 0.0) sf = sqrt(1. + nd / p->tau_spec * (p->Ttar1 / T - 1.));
+  }
+  s->sp_thermo_s = sf;
+}
+
+void orc_spec_init(orc_sys* s, const unsigned* tags, double time0) {
+  if (!s->spec) return;
+  for (int i = 0; i < s->Natm; i++) s->tags[i] = tags ? tags[i] & 0xffu : 0u;
+  s->sp_time = time0;
+  s->sp_removed = s->sp_ions_removed = 0;
+  s->sp_rebuilds = 0;
+  spec_reduce(s);
+}
+
+/* round(x * qscale) to the nearest integer (ties to even) in one rounding,
+   the fixed-point coordinate of x (qscale = 2^32 / Lb) */
+static inline double fixed_coord(double x, double qscale) {
+  return fma(x, qscale, 6755399441055744.0) - 6755399441055744.0;
+}
+
+int orc_spec_step(orc_sys* s, int nthreads) {
+  int N = s->Natm;
+  const fibmd_params* p = &s->p;
+  double dt = s->sp_dt, h2 = 0.5 * dt * dt, hdt = 0.5 * dt, ts = s->sp_thermo_s;
+  double qs[3];
+  for (int d = 0; d < 3; d++) qs[d] = 4294967296.0 / s->Lb[d];
+  int trig = 0;
+  /* drift: thermostat scaling, X += V dt + F dt^2/(2m), pinning, removal
+     (on the unwrapped height), wrap of atoms that left the box, and the
+     rebuild test against the positions of the last build */
+  for (int i = 1; i <= N; i++) {
+    unsigned tg = s->tags[i - 1];
+    if (tg & FIBMD_TAG_REMOVED) continue;
+    double x[3], v[3];
+    for (int d = 0; d < 3; d++) {
+      x[d] = CM(s->X, N, i, d);
+      v[d] = CM(s->V, N, i, d);
+    }
+    if (tg & FIBMD_TAG_THERMO)
+      for (int d = 0; d < 3; d++) v[d] = v[d] * ts;
+    double c = h2 * (1.0 / s->mass[i - 1]);
+    for (int d = 0; d < 3; d++) x[d] = x[d] + v[d] * dt + c * CM(s->F, N, i, d);
+    if (tg & FIBMD_TAG_FROZEN)
+      for (int d = 0; d < 3; d++) {
+        x[d] = CM(s->Xi, N, i, d);
+        v[d] = 0.0;
+      }
+    int removed = (p->remove_z > 0.0 && x[2] > p->remove_z) || x[2] < s->sp_remove_zlo;
+    /* an atom outside [0, Lb) by its fixed-point coordinate moves one box
+       back; z stays unwrapped on an open axis */
+    for (int d = 0; d < 3; d++) {
+      if (d == 2 && s->sp_zopen) continue;
+      double k = fixed_coord(x[d], qs[d]);
+      if (k < 0.0 || k >= 4294967296.0) x[d] = x[d] + (k < 0.0 ? s->Lb[d] : -s->Lb[d]);
+    }
+    if (removed) {
+      s->tags[i - 1] = tg | FIBMD_TAG_REMOVED;
+      for (int d = 0; d < 3; d++) v[d] = 0.0;
+      if (s->atype[i - 1] < 3) s->sp_removed++;
+      else s->sp_ions_removed++;
+    }
+    for (int d = 0; d < 3; d++) {
+      CM(s->X, N, i, d) = x[d];
+      CM(s->V, N, i, d) = v[d];
+    }
+    if (!removed) {
+      double dd = 0.0;
+      for (int d = 0; d < 3; d++) {
+        double e = x[d] - CM(s->Xb, N, i, d);
+        e = e - f_nint(e * s->iLb[d]) * s->Lb[d];
+        dd = dd + e * e;
+      }
+      if (dd >= s->sp_trig2) trig = 1;
+    }
+  }
+  if (trig) {
+    orc_si_nlist(s, s->X);
+    s->sp_rebuilds++;
+  }
+  double* Fp = (double*)malloc(sizeof(double) * 3 * (size_t)N);
+  if (nthreads > 1)
+    orc_si_force_omp(s, s->X, Fp, nthreads);
+  else
+    orc_si_force(s, s->X, Fp);
+  /* kick: V += (F + Fp) dt/(2m) for the atoms in the run (pinned ones
+     included: the next drift pins them again) */
+  for (int i = 1; i <= N; i++) {
+    if (s->tags[i - 1] & FIBMD_TAG_REMOVED) continue;
+    double c = hdt * (1.0 / s->mass[i - 1]);
+    for (int d = 0; d < 3; d++)
+      CM(s->V, N, i, d) = CM(s->V, N, i, d) + c * (CM(s->F, N, i, d) + CM(Fp, N, i, d));
+  }
+  memcpy(s->F, Fp, sizeof(double) * 3 * (size_t)N);
+  free(Fp);
+  s->sp_time = s->sp_time + dt;
+  spec_reduce(s);
+  return trig;
+}
+
+void orc_spec_scalars(orc_sys* s, double* out7) {
+  out7[0] = s->sp_time;
+  out7[1] = s->sp_dt;
+  out7[2] = s->sp_thermo_s;
+  out7[3] = s->sp_vmax2;
+  out7[4] = (double)s->sp_removed;
+  out7[5] = (double)s->sp_ions_removed;
+  out7[6] = (double)s->sp_rebuilds;
+}
+
+const unsigned* orc_spec_tags(orc_sys* s) { return s->tags; }
+
+void orc_maxwell(orc_rng* r, int n, int N, const double* mass, double T, double kB, double* V) {
+  const double Pi = 4. * atan(1.0);
+  long long nv = 3 * (long long)n;
+  for (long long m = 0; m < nv; m += 2) {
+    double u1 = orc_ran1(r);
+    double u2 = orc_ran1(r);
+    double rad = sqrt(-2. * log(u1));
+    double z[2] = {rad * cos(2. * Pi * u2), rad * sin(2. * Pi * u2)};
+    for (int q = 0; q < 2 && m + q < nv; q++) {
+      long long e = m + q;
+      int i = (int)(e / 3), d = (int)(e % 3);
+      V[(size_t)d * (size_t)N + (size_t)i] = z[q] * sqrt(kB * T / mass[i]);
+    }
+  }
+  double P[3] = {0.0, 0.0, 0.0}, M = 0.0;
+  for (int i = 0; i < n; i++) {
+    M = M + mass[i];
+    for (int d = 0; d < 3; d++) P[d] = P[d] + mass[i] * V[(size_t)d * (size_t)N + (size_t)i];
+  }
+  for (int i = 0; i < n; i++)
+    for (int d = 0; d < 3; d++)
+      V[(size_t)d * (size_t)N + (size_t)i] = V[(size_t)d * (size_t)N + (size_t)i] - P[d] / M;
 }
 
 /* ---- test helpers --------------------------------------------------------- */

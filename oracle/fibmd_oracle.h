@@ -72,6 +72,19 @@ typedef struct orc_sys {
   int ntlist, atlist, dslist, atm_out;
   int impact;
   int atom_is_fast, atom_is_slow;
+
+  /* spec mode: the specified set-up, which the reference does not have
+     (variable dt, half-skin rebuild, layer tags, removal); see orc_spec_* */
+  int spec;                    /* lists and steps follow spec mode           */
+  unsigned* tags;              /* FIBMD_TAG_* bits per atom                  */
+  double* Xb;                  /* positions at the last list build (Natm,3)  */
+  double sp_dt, sp_thermo_s;   /* current step, thermostat-layer factor      */
+  double sp_time, sp_vmax2;    /* simulated time, max |v|^2 of the last kick */
+  double sp_remove_zlo;        /* atoms below are removed (open z axis)      */
+  double sp_trig2;             /* squared half skin: the rebuild trigger     */
+  int sp_zopen;                /* z is an open axis (not wrapped)            */
+  int sp_removed, sp_ions_removed;
+  long long sp_rebuilds;
 } orc_sys;
 
 /* Park-Miller minimal standard with Bays-Durham shuffle (ran1, src/ran1.f). */
@@ -126,6 +139,41 @@ void orc_assignmass(orc_sys* s);
 void orc_randvel(orc_sys* s, orc_rng* r, double Uo);
 void orc_knock(orc_sys* s, orc_rng* r, int knc, double eV, double phiz,
                double phixy, const double* Xrand, int Nrand);
+
+/* ---- spec mode ------------------------------------------------------------
+   The specified physical set-up of the benchmark slabs, which the
+   reference lacks (restated from the GPU library's spec mode as
+   fibmd_gpu.h documents it; it is on when the parameters' mode is
+   FIBMD_MODE_SPEC):
+   variable dt = min(dt_max, dx_max / max|v|); lists of radius cutoff + skin
+   (0.999 a sigma + list_skin for Si/Ge pairs, 2.5 sigma + list_skin for
+   pairs with an ion, every such pair found) rebuilt when an atom has moved
+   half the skin since the last build; frozen and thermostatted layers as
+   per-atom tags; atoms above remove_z removed (and, with z an open axis,
+   atoms 10 A below z = 0). A step: thermostat scaling of the tagged layer,
+   drift, pinning, removal, wrap, the rebuild test, [rebuild], force, kick,
+   then the reductions that set the next dt and thermostat factor. */
+
+/* Spec mode on: tags (Natm entries, may be NULL for none), the state's V
+   gives the first dt and thermostat factor, time0 the start time. Call
+   after the state is loaded and before orc_si_nlist; afterwards
+   orc_si_nlist builds spec-mode lists and orc_si_force skips removed
+   atoms. */
+void orc_spec_init(orc_sys* s, const unsigned* tags, double time0);
+/* One spec-mode step (nthreads > 1: the OpenMP force). Returns 1 when the
+   lists were rebuilt in it. */
+int orc_spec_step(orc_sys* s, int nthreads);
+/* time, dt, thermostat factor, vmax2, removed lattice atoms, removed ions,
+   rebuilds since orc_spec_init */
+void orc_spec_scalars(orc_sys* s, double* out7);
+const unsigned* orc_spec_tags(orc_sys* s);
+
+/* Maxwell-Boltzmann velocities at temperature T for rows 0..n-1 of V
+   ((N,3) column-major): normal deviates by the Box-Muller method (Box and
+   Muller, 1958) from consecutive ran1 pairs, filled atom by atom (x, y, z),
+   scaled by sqrt(kB T / m); then the mass-weighted mean velocity is
+   removed. */
+void orc_maxwell(orc_rng* r, int n, int N, const double* mass, double T, double kB, double* V);
 
 /* accessors for the Python test harness */
 orc_sys* orc_create(const fibmd_params* p);

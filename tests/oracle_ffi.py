@@ -14,7 +14,52 @@ import numpy as np
 ROOT = Path(__file__).resolve().parents[1]
 sys.path.insert(0, str(ROOT))
 
-from fib_md_gb300._abi import Params  # noqa: E402  (struct layout shared with the header)
+_D = C.c_double
+_I = C.c_int
+
+
+class Params(C.Structure):
+    """ctypes mirror of `fibmd_params` (include/fibmd_gpu.h), which the
+    oracle takes too. Declared here so that the oracle harness loads nothing
+    of the GPU package; tests/test_oracle_kat.py checks it field by field
+    against the package's mirror and the library's struct size."""
+
+    _fields_ = [
+        ("abi_version", _I), ("mode", _I), ("precision", _I),
+        ("Natm", _I), ("Nsg", _I), ("Nlj", _I),
+        ("Lb", _D * 3),
+        ("A", _D), ("B", _D), ("psi", _D), ("qsi", _D), ("al", _D), ("gamma", _D),
+        ("lambdaSi", _D), ("lambdaGe", _D), ("epsSi", _D), ("epsGe", _D),
+        ("sigmaSi", _D), ("sigmaGe", _D),
+        ("massSi", _D), ("massGe", _D), ("massGa", _D),
+        ("ZSi", _D), ("ZGe", _D), ("ZGa", _D),
+        ("Amol", _D), ("Bmol", _D), ("Cmol", _D),
+        ("alpha_mol", _D), ("beta_mol", _D), ("gamma_mol", _D),
+        ("kB", _D), ("eps0", _D), ("ec", _D), ("ao", _D),
+        ("listfac", _D), ("Ntable", _I),
+        ("Ts_i", _D), ("Ts_r", _D), ("Ttar1", _D), ("ke_limit_1", _D),
+        ("Tau_i", _D), ("Tau_r", _D), ("Teps", _D),
+        ("ntlist_i", _I), ("ntlist_r", _I), ("atlist_i", _I), ("atlist_r", _I),
+        ("dslist_i", _I), ("dslist_r", _I),
+        ("atm_out_i", _I), ("atm_out_r", _I), ("res_out", _I),
+        ("outz", _D * 4), ("atomz", _D * 2), ("ionz", _D), ("knockz", _D),
+        ("sidewidth", _D), ("dti", _D),
+        ("dt_max", _D), ("dx_max", _D), ("tau_spec", _D), ("remove_z", _D),
+        ("mixed_mol_fp64_r", _D), ("list_skin", _D),
+        ("max_sw_nbrs", _I), ("max_mol_pairs", _I), ("reserved", _I * 8),
+    ]
+
+    def copy(self) -> "Params":
+        q = Params()
+        C.memmove(C.byref(q), C.byref(self), C.sizeof(Params))
+        return q
+
+    def as_ctype(self, cls):
+        """The same bytes as another mirror class of the struct."""
+        q = cls()
+        C.memmove(C.byref(q), C.byref(self), C.sizeof(cls))
+        return q
+
 
 _DP = C.POINTER(C.c_double)
 _IP = C.POINTER(C.c_int)
@@ -50,6 +95,11 @@ _SIG = {
     "orc_assignmass": (None, [_VP]),
     "orc_randvel": (None, [_VP, _VP, C.c_double]),
     "orc_knock": (None, [_VP, _VP, C.c_int, C.c_double, C.c_double, C.c_double, _DP, C.c_int]),
+    "orc_spec_init": (None, [_VP, C.POINTER(C.c_uint), C.c_double]),
+    "orc_spec_step": (C.c_int, [_VP, C.c_int]),
+    "orc_spec_scalars": (None, [_VP, _DP]),
+    "orc_spec_tags": (C.POINTER(C.c_uint), [_VP]),
+    "orc_maxwell": (None, [_VP, C.c_int, C.c_int, _DP, C.c_double, C.c_double, _DP]),
     "orc_get_pairs": (C.c_longlong, [_VP, C.c_int, _IP, C.c_longlong]),
     "orc_get_triplets": (C.c_longlong, [_VP, _IP, C.c_longlong]),
 }
@@ -77,8 +127,32 @@ def _dp(a):
     return a.ctypes.data_as(_DP)
 
 
+def per_atom_err(A, B):
+    """The parity measure of per-atom forces or energies: the largest
+    |A_i - B_i| / max(|B_i|, RMS(B)) over atoms i (vector norms for (N,3)
+    forces). Every atom is held to its own scale, and atoms whose reference
+    value is near zero (a perfect crystal) to the system's RMS."""
+    A = np.asarray(A, dtype=np.float64)
+    B = np.asarray(B, dtype=np.float64)
+    if A.ndim == 1:
+        A, B = A[:, None], B[:, None]
+    d = np.linalg.norm(A - B, axis=1)
+    n = np.linalg.norm(B, axis=1)
+    rms = float(np.sqrt(np.mean(n * n)))
+    return float(np.max(d / np.maximum(n, max(rms, 1e-300))))
+
+
 def _ip(a):
     return a.ctypes.data_as(_IP)
+
+
+def as_params(p) -> Params:
+    """A copy of p as this harness's Params (p: any same-layout mirror)."""
+    if C.sizeof(type(p)) != C.sizeof(Params):
+        raise TypeError(f"{type(p).__name__} is not a fibmd_params mirror")
+    q = Params()
+    C.memmove(C.byref(q), C.byref(p), C.sizeof(Params))
+    return q
 
 
 def params_default() -> Params:
@@ -110,7 +184,7 @@ class Oracle:
     """One oracle system (orc_sys) with numpy views of its state arrays."""
 
     def __init__(self, params: Params):
-        self.p = params.copy()
+        self.p = as_params(params)
         self.h = lib().orc_create(C.byref(self.p))
         if not self.h:
             raise RuntimeError("orc_create failed")
@@ -242,6 +316,26 @@ class Oracle:
         lib().orc_get_triplets(self.h, _ip(out), n)
         return out[:n]
 
+    # ---- spec mode (params.mode == 1)
+    def spec_init(self, tags=None, time0: float = 0.0):
+        t = None if tags is None else np.ascontiguousarray(tags, dtype=np.uint32)
+        lib().orc_spec_init(self.h, None if t is None else t.ctypes.data_as(C.POINTER(C.c_uint)),
+                            float(time0))
+
+    def spec_step(self, nthreads: int = 0) -> bool:
+        """One spec-mode step; True when it rebuilt the lists."""
+        return bool(lib().orc_spec_step(self.h, nthreads))
+
+    def spec_scalars(self) -> dict:
+        out = (C.c_double * 7)()
+        lib().orc_spec_scalars(self.h, out)
+        keys = ["time", "dt", "thermo_s", "vmax2", "removed", "ions_removed", "rebuilds"]
+        return dict(zip(keys, list(out)))
+
+    def spec_tags(self) -> np.ndarray:
+        t = lib().orc_spec_tags(self.h)
+        return np.ctypeslib.as_array(t, shape=(self.N,)).copy()
+
     def knock(self, rng: OrcRng, knc, eV, phiz, phixy, Xrand):
         Xr = np.asfortranarray(Xrand, dtype=np.float64)
         lib().orc_knock(self.h, rng.ptr, knc, eV, phiz, phixy, _dp(Xr), Xr.shape[0])
@@ -260,7 +354,7 @@ def crystal(nc=(4, 4, 4), nlj=1, seed=-1001, nrand=10000, fwhm=2.0, Uo=150.0, pa
             periodic_z=False):
     """The reference's initial state (pureepi, initranions, initIons,
     assignmass, randvel) from the oracle's restatements."""
-    p = params_default() if params is None else params.copy()
+    p = params_default() if params is None else as_params(params)
     XX, xs, Lb = pureepi(*nc)
     nsg = XX.shape[0]
     p.Nsg, p.Nlj, p.Natm = nsg, nlj, nsg + nlj
@@ -280,3 +374,68 @@ def crystal(nc=(4, 4, 4), nlj=1, seed=-1001, nrand=10000, fwhm=2.0, Uo=150.0, pa
     lib().orc_randvel(o.h, rng.ptr, Uo)
     o.xsides[:nsg] = xs
     return o, rng, Xrand
+
+
+A_LATTICE = 5.431073e-10
+TAG_FROZEN, TAG_THERMO, TAG_REMOVED = 1, 2, 4
+
+
+def spec_slab(cells, seed: int, ion_eV: float, polar_deg: float, T: float = 300.0,
+              ion_height: float = 10e-10, remove_above: float = 35e-10, fixed_layers: int = 2,
+              thermo_layers: int = 4, params=None, azimuth=None, impact_xy=None) -> dict:
+    """The spec-mode impact set-up from the oracle's restatements alone: the
+    reference's crystal (pureepi, initranions, initIons, assignmass, randvel
+    with ran1 seed -|seed|-1), Maxwell-Boltzmann velocities continuing that
+    ran1 stream (orc_maxwell), the bottom fixed_layers (001) planes frozen
+    and the next thermo_layers thermostatted, and the ion ion_height above
+    the top plane at a ran1 azimuth and point (or the given ones), moving
+    polar_deg off the inward normal with ion_eV. The same draws in the same
+    order as the GPU package's spec_slab."""
+    p = params_default() if params is None else as_params(params)
+    p.mode = 1
+    o, rng, _ = crystal(tuple(cells), 1, -abs(int(seed)) - 1, params=p)
+    q = o.p.copy()
+    N, nsg = q.Natm, q.Nsg
+    mass = o.mass.copy()
+    V = np.zeros((N, 3), order="F")
+    lib().orc_maxwell(rng.ptr, nsg, N, _dp(mass), float(T), q.kB, _dp(V))
+    X = o.X.copy(order="F")
+    Xi = o.Xi.copy(order="F")
+    atype = o.atype.copy()
+    o.close()
+    z = X[:nsg, 2]
+    layer = np.rint(z / (A_LATTICE / 4)).astype(int)
+    tags = np.zeros(N, dtype=np.uint32)
+    tags[:nsg][layer < fixed_layers] = TAG_FROZEN
+    tags[:nsg][(layer >= fixed_layers) & (layer < fixed_layers + thermo_layers)] = TAG_THERMO
+    V[:nsg][layer < fixed_layers] = 0.0
+    surf = float(z.max())
+    az = 2 * np.pi * rng() if azimuth is None else float(azimuth)
+    th = np.deg2rad(polar_deg)
+    speed = np.sqrt(2 * ion_eV * q.ec / q.massGa)
+    if impact_xy is None:
+        xr = rng()
+        yr = rng()
+        xy = (xr * q.Lb[0], yr * q.Lb[1])
+    else:
+        xy = impact_xy
+    X[nsg] = [xy[0], xy[1], surf + ion_height]
+    V[nsg] = speed * np.array([np.sin(th) * np.cos(az), np.sin(th) * np.sin(az), -np.cos(th)])
+    q.remove_z = surf + remove_above
+    return dict(params=q, X=X, Xi=Xi, V=V, mass=mass, atype=atype, tags=tags, surface_z=surf)
+
+
+def spec_oracle(slab: dict, params=None, impact: int = 1) -> Oracle:
+    """An oracle in spec mode holding the slab's state, its lists built and
+    its first force evaluated (what a context's upload, set_tags, si_nlist
+    and si_force leave)."""
+    p = (slab["params"] if params is None else params).copy()
+    p.mode = 1
+    o = Oracle(p)
+    o.load(slab["X"], slab["V"], slab["Xi"], slab["mass"], slab["atype"],
+           np.zeros(p.Natm, dtype=np.int32))
+    o.set_impact(impact)
+    o.spec_init(slab["tags"], 0.0)
+    o.si_nlist()
+    o.F[:] = o.si_force()
+    return o

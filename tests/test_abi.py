@@ -32,6 +32,10 @@ def test_params_layout_and_defaults(gpu_lib):
     from fib_md_gb300 import _abi, params_default
 
     assert gpu_lib.fibmd_gpu_params_size() == C.sizeof(_abi.Params)
+    # the oracle harness's own mirror of the struct: the same fields in order
+    assert [(n, C.sizeof(t)) for n, t in of.Params._fields_] == \
+        [(n, C.sizeof(t)) for n, t in _abi.Params._fields_]
+    assert C.sizeof(of.Params) == C.sizeof(_abi.Params)
     a = params_default()
     b = of.params_default()
     for name, _ in _abi.Params._fields_:

@@ -1,9 +1,9 @@
 """GPU (sm_103a) path against the CPU oracle, through the C-ABI.
 
 Bars: neighbour lists bit-exact as sorted (i,j) sets (and the connected
-triplet set); per-atom forces and energies within 1e-10 of the oracle,
-relative to the largest per-atom value; positions within 1e-8 Angstrom after
-100 steps of the reference's onestep.
+triplet set); every atom's force and energy within 1e-10 of the oracle's,
+relative to max(|value_i|, RMS over atoms) (oracle_ffi.per_atom_err);
+positions within 1e-8 Angstrom after 100 steps of the reference's onestep.
 """
 from __future__ import annotations
 
@@ -14,8 +14,9 @@ import oracle_ffi as of
 
 pytestmark = pytest.mark.gpu
 
-FORCE_RTOL = 1e-10     # |F_gpu - F_ref| / max|F_ref|
-ENERGY_RTOL = 1e-10    # |u_gpu - u_ref| / max|u_ref|
+FORCE_RTOL = 1e-10     # per atom: |F_gpu,i - F_ref,i| / max(|F_ref,i|, RMS(F_ref))
+ENERGY_RTOL = 1e-10    # per atom: |u_gpu,i - u_ref,i| / max(|u_ref,i|, RMS(u_ref))
+per_atom_err = of.per_atom_err
 TRAJ_ATOL_M = 1e-18    # 1e-8 Angstrom
 
 
@@ -73,19 +74,23 @@ def test_lists_small_boxes(gpu_lib):
         assert np.array_equal(g.get_triplets(), o.triplets()), nc
 
 
-def test_force_and_energy_parity_fp64(gpu_lib):
-    o = _slab()
+@pytest.mark.parametrize("ion_height_A", [1.6, 12.0])
+def test_force_and_energy_parity_fp64(gpu_lib, ion_height_A):
+    """The ion in contact (its Moliere force ~50 times the thermal SW forces)
+    and far above the surface: every atom at its own scale."""
+    o = _slab(ion_height_A=ion_height_A)
     g = _gpu(o, impact=1)
     o.si_nlist()
     g.si_nlist()
     Fr = o.si_force()
     Ur, ur = o.si_potential()
     F, u, U = g.si_force_energy()
-    assert _maxrel(F, Fr) < FORCE_RTOL
-    assert _maxrel(u, ur) < ENERGY_RTOL
+    assert per_atom_err(F, Fr) < FORCE_RTOL
+    assert per_atom_err(u, ur) < ENERGY_RTOL
     assert abs(U - Ur) < 1e-12 * abs(Ur)
-    # the fired ion feels the Moliere force
-    assert np.abs(Fr[-1]).max() > 0 and _maxrel(F[-1], Fr[-1]) < FORCE_RTOL
+    if ion_height_A < 2.0:
+        # the fired ion feels the Moliere force
+        assert np.abs(Fr[-1]).max() > 0 and _maxrel(F[-1], Fr[-1]) < FORCE_RTOL
 
 
 def test_unfired_ions_skipped(gpu_lib):
@@ -97,11 +102,11 @@ def test_unfired_ions_skipped(gpu_lib):
     Fr = o.si_force()
     F = g.si_force()
     assert np.all(Fr[-1] == 0.0) and np.all(F[-1] == 0.0)
-    assert _maxrel(F, Fr) < FORCE_RTOL
+    assert per_atom_err(F, Fr) < FORCE_RTOL
     # si_potential still counts the unfired ion's Moliere energy
     Ur, ur = o.si_potential()
     _, u, U = g.si_force_energy()
-    assert _maxrel(u, ur) < ENERGY_RTOL
+    assert per_atom_err(u, ur) < ENERGY_RTOL
 
 
 def _run_both(o, g, whichctrl, nsteps, lt0=0, time0=0.0, temp0=300.0):
@@ -307,7 +312,7 @@ def test_many_leg_centres(gpu_lib, precision, stage):
     # the many-leg kernel ran (stage 1 has no separate many-leg pass)
     assert (g.work_counters()[5] > 0) == (stage != 1)
     if precision == 0:
-        assert _maxrel(F, Fr) < FORCE_RTOL
+        assert per_atom_err(F, Fr) < FORCE_RTOL
     else:
         rms_rel = np.sqrt(np.mean(np.sum((F - Fr) ** 2, axis=1))) / np.sqrt(
             np.mean(np.sum(Fr ** 2, axis=1)))

@@ -47,7 +47,9 @@ def _context_force(o):
 def _noalloc_force(lib, o):
     import torch
 
-    p = o.p.copy()
+    import fib_md_gb300 as fm
+
+    p = fm.md.as_params(o.p)
     X = torch.tensor(np.ascontiguousarray(o.X.T), dtype=torch.float64, device="cuda")  # (3,N)
     t = torch.tensor(np.asarray(o.atype, dtype=np.int32), device="cuda")
     F = torch.zeros((3, o.N), dtype=torch.float64, device="cuda")
@@ -64,18 +66,24 @@ def _noalloc_force(lib, o):
 
 def test_noalloc_force_matches_context_force(gpu_lib):
     # two calls in a row on different configurations: the second must not
-    # see the first's lists or counters in the shared scratch array
+    # see the first's lists or counters in the shared scratch array; each
+    # result is also held to the oracle's si_force at the per-atom bar
     for seed in (3, 4):
         o = _configuration(seed)
         F_ref = _context_force(o)
         F = _noalloc_force(gpu_lib, o)
-        err = np.abs(F - F_ref).max() / np.abs(F_ref).max()
+        err = of.per_atom_err(F, F_ref)
         assert err < FORCE_RTOL, (seed, err)
+        o.set_impact(1)
+        o.si_nlist()
+        assert of.per_atom_err(F, o.si_force()) < FORCE_RTOL, seed
 
 
 def test_noalloc_rejects_oversize(gpu_lib):
+    import fib_md_gb300 as fm
+
     o = _configuration(3)
-    p = o.p.copy()
+    p = fm.md.as_params(o.p)
     p.Natm = 100000
     rc = gpu_lib.fibmd_gpu_force_noalloc(C.byref(p), C.c_void_p(1), C.c_void_p(1), 1,
                                          C.c_void_p(1), None)
