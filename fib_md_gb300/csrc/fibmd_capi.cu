@@ -362,6 +362,19 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   P.umax = umax;
   P.tab_last = tab_last;
   P.Ntable = p.Ntable;
+  // a listed pair's table coordinate INT(u/umax*(Ntable-1)) + 1 must stay
+  // within Ntable (itable2bd reports an error past it, src/si.f90:562-564):
+  // a list radius beyond the table is refused here
+  {
+    const double sigmin = p.sigmaGe < p.sigmaSi ? p.sigmaGe : p.sigmaSi;
+    const double ulist = rc / sigmin;
+    if (ulist / umax * (double)(p.Ntable - 1) >= (double)p.Ntable) {
+      std::snprintf(err, (size_t)errlen,
+                    "list radius %.4g A (u = %.4g) reaches beyond the 2-body table (umax %.4g, "
+                    "Ntable %d)", rc * 1e10, ulist, umax, p.Ntable);
+      return FIBMD_ETABLE;
+    }
+  }
   // abscissa after the last non-zero entry: u(k+1) = umax*k/(Ntable-1)
   const double u_next = umax * (double)(tab_last + 1) / (double)(p.Ntable - 1);
   const double usup = std::max(P.cut3, u_next);
@@ -586,11 +599,8 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
     return fail(nullptr, FIBMD_EINVAL, "max_sw_nbrs %d exceeds 64", p->max_sw_nbrs);
   if (p->precision == FIBMD_PREC_MIXED && (p->psi != 4.0 || p->qsi != 0.0))
     return fail(nullptr, FIBMD_EINVAL, "mixed precision implements psi = 4, qsi = 0 only");
-  int ndev = 0;
-  cudaError_t e = cudaGetDeviceCount(&ndev);
-  if (e != cudaSuccess || ndev == 0)
-    return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
 
+  // the parameters are checked (host arithmetic only) before the device is
   ctx = new fibmd_ctx();
   ctx->p = *p;
   int rc = derive_params(ctx);
@@ -598,6 +608,12 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
     set_noctx_error(ctx->err.c_str());
     delete ctx;
     return rc;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    delete ctx;
+    return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
   }
   ctx->geo.assign(1, ctx->geo0);
   ctx->rep_of.assign((size_t)p->Natm, 0);
@@ -650,6 +666,7 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   AL(S.scan_blocks, (size_t)nscan + 1);
   AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
   AL(S.n_sw, N);
+  AL(S.sw_extra, N);
   AL(S.mol_pairs, (size_t)ctx->P.mol_cap);
   AL(S.fast_flag, N);
   AL(S.fast_list, N);
@@ -1056,8 +1073,9 @@ static int check_list_status(fibmd_ctx* ctx) {
   if (h.nan_flag)
     return fail(ctx, FIBMD_ENAN, "non-finite velocity after a kick (upload a valid state)");
   if (h.overflow_sw)
-    return fail(ctx, FIBMD_EOVERFLOW, "%d atoms exceeded %d SW list slots", h.overflow_sw,
-                ctx->P.max_sw);
+    return fail(ctx, FIBMD_EOVERFLOW,
+                "SW list slots exceeded (%d entries dropped): capacity %d, needed %d "
+                "(max_sw_nbrs)", h.overflow_sw, ctx->P.max_sw, h.sw_needed);
   if (h.overflow_mol)
     return fail(ctx, FIBMD_EOVERFLOW, "Moliere list needs %d entries, capacity %d",
                 h.overflow_mol, ctx->P.mol_cap);

@@ -38,14 +38,17 @@ __device__ __forceinline__ double table_df(const DevParams& P, const double* __r
                                            const double* __restrict__ tabu, double ue,
                                            int* err) {
   const double t = ue / P.umax * (double)(P.Ntable - 1);
-  // all three stencil entries are zero beyond tab_last; a non-finite ue (a
-  // corrupted state, reported by the kick) must not become an index either
-  if (!(t >= 0.0 && t < (double)(P.tab_last + 1))) return 0.0;
-  const int it = (int)t;
-  if (it + 1 > P.Ntable) {
+  // a non-finite ue (a corrupted state, reported by the kick) must not
+  // become an index
+  if (!(t >= 0.0)) return 0.0;
+  // the reference's check: i = INT(t) + 1 > Ntable is an error, and 0 is used
+  if (t >= (double)P.Ntable) {
     *err = 1;
     return 0.0;
   }
+  // all three stencil entries are zero beyond tab_last
+  if (!(t < (double)(P.tab_last + 1))) return 0.0;
+  const int it = (int)t;
   const double d1 = ue - __ldg(&tabu[it]);
   const double d2 = ue - __ldg(&tabu[it + 1]);
   const double d3 = ue - __ldg(&tabu[it + 2]);

@@ -146,6 +146,7 @@ struct DevScalars {
   int mol_count;
   int heavy_count;
   int overflow_sw;
+  int sw_needed;       // SW slots the most crowded atom needed (overflow)
   int overflow_mol;
   int table_err;
   int cell_oob;
@@ -195,6 +196,7 @@ struct DevState {
   // lists
   int* nbr_sw;
   int* n_sw;
+  int* sw_extra;     // per atom: SW partners beyond the max_sw slots (overflow)
   int2* mol_pairs;
   // stale-list and heavy-centre work lists
   uint8_t* fast_flag;

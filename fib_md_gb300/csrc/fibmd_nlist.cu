@@ -47,6 +47,7 @@ __global__ void k_build_begin(DevParams P, DevState S, int from_flag) {
     S.sc->mol_count = 0;
     S.sc->fast_count = 0;
     S.sc->overflow_sw = 0;
+    S.sc->sw_needed = 0;
     S.sc->overflow_mol = 0;
     S.sc->cell_oob = 0;
     S.sc->disp_max2 = 0.0;
@@ -71,6 +72,7 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
   if (i >= P.N) return;
   const int4 q = S.posq[i];
   S.n_sw[i] = 0;  // the list build appends with atomics
+  S.sw_extra[i] = 0;
   if ((q.w >> 8) & FL_REMOVED) {
     S.atom_cell[i] = -1;
     S.posq_build[i] = q;
@@ -234,13 +236,21 @@ __device__ __forceinline__ bool exact_in(const Geo& G, const DevState& S, int i,
 constexpr int kBuildThreads = 128;
 constexpr int kBuildBuf = 24;  // buffered candidates per atom
 
+// Entries of atom x that found its list full: counted per atom, so that the
+// capacity the most crowded atom needed is known (max_sw + its extras).
+__device__ __forceinline__ void list_spill(const DevParams& P, const DevState& S, int x, int n) {
+  const int extra = atomicAdd(&S.sw_extra[x], n) + n;
+  atomicAdd(&S.sc->overflow_sw, 1);
+  atomicMax(&S.sc->sw_needed, P.max_sw + extra);
+}
+
 // A slot in atom x's list, or -1 (counted) when the list is full; the count
 // ends at min(entries, max_sw) whatever the order of the atomics.
 __device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, int x) {
   const int slot = atomicAdd(&S.n_sw[x], 1);
   if (slot < P.max_sw) return slot;
   atomicSub(&S.n_sw[x], 1);
-  atomicAdd(&S.sc->overflow_sw, 1);
+  list_spill(P, S, x, 1);
   return -1;
 }
 
@@ -373,7 +383,7 @@ __global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, D
     int keep = min(nb, max(0, P.max_sw - base));
     if (keep < nb) {
       atomicSub(&S.n_sw[i], nb - keep);
-      atomicAdd(&S.sc->overflow_sw, 1);
+      list_spill(P, S, i, nb - keep);
     }
     for (int k = 0; k < nb; k++) {
       const int j = buf[k][t];

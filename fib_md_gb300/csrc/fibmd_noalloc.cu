@@ -38,7 +38,7 @@ constexpr size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 // byte offsets of the sub-arrays inside the scratch array
 struct Layout {
   size_t pos, frc_new, posq, posq_build, posq_cell, atype, flags, cell_count, cell_start,
-      cell_atoms, atom_cell, scan_blocks, nbr_sw, n_sw, mol_pairs, fast_flag,
+      cell_atoms, atom_cell, scan_blocks, nbr_sw, n_sw, sw_extra, mol_pairs, fast_flag,
       fast_list, heavy_list, tab, tabu, partials, sc, geo, ion_list, total;
 };
 
@@ -60,6 +60,7 @@ constexpr Layout make_layout() {
   L.scan_blocks = o; o += align256(sizeof(int) * (C / 1024 + 2));
   L.nbr_sw = o; o += align256(sizeof(int) * (size_t)kNaMaxSw * N);
   L.n_sw = o; o += align256(sizeof(int) * N);
+  L.sw_extra = o; o += align256(sizeof(int) * N);
   L.mol_pairs = o; o += align256(sizeof(int2) * kNaMolPairs);
   L.fast_flag = o; o += align256(sizeof(uint8_t) * N);
   L.fast_list = o; o += align256(sizeof(int) * N);
@@ -232,6 +233,7 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
   S.scan_blocks = reinterpret_cast<int*>(b + kLayout.scan_blocks);
   S.nbr_sw = reinterpret_cast<int*>(b + kLayout.nbr_sw);
   S.n_sw = reinterpret_cast<int*>(b + kLayout.n_sw);
+  S.sw_extra = reinterpret_cast<int*>(b + kLayout.sw_extra);
   S.mol_pairs = reinterpret_cast<int2*>(b + kLayout.mol_pairs);
   S.fast_flag = reinterpret_cast<uint8_t*>(b + kLayout.fast_flag);
   S.fast_list = reinterpret_cast<int*>(b + kLayout.fast_list);
@@ -272,7 +274,11 @@ extern "C" int fibmd_gpu_force_noalloc(const fibmd_params* p, const double* X_de
     return fail_na(FIBMD_ECUDA, msg);
   }
   if (h.nan_flag) return fail_na(FIBMD_EINVAL, "force_noalloc: atype outside 1..3");
-  if (h.overflow_sw) return fail_na(FIBMD_EOVERFLOW, "force_noalloc: SW list slots exceeded");
+  if (h.overflow_sw) {
+    std::snprintf(msg, sizeof msg, "force_noalloc: SW list slots exceeded: capacity %d, needed %d",
+                  P.max_sw, h.sw_needed);
+    return fail_na(FIBMD_EOVERFLOW, msg);
+  }
   if (h.overflow_mol) return fail_na(FIBMD_EOVERFLOW, "force_noalloc: Moliere list exceeded");
   if (h.table_err) return fail_na(FIBMD_ETABLE, "force_noalloc: 2-body table index beyond Ntable");
   return FIBMD_OK;

@@ -85,6 +85,20 @@ def test_nve_energy_conservation(gpu_lib, precision):
     assert drift_eV_per_atom < 2e-4, drift_eV_per_atom
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_nve_drift_gate(gpu_lib, precision):
+    """The stated NVE bar: the total energy of the spec-mode slab (12x12x8
+    unit cells at 300 K, the ion parked outside, thermostat off, the fixed
+    layers kept) drifts by at most 1e-5 eV per mobile atom per ps, the
+    slope of a line fitted to 11 samples over 2 ps (2000 steps at the 1 fs
+    cap), in both precisions."""
+    import bench
+
+    w = bench.make_workload((12, 12, 8), list_skin_A=0.6)
+    drift = bench.nve_drift(w, precision, steps=2000)
+    assert abs(drift) <= 1e-5, drift
+
+
 def _pairs_within(X, Lb, r, sel):
     """Every pair closer than r by the minimum image in x and y (z open),
     with at least one atom in sel, as get_pairs reports it: (i, j), i < j,
