@@ -83,8 +83,8 @@ def parse():
     ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step", "ensemble", "dose"],
                     default=None,
                     help="set up the workload, evaluate the force 3 times (mixed, fp64), "
-                         "rebuild the lists 5 times (build), run 10 mixed steps launch "
-                         "by launch (step), run the 256-impact ensemble 1000 steps as "
+                         "rebuild the lists 5 times (build), run the window's first "
+                         "min(md-steps, 300) mixed steps launch by launch (step), run the 256-impact ensemble 1000 steps as "
                          "graphs and 20 launch by launch (ensemble), or run the dose slab's "
                          "first impact 300 steps as graphs and 20 launch by launch on the "
                          "8-lanes-per-centre force path (dose), exit (for ncu)")
@@ -1048,9 +1048,10 @@ def main():
         w = make_workload(cells, list_skin_A=args.list_skin)
         g = make_ctx(w, fm.PREC_FP64 if args.profile == "fp64" else fm.PREC_MIXED)
         if args.profile == "step":
-            # ten mixed spec-mode steps launch by launch (the integrator kernels)
+            # the window's first min(md_steps, 300) mixed spec-mode steps
+            # launch by launch (every kernel of the step loop)
             g.set_option("graph", 0)
-            g.steps(2, 10, 0, 0.0, 300.0)
+            g.steps(2, min(args.md_steps, 300), 0, 0.0, 300.0)
             g.close()
             return 0
         for _ in range(5 if args.profile == "build" else 3):
