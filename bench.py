@@ -78,6 +78,13 @@ def parse():
                     help="impacts of the cumulative-dose run (0: skip)")
     ap.add_argument("--dose-fp64-impacts", type=int, default=-1,
                     help="impacts of its binary64 counterpart (default: as many)")
+    ap.add_argument("--dose-study", action="store_true",
+                    help="run only the config-4 dose study (--dose-impacts mixed impacts on the "
+                         "first seed, --dose-compare mixed and binary64 impacts on each of "
+                         "--dose-seeds seeds) and print its JSON")
+    ap.add_argument("--dose-compare", type=int, default=100)
+    ap.add_argument("--dose-seeds", type=int, default=3)
+    ap.add_argument("--dose-chunk", type=int, default=50)
     ap.add_argument("--large-steps", type=int, default=20000,
                     help="MD steps of the 1,048,577-atom 30 keV cascade (0: skip)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "build", "step", "ensemble", "dose"],
@@ -836,6 +843,104 @@ def bench_dose(args):
 
 
 # ---------------------------------------------------------------------------
+# config 4 at its stated size: the cumulative-dose study
+def dose_run_chunked(d, precision, nimp, chunk, steps=3000, relax=2e-12):
+    """One dose of nimp successive impacts on the device, run in calls of
+    `chunk` impacts with the positions downloaded after each call: the
+    sputtered atoms after every impact and the crater depth after every
+    chunk."""
+    import fib_md_gb300 as fm
+
+    sl = d.slab
+    p = sl.params.copy()
+    p.precision = precision
+    g = fm.FibMD(p)
+    g.upload(sl.X, sl.V, None, sl.Xi, sl.mass, sl.atype, np.zeros(p.Natm, np.int32))
+    g.set_tags(sl.tags)
+    g.set_impact(len(d.ion_atoms))
+    g.si_nlist()
+    g.si_force()
+    removed, reflected, crater, steps_run = [], [], [], 0
+    w0 = time.perf_counter()
+    for k0 in range(0, nimp, chunk):
+        k1 = min(nimp, k0 + chunk)
+        rm, ir, _, st = g.dose(d.ion_atoms[k0:k1], d.X0[k0:k1], d.V0[k0:k1], steps, relax)
+        removed += rm.tolist()
+        reflected += ir.tolist()
+        steps_run += int(st[-1])
+        X, _, _ = g.download()
+        crater.append((k1, fm.crater_depth(X, sl.atype, list(p.Lb), sl.surface_z, p.remove_z,
+                                           (0.5 * p.Lb[0], 0.5 * p.Lb[1]), 30e-10)))
+    wall = time.perf_counter() - w0
+    g.close()
+    per = np.diff(np.concatenate([[0], removed])).tolist()
+    return {"impacts": nimp, "wall_s": wall, "md_steps": steps_run,
+            "impacts_per_hour": 3600.0 * nimp / wall,
+            "sputtered_per_impact": per, "sputtered_total": removed[-1],
+            "reflected_ions": reflected[-1], "crater_depth_A": [[k, 1e10 * c] for k, c in crater]}
+
+
+def dose_study(args):
+    """Config 4: a 20x20x12 unit-cell slab (38,400 Si) receiving 2 keV Ga at
+    normal incidence at seeded points of a 30x30 A window, 3000 steps plus
+    2 ps of relaxation per impact, atoms 15 A above the surface removed.
+    The first seed runs args.dose_impacts mixed-precision impacts (the full
+    dose); every seed runs args.dose_compare mixed and binary64 impacts,
+    whose per-impact yields and crater depths are compared by two-sample
+    tests."""
+    import fib_md_gb300 as fm
+
+    seeds = [4001 + k for k in range(args.dose_seeds)]
+    nfull, ncmp = args.dose_impacts, args.dose_compare
+    p = fm.params_default()
+    p.list_skin = args.list_skin * 1e-10
+    runs = {}
+    for k, seed in enumerate(seeds):
+        n_mixed = max(ncmp, nfull) if k == 0 else ncmp
+        d = fm.dose_slab((20, 20, 12), n_mixed, seed=seed, ion_eV=2000.0, window=30e-10,
+                         remove_above=15e-10, params=p)
+        runs[seed] = {"mixed": dose_run_chunked(d, fm.PREC_MIXED, n_mixed, args.dose_chunk),
+                      "fp64": dose_run_chunked(d, fm.PREC_FP64, ncmp, args.dose_chunk)}
+        print(json.dumps({"seed": seed, "mixed_impacts": n_mixed,
+                          "mixed_wall_s": runs[seed]["mixed"]["wall_s"],
+                          "fp64_wall_s": runs[seed]["fp64"]["wall_s"]}), file=sys.stderr,
+              flush=True)
+    ym = [y for sd in seeds for y in runs[sd]["mixed"]["sputtered_per_impact"][:ncmp]]
+    yf = [y for sd in seeds for y in runs[sd]["fp64"]["sputtered_per_impact"][:ncmp]]
+
+    def crater_at(r, n):
+        return dict((kk, c) for kk, c in r["crater_depth_A"]).get(n)
+
+    cm = [crater_at(runs[sd]["mixed"], ncmp) for sd in seeds]
+    cf = [crater_at(runs[sd]["fp64"], ncmp) for sd in seeds]
+    from scipy import stats
+
+    out = {
+        "config": "20x20x12 unit cells (38,400 Si), 2 keV Ga at normal incidence at seeded "
+                  "uniform points of a 30x30 A window, 3000 steps then 2 ps of relaxation per "
+                  "impact, atoms 15 A above the surface removed, spec mode, list skin "
+                  f"{args.list_skin} A, device-side dose calls of {args.dose_chunk} impacts",
+        "seeds": seeds,
+        "full_dose": {"seed": seeds[0], "precision": "mixed", **runs[seeds[0]]["mixed"]},
+        "comparison": {
+            "impacts_per_seed": ncmp,
+            "per_impact_yield": two_sample(ym, yf),
+            "per_impact_yield_t_test_p": float(stats.ttest_ind(ym, yf, equal_var=False).pvalue),
+            "crater_depth_A_after": ncmp,
+            "crater_depth_A": {"mixed": cm, "fp64": cf},
+            "yield_per_seed": {str(sd): {"mixed": float(np.mean(
+                runs[sd]["mixed"]["sputtered_per_impact"][:ncmp])), "fp64": float(np.mean(
+                    runs[sd]["fp64"]["sputtered_per_impact"]))} for sd in seeds},
+            "impacts_per_hour": {"mixed": [runs[sd]["mixed"]["impacts_per_hour"] for sd in seeds],
+                                 "fp64": [runs[sd]["fp64"]["impacts_per_hour"] for sd in seeds]},
+        },
+    }
+    if len(seeds) >= 2:
+        out["comparison"]["crater_depth_two_sample"] = two_sample(cm, cf)
+    return out
+
+
+# ---------------------------------------------------------------------------
 # config 1: the small slab in plain binary64 on the GPU beside the oracle
 def bench_config1(args, repeats=3, cpu_sample=200):
     """8x8x8 unit cells (4096 Si + 1 Ga), 500 eV Ga at normal incidence 10 A
@@ -997,6 +1102,10 @@ def main():
                "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0,
                        "d2h_bytes_per_step": 0}}
         print(json.dumps(out))
+        return 0
+
+    if args.dose_study:
+        print(json.dumps(dose_study(args)))
         return 0
 
     if args.profile == "ensemble":

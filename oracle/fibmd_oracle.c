@@ -1349,9 +1349,11 @@ int orc_spec_step(orc_sys* s, int nthreads) {
       if (dd >= s->sp_trig2) trig = 1;
     }
   }
-  if (trig) {
+  if (trig || s->sp_force_rebuild) {
     orc_si_nlist(s, s->X);
     s->sp_rebuilds++;
+    s->sp_force_rebuild = 0;
+    trig = 1;
   }
   double* Fp = (double*)malloc(sizeof(double) * 3 * (size_t)N);
   if (nthreads > 1)
@@ -1384,6 +1386,18 @@ void orc_spec_scalars(orc_sys* s, double* out7) {
 }
 
 const unsigned* orc_spec_tags(orc_sys* s) { return s->tags; }
+
+void orc_spec_inject(orc_sys* s, int i, const double x[3], const double v[3]) {
+  int N = s->Natm;
+  s->tags[i - 1] &= ~(unsigned)FIBMD_TAG_REMOVED;
+  for (int d = 0; d < 3; d++) {
+    CM(s->X, N, i, d) = x[d];
+    CM(s->V, N, i, d) = v[d];
+    CM(s->F, N, i, d) = 0.0;
+  }
+  s->sp_force_rebuild = 1;
+  spec_reduce(s);
+}
 
 void orc_maxwell(orc_rng* r, int n, int N, const double* mass, double T, double kB, double* V) {
   const double Pi = 4. * atan(1.0);

@@ -83,6 +83,7 @@ typedef struct orc_sys {
   double sp_remove_zlo;        /* atoms below are removed (open z axis)      */
   double sp_trig2;             /* squared half skin: the rebuild trigger     */
   int sp_zopen;                /* z is an open axis (not wrapped)            */
+  int sp_force_rebuild;        /* the next step rebuilds the lists           */
   int sp_removed, sp_ions_removed;
   long long sp_rebuilds;
 } orc_sys;
@@ -166,6 +167,12 @@ int orc_spec_step(orc_sys* s, int nthreads);
 /* time, dt, thermostat factor, vmax2, removed lattice atoms, removed ions,
    rebuilds since orc_spec_init */
 void orc_spec_scalars(orc_sys* s, double* out7);
+/* One impact of a dose (the device side of knock repeated): atom i
+   (1-based, a pre-allocated ion kept removed until now) joins the run at
+   position x with velocity v and zero force, the lists are rebuilt at the
+   next step, and the step and thermostat factor are recomputed for the new
+   velocities. */
+void orc_spec_inject(orc_sys* s, int i, const double x[3], const double v[3]);
 const unsigned* orc_spec_tags(orc_sys* s);
 
 /* Maxwell-Boltzmann velocities at temperature T for rows 0..n-1 of V

@@ -99,6 +99,7 @@ _SIG = {
     "orc_spec_step": (C.c_int, [_VP, C.c_int]),
     "orc_spec_scalars": (None, [_VP, _DP]),
     "orc_spec_tags": (C.POINTER(C.c_uint), [_VP]),
+    "orc_spec_inject": (None, [_VP, C.c_int, _DP, _DP]),
     "orc_maxwell": (None, [_VP, C.c_int, C.c_int, _DP, C.c_double, C.c_double, _DP]),
     "orc_get_pairs": (C.c_longlong, [_VP, C.c_int, _IP, C.c_longlong]),
     "orc_get_triplets": (C.c_longlong, [_VP, _IP, C.c_longlong]),
@@ -331,6 +332,31 @@ class Oracle:
         lib().orc_spec_scalars(self.h, out)
         keys = ["time", "dt", "thermo_s", "vmax2", "removed", "ions_removed", "rebuilds"]
         return dict(zip(keys, list(out)))
+
+    def spec_inject(self, i: int, x, v):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        v = np.ascontiguousarray(v, dtype=np.float64)
+        lib().orc_spec_inject(self.h, int(i), _dp(x), _dp(v))
+
+    def spec_dose(self, ion_atoms, X0, V0, steps: int, relax_s: float = 0.0, nthreads: int = 0):
+        """Successive impacts as the device dose runs them: inject, the
+        cascade's steps (rounded up to even), then step pairs until relax_s
+        of simulated time has passed (at least one pair). Returns the
+        simulated time after each impact."""
+        times = []
+        for k, a in enumerate(ion_atoms):
+            self.spec_inject(int(a), X0[k], V0[k])
+            for _ in range(2 * ((steps + 1) // 2)):
+                self.spec_step(nthreads)
+            if relax_s > 0.0:
+                t_stop = self.spec_scalars()["time"] + relax_s
+                while True:
+                    self.spec_step(nthreads)
+                    self.spec_step(nthreads)
+                    if not self.spec_scalars()["time"] < t_stop:
+                        break
+            times.append(self.spec_scalars()["time"])
+        return times
 
     def spec_tags(self) -> np.ndarray:
         t = lib().orc_spec_tags(self.h)

@@ -73,3 +73,32 @@ def test_dose_relaxation_and_records(gpu_lib):
     g.close()
     assert np.all(np.diff(t) > relax) and t[0] > relax
     assert np.all(np.diff(rm) >= 0) and np.all(rm >= 0) and np.all(ir >= 0)
+
+
+def test_dose_matches_oracle(gpu_lib):
+    """The device dose (binary64) against the oracle running the same
+    impacts (inject, cascade steps, relaxation until its end time): the
+    same times, positions within 1e-8 A, the same atoms removed."""
+    import oracle_ffi as of
+
+    d = _dose_slab(2)
+    steps, relax = 60, 15e-15
+    g = _ctx(d)
+    rm, ir, t, st = g.dose(d.ion_atoms, d.X0, d.V0, steps, relax)
+    Xd, _, _ = g.download()
+    tags_d = g.get_tags()
+    g.close()
+    sl = d.slab
+    slab = dict(params=sl.params, X=sl.X, V=sl.V, Xi=sl.Xi, mass=sl.mass, atype=sl.atype,
+                tags=sl.tags)
+    o = of.spec_oracle(slab, impact=len(d.ion_atoms))
+    t_o = o.spec_dose(d.ion_atoms, d.X0, d.V0, steps, relax)
+    assert np.allclose(t, t_o, rtol=1e-12, atol=0)
+    Lb = np.array(sl.params.Lb[:])
+    dX = Xd - o.X
+    dX[:, :2] -= Lb[:2] * np.rint(dX[:, :2] / Lb[:2])
+    assert np.abs(dX).max() < 1e-18
+    assert np.array_equal(tags_d, o.spec_tags())
+    sc = o.spec_scalars()
+    assert rm[-1] == sc["removed"] and ir[-1] == sc["ions_removed"]
+    o.close()
