@@ -86,6 +86,10 @@ struct fibmd_ctx {
   // each chunk of kTuneSteps spec-mode steps
   int stage = kStageSmall;
   bool autotune = true;
+  // programmatic dependent launch of the step loop's kernels (turned off
+  // for good if the device or a graph refuses it)
+  bool pdl = true;
+  int graph_pdl = -1;                // the pdl setting the graph was captured with
   LoopCtl* d_loop = nullptr;
   // replicas: one for a single system, several for a batched ensemble
   Geo geo0;                 // the single system's geometry
@@ -131,6 +135,7 @@ static Launch launch_of(const fibmd_ctx* ctx) {
   L.stream = ctx->stream;
   L.sms = ctx->sms;
   L.stage = ctx->stage;
+  L.pdl = ctx->pdl;
   return L;
 }
 
@@ -1282,6 +1287,8 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->use_graph = value != 0.0;
   } else if (!std::strcmp(key, "autotune")) {
     ctx->autotune = value != 0.0;
+  } else if (!std::strcmp(key, "pdl")) {
+    ctx->pdl = value != 0.0;
   } else if (!std::strcmp(key, "stage")) {
     if (value != kStageSmall && value != kStageLarge && value != kStageGroup)
       return fail(ctx, FIBMD_EINVAL, "stage must be %d, %d or %d", kStageSmall, kStageLarge,
@@ -1304,6 +1311,8 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = ctx->use_graph ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "autotune")) {
     *value = ctx->autotune ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "pdl")) {
+    *value = ctx->pdl ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "stage")) {
     *value = (double)ctx->stage;
   } else {
@@ -1420,8 +1429,9 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
     cudaGraphConditionalHandle hi;
     CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
-    // the drift's last block sets the rebuild condition
-    CKC(launch_spec_drift(L, P, Sx, Ttar, &hi), "drift");
+    // the drift's last block sets the rebuild condition; the second step's
+    // drift follows the first step's kick as its programmatic dependent
+    CKC(launch_spec_drift(L, P, Sx, Ttar, &hi, half == 1), "drift");
     CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd), "deps");
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
@@ -1444,7 +1454,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
     std::swap(Sx.frc, Sx.frc_new);
   }
-  CKC(launch_loop_ctl(cs, ctx->d_loop, Sx.sc, hw), "loop");
+  CKC(launch_loop_ctl(cs, ctx->d_loop, Sx.sc, hw, L.pdl), "loop");
 #undef CKC
   cudaGraph_t out = nullptr;
   CK(cudaStreamEndCapture(cs, &out));
@@ -1456,6 +1466,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_frc = ctx->S.frc;
   ctx->graph_stage = ctx->stage;
   ctx->graph_nfired = P.nfired;
+  ctx->graph_pdl = ctx->pdl ? 1 : 0;
   return FIBMD_OK;
 }
 
@@ -1521,8 +1532,15 @@ static int tune_stage(fibmd_ctx* ctx) {
 
 static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
-      ctx->graph_stage != ctx->stage) {
+      ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0)) {
     int rc = build_spec_graph(ctx);
+    if (rc && ctx->pdl) {
+      // a device or driver without programmatic edges in conditional
+      // bodies: capture the graph with plain launches instead
+      cudaGetLastError();
+      ctx->pdl = false;
+      rc = build_spec_graph(ctx);
+    }
     if (rc) return rc;
   }
   if (pairs <= 0) return FIBMD_OK;

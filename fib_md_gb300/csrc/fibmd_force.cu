@@ -81,6 +81,8 @@ struct LegSmem {
 
 template <bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   LegSmem<double, kBlock64, kLegF64> leg;
   leg.v = reinterpret_cast<double*>(smem_raw);
@@ -268,6 +270,8 @@ inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P
 
 template <bool ENERGY, bool COUNT, int LEGS>
 __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   // the last mol_blocks blocks evaluate the Moliere list (a few dozen pairs
   // per ion), which saves a launch per step
   const int nbm = (P.N + kBlock32 - 1) / kBlock32;
@@ -514,6 +518,8 @@ constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
 template <bool MIXED, bool ENERGY>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
   using R = typename std::conditional<MIXED, float, double>::type;
   constexpr int GROUP = MIXED ? 8 : 32;  // lanes per centre
@@ -659,6 +665,8 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
 // where it is faster (tens of thousands of atoms).
 template <bool ENERGY, bool COUNT>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   constexpr int GROUP = 8;
   constexpr int GPW = 32 / GROUP;
   constexpr int NG = kHeavyWarps * GPW;
@@ -817,6 +825,8 @@ __device__ __forceinline__ bool in_list(const DevParams& P, const DevState& S, i
 // per-centre sweep does not: centre f (legs a, x) and centre x (legs a, f).
 template <bool ENERGY>
 __global__ void k_force_stale(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   const int cnt = *((volatile int*)&S.sc->fast_count);
   for (int h = blockIdx.x * blockDim.x + threadIdx.x; h < cnt; h += gridDim.x * blockDim.x) {
     const int f = S.fast_list[h];
@@ -938,6 +948,8 @@ __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevSta
 
 template <bool MIXED, bool ENERGY>
 __global__ void k_force_moliere(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   moliere_entries<MIXED, ENERGY>(P, S, blockIdx.x * blockDim.x + threadIdx.x,
                                  gridDim.x * blockDim.x);
 }
@@ -975,14 +987,21 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
   kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
-  if (!MIXED) k_force_moliere<MIXED, ENERGY><<<side, 128, 0, L.stream>>>(P, S);
+  // the kernels after the main one are programmatic dependents (L.pdl)
+  const bool pdl = L.pdl && !L.force_b;
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && !MIXED)
+    e = launch_k(k_force_moliere<MIXED, ENERGY>, side, 128, 0, L.stream, pdl, P, S);
   // a group of lanes per many-leg centre; the count is known only on the
   // device, so the grid covers thousands of centres (cascade cores of a
   // batch) in one round and idle warps return at once
   const int heavy_blocks = std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
-  k_force_heavy<MIXED, ENERGY><<<heavy_blocks, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
-  if (P.mode == FIBMD_MODE_REF) k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
-  return cudaGetLastError();
+  if (e == cudaSuccess)
+    e = launch_k(k_force_heavy<MIXED, ENERGY>, heavy_blocks, 32 * kHeavyWarps, 0, L.stream, pdl,
+                 P, S);
+  if (e == cudaSuccess && P.mode == FIBMD_MODE_REF)
+    e = launch_k(k_force_stale<ENERGY>, side, 64, 0, L.stream, pdl, P, S);
+  return e;
 }
 
 // The eight-lanes-per-centre path: one kernel for the SW terms of every
@@ -994,11 +1013,12 @@ static cudaError_t group_impl(const Launch& L, const DevParams& P, const DevStat
   k_force_group<ENERGY, COUNT>
       <<<(P.N + NG - 1) / NG + mol_blocks(P), 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
-  if (P.mode == FIBMD_MODE_REF) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && P.mode == FIBMD_MODE_REF) {
     const int side = L.sms > 0 ? L.sms : 152;
-    k_force_stale<ENERGY><<<side, 64, 0, L.stream>>>(P, S);
+    e = launch_k(k_force_stale<ENERGY>, side, 64, 0, L.stream, L.pdl && !L.force_b, P, S);
   }
-  return cudaGetLastError();
+  return e;
 }
 
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S, bool energy,

@@ -11,6 +11,7 @@
 namespace fibmd {
 
 __global__ void k_loop_ctl(LoopCtl* loop, const DevScalars* sc, cudaGraphConditionalHandle h) {
+  pdl_wait();
   const long long r = loop->pairs - 1;
   loop->pairs = r;
   loop->pairs_run += 1;
@@ -24,9 +25,8 @@ __global__ void k_loop_set(LoopCtl* loop, const DevScalars* sc, long long pairs,
 }
 
 cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
-                            cudaGraphConditionalHandle h) {
-  k_loop_ctl<<<1, 1, 0, s>>>(loop, sc, h);
-  return cudaGetLastError();
+                            cudaGraphConditionalHandle h, bool pdl) {
+  return launch_k(k_loop_ctl, 1, 1, 0, s, pdl, loop, sc, h);
 }
 
 cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc, long long pairs,

@@ -332,6 +332,8 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // and the rebuild trigger at half the list skin.
 template <int BATCH>
 __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   bool trig = false;
   if (i < P.N) {
@@ -415,21 +417,22 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
 // own rather than a last-block ticket in the drift: a same-address atomic
 // from each of ~1000 blocks serialises in L2 for longer than a launch.
 __global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond) {
+  pdl_wait();
+  pdl_trigger();
   if (threadIdx.x == 0)
     cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
-                              double Ttar, const cudaGraphConditionalHandle* cond) {
+                              double Ttar, const cudaGraphConditionalHandle* cond,
+                              bool pdl_first) {
   (void)Ttar;
   const int nb = (P.N + 255) / 256;
-  if (P.nrep > 1)
-    k_spec_drift<1><<<nb, 256, 0, L.stream>>>(P, S);
-  else
-    k_spec_drift<0><<<nb, 256, 0, L.stream>>>(P, S);
+  cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, 256, 0, L.stream,
+                           L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
-  if (cond) k_spec_cond<<<1, 32, 0, L.stream>>>(S, *cond);
-  return cudaGetLastError();
+  if (e == cudaSuccess && cond) e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond);
+  return e;
 }
 
 // Kick (apply != 0) followed by the reductions the next step needs: the
@@ -465,6 +468,8 @@ __device__ __forceinline__ void kick_combine(unsigned long long& m, double& a, i
 template <int BATCH>
 __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
                                                              double Ttar) {
+  pdl_wait();
+  pdl_trigger();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   uint32_t fl = FL_REMOVED;
   unsigned long long vb = 0ull;  // bits of v^2
@@ -611,11 +616,9 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
                              double Ttar, int apply) {
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   if (nb > kMaxRedBlocks) return cudaErrorInvalidConfiguration;
-  if (P.nrep > 1)
-    k_spec_kick<1><<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
-  else
-    k_spec_kick<0><<<nb, kKickThreads, 0, L.stream>>>(P, S, apply, Ttar);
-  return cudaGetLastError();
+  // a programmatic dependent of the force kernels before it
+  return launch_k(P.nrep > 1 ? k_spec_kick<1> : k_spec_kick<0>, nb, kKickThreads, 0, L.stream,
+                  L.pdl && apply, P, S, apply, Ttar);
 }
 
 // ---- dose: successive impacts without host round trips ---------------------

@@ -217,6 +217,22 @@ struct DevState {
   const int* ion_list;  // the ions (atype 3), ascending
 };
 
+// ---- programmatic dependent launch -----------------------------------------
+// A kernel launched with the programmatic stream-serialization attribute
+// (launch_k with pdl = true) may be dispatched while its predecessor in the
+// stream still runs. pdl_wait() returns once the predecessor has completed
+// and its writes are visible (a hardware wait, no spin; a no-op for a kernel
+// launched without the attribute), so every kernel of the step loop calls it
+// before its first load: a predecessor completes only after its own
+// predecessor has, so completion is transitive along the chain.
+// pdl_trigger() lets the successor's blocks be dispatched onto SMs as this
+// grid's blocks retire, which hides the successor's launch and ramp-up
+// behind this grid's tail.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // ---- small device helpers ------------------------------------------------
 
 __device__ __forceinline__ int type_index(int8_t t) { return t - 1; }
@@ -402,11 +418,31 @@ constexpr int kStageGroup = 1;
 struct Launch {
   cudaStream_t stream;
   int sms;
+  bool pdl = false;               // launch the step loop's kernels with
+                                  // programmatic dependent launch
   cudaEvent_t force_a = nullptr;  // recorded around the main force kernel
   cudaEvent_t force_b = nullptr;  // when kernel timing is on
   int stage = kStageSmall;        // binary32 force kernel: staged candidates
                                   // per centre (kStageSmall or kStageLarge)
 };
+
+// A kernel launch, with the programmatic stream-serialization attribute when
+// pdl is set (the kernel must call pdl_wait() before its first load).
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t s, bool pdl, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = pdl ? at : nullptr;
+  cfg.numAttrs = pdl ? 1u : 0u;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
 
 // fibmd_nlist.cu
 cudaError_t launch_update_posq(const Launch& L, const DevParams& P, const DevState& S);
@@ -435,13 +471,16 @@ cudaError_t launch_unpack(const Launch& L, int N, const double4_32a* src, double
 cudaError_t launch_track_all(const Launch& L, const DevParams& P, const DevState& S);
 cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevState& S);
 // cond (in a captured graph): the IF handle the rebuild hangs on
+// pdl_first: the drift may itself be launched as a programmatic dependent of
+// the kernel before it (a kick); the condition kernel always is (L.pdl)
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
-                              double Ttar, const cudaGraphConditionalHandle* cond = nullptr);
+                              double Ttar, const cudaGraphConditionalHandle* cond = nullptr,
+                              bool pdl_first = false);
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
 // fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
 cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
-                            cudaGraphConditionalHandle h);
+                            cudaGraphConditionalHandle h, bool pdl = false);
 // sets the loop to `pairs` step pairs, stopping early once the time of
 // replica 0 passes its value at this point plus `relax` (relax <= 0: no stop)
 cudaError_t launch_loop_set(cudaStream_t s, LoopCtl* loop, const DevScalars* sc, long long pairs,
