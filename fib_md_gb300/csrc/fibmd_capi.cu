@@ -86,9 +86,9 @@ struct fibmd_ctx {
   // each chunk of kTuneSteps spec-mode steps
   int stage = kStageSmall;
   bool autotune = true;
-  // programmatic dependent launch of the step loop's kernels (turned off
-  // for good if the device or a graph refuses it)
-  bool pdl = true;
+  // programmatic dependent launch of the step loop's kernels (option "pdl";
+  // off by default: measured no faster on the graph step loop)
+  bool pdl = false;
   int graph_pdl = -1;                // the pdl setting the graph was captured with
   LoopCtl* d_loop = nullptr;
   // replicas: one for a single system, several for a batched ensemble

@@ -289,7 +289,7 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    keep the fastest, default 1) and "stage" (the binary32 force path: 8 or
    10 staged leg candidates per centre with one thread per centre, or 1 for
    eight lanes per centre, the faster on small systems; setting it turns
-   "autotune" off) and "pdl" (default 1: the step loop's kernels are
+   "autotune" off) and "pdl" (default 0; 1: the step loop's kernels are
    launched as programmatic dependents of the kernel before them, so each
    is dispatched during its predecessor's tail and waits in hardware for its
    completion; a graph that cannot be captured so is captured with plain
