@@ -90,6 +90,12 @@ struct fibmd_ctx {
   // off by default: measured no faster on the graph step loop)
   bool pdl = false;
   int graph_pdl = -1;                // the pdl setting the graph was captured with
+  // the graph's kick of each step fused with the next step's drift (option
+  // "fuse"), in a grid of at most kd_blocks resident blocks
+  bool fuse = true;
+  int kd_blocks = 0;       // resident blocks of the fused kernel (0: unavailable)
+  int kd_grid = 0;         // option "kd_grid": its grid size instead (tests)
+  int graph_fuse = -1;
   LoopCtl* d_loop = nullptr;
   // replicas: one for a single system, several for a batched ensemble
   Geo geo0;                 // the single system's geometry
@@ -733,6 +739,8 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
     return FIBMD_ECUDA;
   }
   set_regime(ctx, 1);
+  ctx->kd_blocks = spec_kd_resident_blocks(ctx->P.nrep, ctx->sms);
+  cudaGetLastError();
   *out = ctx;
   return FIBMD_OK;
 }
@@ -970,6 +978,7 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   if (ctx->lists_built) CK(launch_track_all(L, ctx->P, ctx->S));
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemsetAsync(&ctx->S.sc->nan_flag, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(&ctx->S.sc->kd_timeout, 0, sizeof(int), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
@@ -1077,6 +1086,10 @@ static int check_list_status(fibmd_ctx* ctx) {
   const DevScalars& h = *ctx->h_sc;
   if (h.nan_flag)
     return fail(ctx, FIBMD_ENAN, "non-finite velocity after a kick (upload a valid state)");
+  if (h.kd_timeout)
+    return fail(ctx, FIBMD_ETIMEOUT,
+                "the fused kick-drift's grid barrier gave up (blocks not resident together); "
+                "the state is not valid: upload a state, or set the option \"fuse\" to 0");
   if (h.overflow_sw)
     return fail(ctx, FIBMD_EOVERFLOW,
                 "SW list slots exceeded (%d entries dropped): capacity %d, needed %d "
@@ -1289,6 +1302,13 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->autotune = value != 0.0;
   } else if (!std::strcmp(key, "pdl")) {
     ctx->pdl = value != 0.0;
+  } else if (!std::strcmp(key, "fuse")) {
+    ctx->fuse = value != 0.0;
+  } else if (!std::strcmp(key, "kd_grid")) {
+    if (value < 0.0 || value > (double)kMaxRedBlocks)
+      return fail(ctx, FIBMD_EINVAL, "kd_grid %g out of range", value);
+    ctx->kd_grid = (int)value;
+    ctx->graph_fuse = -1;  // recapture
   } else if (!std::strcmp(key, "stage")) {
     if (value != kStageSmall && value != kStageLarge && value != kStageGroup)
       return fail(ctx, FIBMD_EINVAL, "stage must be %d, %d or %d", kStageSmall, kStageLarge,
@@ -1313,6 +1333,10 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = ctx->autotune ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "pdl")) {
     *value = ctx->pdl ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "fuse")) {
+    *value = (ctx->fuse && ctx->kd_blocks > 0) ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "kd_grid")) {
+    *value = (double)(ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks);
   } else if (!std::strcmp(key, "stage")) {
     *value = (double)ctx->stage;
   } else {
@@ -1381,80 +1405,128 @@ static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, in
   return FIBMD_OK;
 }
 
-// Captures two spec-mode MD steps (the force buffers swap back) as the body
-// of a WHILE node; in each step an IF node runs the list rebuild only when
-// the drift found an atom beyond half the skin.
+// The spec-mode step loop as one CUDA graph: a WHILE node runs step pairs
+// (the force buffers swap back after two steps) until the device-side loop
+// counter or the relaxation's end time stops it; after each drift an IF node
+// runs the list rebuild only when an atom moved half the skin.
+//   unfused: WHILE { [drift, cond, IF{rebuild}, force, kick] x 2, loop control }
+//   fused ("fuse", the default): drift, cond, IF{rebuild},
+//            WHILE { [force, kick + next drift, IF{rebuild}] x 2 }
+// In the fused form each kick runs in one persistent kernel with the next
+// step's drift (k_spec_kd), which also sets the IF condition and, at the end
+// of a pair, the WHILE condition; when the loop stops it does not drift, so
+// the state on exit is that of a completed step in both forms.
 static int build_spec_graph(fibmd_ctx* ctx) {
   drop_graph(ctx);
   if (!ctx->cap2) CK(cudaStreamCreateWithFlags(&ctx->cap2, cudaStreamNonBlocking));
   const DevParams& P = ctx->P;
   const double Ttar = ctx->p.Ttar1;
+  const bool fused = ctx->fuse && ctx->kd_blocks > 0;
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
   ctx->graph = g;
   cudaGraphConditionalHandle hw;
   CK(cudaGraphConditionalHandleCreate(&hw, g, 1, cudaGraphCondAssignDefault));
-  cudaGraphNodeParams wp = {};
-  wp.type = cudaGraphNodeTypeConditional;
-  wp.conditional.handle = hw;
-  wp.conditional.type = cudaGraphCondTypeWhile;
-  wp.conditional.size = 1;
-  cudaGraphNode_t wnode;
-  CK(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
-  cudaGraph_t body = wp.conditional.phGraph_out[0];
 
   cudaStream_t cs = ctx->stream;
   Launch L = launch_of(ctx);
   Launch L2 = L;
   L2.stream = ctx->cap2;
   DevState Sx = ctx->S;
-  CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
-                                   cudaStreamCaptureModeThreadLocal));
   auto abort_capture = [&](cudaError_t e, const char* what) {
     cudaGraph_t tmp = nullptr;
     cudaStreamEndCapture(cs, &tmp);
     drop_graph(ctx);
     return fail(ctx, FIBMD_ECUDA, "graph capture (%s): %s", what, cudaGetErrorString(e));
   };
-#define CKC(call, what)                           \
-  do {                                            \
-    cudaError_t e_ = (call);                      \
-    if (e_ != cudaSuccess) return abort_capture(e_, what); \
+#define CKC(call, what)                                     \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return abort_capture(e_, what);  \
   } while (0)
-  for (int half = 0; half < 2; half++) {
+  // an IF node on the capture's current dependencies, its body the list
+  // rebuild (captured on the second stream), made the new dependency
+  auto add_rebuild_if = [&](cudaGraphConditionalHandle hi) -> cudaError_t {
     cudaStreamCaptureStatus st;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
     size_t nd = 0;
-    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
-    cudaGraphConditionalHandle hi;
-    CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
-    // the drift's last block sets the rebuild condition; the second step's
-    // drift follows the first step's kick as its programmatic dependent
-    CKC(launch_spec_drift(L, P, Sx, Ttar, &hi, half == 1), "drift");
-    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd), "deps");
+    cudaError_t e = cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd);
+    if (e != cudaSuccess) return e;
     cudaGraphNodeParams ip = {};
     ip.type = cudaGraphNodeTypeConditional;
     ip.conditional.handle = hi;
     ip.conditional.type = cudaGraphCondTypeIf;
     ip.conditional.size = 1;
     cudaGraphNode_t inode;
-    CKC(cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip), "if node");
-    CKC(cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1,
-                                            cudaStreamSetCaptureDependencies), "update");
+    e = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamUpdateCaptureDependencies(cs, &inode, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies);
+    if (e != cudaSuccess) return e;
     cudaGraph_t ib = ip.conditional.phGraph_out[0];
-    CKC(cudaStreamBeginCaptureToGraph(ctx->cap2, ib, nullptr, nullptr, 0,
-                                      cudaStreamCaptureModeThreadLocal), "if capture");
-    cudaError_t eb = launch_build_lists(L2, P, Sx, 0);
+    e = cudaStreamBeginCaptureToGraph(ctx->cap2, ib, nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return e;
+    const cudaError_t eb = launch_build_lists(L2, P, Sx, 0);
     cudaGraph_t tmp = nullptr;
-    cudaError_t ee = cudaStreamEndCapture(ctx->cap2, &tmp);
-    if (eb != cudaSuccess) return abort_capture(eb, "rebuild");
-    if (ee != cudaSuccess) return abort_capture(ee, "if end");
-    CKC(launch_force(L, P, Sx, false, false, true), "force");
-    CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
+    const cudaError_t ee = cudaStreamEndCapture(ctx->cap2, &tmp);
+    return eb != cudaSuccess ? eb : ee;
+  };
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = hw;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  if (fused) {
+    // the prologue: the first step's drift and rebuild, then the WHILE node
+    CK(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0,
+                                     cudaStreamCaptureModeThreadLocal));
+    cudaGraphConditionalHandle h0;
+    CKC(cudaGraphConditionalHandleCreate(&h0, g, 0, cudaGraphCondAssignDefault), "handle");
+    CKC(launch_spec_drift(L, P, Sx, Ttar, &h0), "drift");
+    CKC(add_rebuild_if(h0), "rebuild");
+    cudaStreamCaptureStatus st;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, nullptr, &deps, nullptr, &nd), "deps");
+    cudaGraphNode_t wnode;
+    CKC(cudaGraphAddNode(&wnode, g, deps, nullptr, nd, &wp), "while node");
+    CKC(cudaStreamUpdateCaptureDependencies(cs, &wnode, nullptr, 1,
+                                            cudaStreamSetCaptureDependencies), "update");
+    cudaGraph_t tmp = nullptr;
+    CK(cudaStreamEndCapture(cs, &tmp));
+  } else {
+    cudaGraphNode_t wnode;
+    CK(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
+  }
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  for (int half = 0; half < 2; half++) {
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
+    cudaGraphConditionalHandle hi;
+    CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
+    if (fused) {
+      CKC(launch_force(L, P, Sx, false, false, true), "force");
+      CKC(launch_spec_kd(L, P, Sx, Ttar, ctx->d_loop, hi, hw, half == 1,
+                         ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks),
+          "kick-drift");
+      CKC(add_rebuild_if(hi), "rebuild");
+    } else {
+      // the drift's last block sets the rebuild condition; the second
+      // step's drift follows the first step's kick as its programmatic
+      // dependent
+      CKC(launch_spec_drift(L, P, Sx, Ttar, &hi, half == 1), "drift");
+      CKC(add_rebuild_if(hi), "rebuild");
+      CKC(launch_force(L, P, Sx, false, false, true), "force");
+      CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
+    }
     std::swap(Sx.frc, Sx.frc_new);
   }
-  CKC(launch_loop_ctl(cs, ctx->d_loop, Sx.sc, hw, L.pdl), "loop");
+  if (!fused) CKC(launch_loop_ctl(cs, ctx->d_loop, Sx.sc, hw, L.pdl), "loop");
 #undef CKC
   cudaGraph_t out = nullptr;
   CK(cudaStreamEndCapture(cs, &out));
@@ -1467,6 +1539,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_stage = ctx->stage;
   ctx->graph_nfired = P.nfired;
   ctx->graph_pdl = ctx->pdl ? 1 : 0;
+  ctx->graph_fuse = ctx->fuse ? 1 : 0;
   return FIBMD_OK;
 }
 
@@ -1532,7 +1605,8 @@ static int tune_stage(fibmd_ctx* ctx) {
 
 static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
-      ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0)) {
+      ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
+      ctx->graph_fuse != (ctx->fuse ? 1 : 0)) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {
       // a device or driver without programmatic edges in conditional

@@ -329,12 +329,12 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z (and, with an open z axis, of atoms 10 A below the lowest plane),
-// and the rebuild trigger at half the list skin.
+// and the rebuild trigger at half the list skin: the kKickThreads atoms of
+// chunk c, one per thread. Returns, in every thread, whether an atom of the
+// chunk moved half the skin since the last list build.
 template <int BATCH>
-__global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
-  pdl_wait();
-  pdl_trigger();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ bool spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
+  const int i = c * kKickThreads + threadIdx.x;
   bool trig = false;
   if (i < P.N) {
     uint32_t fl = S.flags[i];
@@ -356,10 +356,10 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
         v.y *= ts;
         v.z *= ts;
       }
-      const double c = h2 * im;
-      x.x = x.x + v.x * dt + c * f.x;
-      x.y = x.y + v.y * dt + c * f.y;
-      x.z = x.z + v.z * dt + c * f.z;
+      const double cc = h2 * im;
+      x.x = x.x + v.x * dt + cc * f.x;
+      x.y = x.y + v.y * dt + cc * f.y;
+      x.z = x.z + v.z * dt + cc * f.z;
       if (fl & FL_FROZEN) {
         const double4_32a xi = S.xi[i];
         x.x = xi.x;
@@ -402,15 +402,24 @@ __global__ void __launch_bounds__(256) k_spec_drift(DevParams P, DevState S) {
       if (!removed && d.x * d.x + d.y * d.y + d.z * d.z >= P.disp_fastA2) trig = true;
     }
   }
-  const bool any = __syncthreads_or(trig);
+  return __syncthreads_or(trig);
+}
+
+// the force counters of the coming step (the previous step's force is done)
+__device__ __forceinline__ void reset_force_counters(const DevState& S) {
+  S.sc->heavy_count = 0;
+  S.sc->table_err = 0;
+  for (int k = 0; k < 4; k++) S.sc->counters[k] = 0ull;
+}
+
+template <int BATCH>
+__global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
+  const bool any = spec_drift_chunk<BATCH>(P, S, blockIdx.x);
   if (threadIdx.x != 0) return;
   if (any) S.sc->need_rebuild = 1;
-  if (blockIdx.x == 0) {
-    // the force counters of this step (the previous step's force is done)
-    S.sc->heavy_count = 0;
-    S.sc->table_err = 0;
-    for (int k = 0; k < 4; k++) S.sc->counters[k] = 0ull;
-  }
+  if (blockIdx.x == 0) reset_force_counters(S);
 }
 
 // Sets the graph's rebuild condition from the drift's flag. A kernel of its
@@ -427,9 +436,9 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
                               double Ttar, const cudaGraphConditionalHandle* cond,
                               bool pdl_first) {
   (void)Ttar;
-  const int nb = (P.N + 255) / 256;
-  cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, 256, 0, L.stream,
-                           L.pdl && pdl_first, P, S);
+  const int nb = (P.N + kKickThreads - 1) / kKickThreads;
+  cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, kKickThreads, 0,
+                           L.stream, L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
   if (e == cudaSuccess && cond) e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond);
   return e;
@@ -444,9 +453,9 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 // the layer count is an integer, only warps holding layer atoms sum m v^2
 // (binary64 is scarce: a warp instruction holds the SM's FP64 unit for 16
 // cycles), and after one barrier only warp 0 goes on. Completion is counted
-// in two levels — a ticket per group of kKickGroup blocks, whose last block
+// in two levels — a ticket per group of kKickGroup chunks, whose last chunk
 // combines the group's partials, then one ticket per replica, whose last
-// block combines the group partials — because a same-address atomic from
+// chunk combines the group partials — because a same-address atomic from
 // every block serialises in L2, and a last block reducing all block
 // partials is a long dependent chain. Sums run in a fixed order
 // (deterministic). The replica's last warp derives dt and the Berendsen
@@ -465,12 +474,17 @@ __device__ __forceinline__ void kick_combine(unsigned long long& m, double& a, i
   if (c) a = warp_sum(a);
 }
 
+// The kick of chunk c (kKickThreads atoms, one per thread; a chunk lies
+// inside one replica, replicas starting at multiples of the chunk) and its
+// share of the step's reductions. The block-partial stage is double-buffered
+// by `buf`, so a block can take its next chunk while its warp 0 finishes the
+// completion of this one. Returns the replica this call finalized (dt, the
+// thermostat factor and the time written) in lane 0 of warp 0 of the block
+// that finalized it, -1 everywhere else.
 template <int BATCH>
-__global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
-                                                             double Ttar) {
-  pdl_wait();
-  pdl_trigger();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ int spec_kick_chunk(const DevParams& P, const DevState& S, int c,
+                                               int apply, double Ttar, int buf) {
+  const int i = c * kKickThreads + threadIdx.x;
   uint32_t fl = FL_REMOVED;
   unsigned long long vb = 0ull;  // bits of v^2
   double ts = 0.0;
@@ -487,15 +501,13 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     }
     const double m = S.mass[i];
     const int8_t at = S.atype[i];
-    // a kick block lies inside one replica (replicas start at multiples of
-    // the block size)
     const double hdt = S.sc[BATCH ? rep_of_flags(fl) : 0].half_dt;
     if (!(fl & FL_REMOVED)) {
       if (apply) {
-        const double c = hdt * im;
-        v.x = v.x + c * (f.x + g.x);
-        v.y = v.y + c * (f.y + g.y);
-        v.z = v.z + c * (f.z + g.z);
+        const double cc = hdt * im;
+        v.x = v.x + cc * (f.x + g.x);
+        v.y = v.y + cc * (f.y + g.y);
+        v.z = v.z + cc * (f.z + g.z);
         S.vel[i] = v;
         // the old force's buffer accumulates the next force (after the swap)
         S.frc[i] = make_double4_32a(0.0, 0.0, 0.0, 0.0);
@@ -514,29 +526,29 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     }
   }
   kick_combine(vb, ts, tc);
-  __shared__ unsigned long long smax[kKickThreads / 32];
-  __shared__ double ssum[kKickThreads / 32];
-  __shared__ int scnt[kKickThreads / 32];
+  __shared__ unsigned long long smax[2][kKickThreads / 32];
+  __shared__ double ssum[2][kKickThreads / 32];
+  __shared__ int scnt[2][kKickThreads / 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (lane == 0) {
-    smax[w] = vb;
-    ssum[w] = ts;
-    scnt[w] = tc;
+    smax[buf][w] = vb;
+    ssum[buf][w] = ts;
+    scnt[buf][w] = tc;
   }
   __syncthreads();
-  if (w != 0) return;
-  // warp 0: the block's partial
+  if (w != 0) return -1;
+  // warp 0: the chunk's partial
   constexpr int kWarps = kKickThreads / 32;
-  unsigned long long m = lane < kWarps ? smax[lane] : 0ull;
-  int c = lane < kWarps ? scnt[lane] : 0;
-  double a = c ? ssum[lane] : 0.0;
-  kick_combine(m, a, c);
-  // the replica of this block: its first atom's, lane 0's (blocks never
-  // straddle replicas, and a replica's padding only ends its last block)
+  unsigned long long m = lane < kWarps ? smax[buf][lane] : 0ull;
+  int cnt = lane < kWarps ? scnt[buf][lane] : 0;
+  double a = cnt ? ssum[buf][lane] : 0.0;
+  kick_combine(m, a, cnt);
+  // the replica of this chunk: its first atom's, lane 0's (chunks never
+  // straddle replicas, and a replica's padding only ends its last chunk)
   const int r = BATCH ? __shfl_sync(0xffffffffu, rep_of_flags(fl), 0) : 0;
   const Geo& G = S.geo[r];
   const int nblk = G.blk_end - G.blk_begin;
-  const int grp = ((int)blockIdx.x - G.blk_begin) / kKickGroup;
+  const int grp = (c - G.blk_begin) / kKickGroup;
   const int gsize = min(kKickGroup, nblk - grp * kKickGroup);
   const int ngrp = (nblk + kKickGroup - 1) / kKickGroup;
   // group slots of different replicas never share an index
@@ -545,53 +557,53 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
   unsigned* gt = S.group_ticket + 8 * (size_t)gidx;
   int st = 0;
   if (lane == 0) {
-    S.partials[blockIdx.x] = __longlong_as_double((long long)m);
-    S.partials[kMaxRedBlocks + blockIdx.x] = a;
-    S.partials[2 * kMaxRedBlocks + blockIdx.x] = (double)c;
+    S.partials[c] = __longlong_as_double((long long)m);
+    S.partials[kMaxRedBlocks + c] = a;
+    S.partials[2 * kMaxRedBlocks + c] = (double)cnt;
     __threadfence();
     st = atomicAdd(gt, 1u) == (unsigned)(gsize - 1);
   }
-  if (!__shfl_sync(0xffffffffu, st, 0)) return;
-  // the group's last block: combine the group's block partials
+  if (!__shfl_sync(0xffffffffu, st, 0)) return -1;
+  // the group's last chunk: combine the group's chunk partials
   __threadfence();
   m = 0ull;
   a = 0.0;
-  c = 0;
+  cnt = 0;
   if (lane < gsize) {
     const int b = G.blk_begin + grp * kKickGroup + lane;
     m = (unsigned long long)__double_as_longlong(__ldcg(S.partials + b));
-    c = (int)__ldcg(S.partials + 2 * kMaxRedBlocks + b);
-    if (c) a = __ldcg(S.partials + kMaxRedBlocks + b);
+    cnt = (int)__ldcg(S.partials + 2 * kMaxRedBlocks + b);
+    if (cnt) a = __ldcg(S.partials + kMaxRedBlocks + b);
   }
-  kick_combine(m, a, c);
+  kick_combine(m, a, cnt);
   double* gp = S.group_part;
   if (lane == 0) {
     gp[gidx] = __longlong_as_double((long long)m);
     gp[gstride + gidx] = a;
-    gp[2 * gstride + gidx] = (double)c;
-    *gt = 0u;  // every block of the group has counted
+    gp[2 * gstride + gidx] = (double)cnt;
+    *gt = 0u;  // every chunk of the group has counted
     __threadfence();
     st = atomicAdd(&S.sc[r].ticket[5], 1u) == (unsigned)(ngrp - 1);
     if (st) S.sc[r].ticket[5] = 0u;
   }
-  if (!__shfl_sync(0xffffffffu, st, 0)) return;
+  if (!__shfl_sync(0xffffffffu, st, 0)) return -1;
   // the replica's last group: combine the group partials
   __threadfence();
   m = 0ull;
   a = 0.0;
-  c = 0;
+  cnt = 0;
   const int g0 = G.blk_begin / kKickGroup + r;
   for (int q = lane; q < ngrp; q += 32) {
     const unsigned long long x = (unsigned long long)__double_as_longlong(__ldcg(gp + g0 + q));
     m = x > m ? x : m;
     const int cq = (int)__ldcg(gp + 2 * gstride + g0 + q);
     if (cq) a += __ldcg(gp + gstride + g0 + q);
-    c += cq;
+    cnt += cq;
   }
-  kick_combine(m, a, c);
-  if (lane != 0) return;
+  kick_combine(m, a, cnt);
+  if (lane != 0) return -1;
   const double mx = __longlong_as_double((long long)m);
-  const double tsum = a, tcnt = (double)c;
+  const double tsum = a, tcnt = (double)cnt;
   DevScalars* R = S.sc + r;
   R->thermo_sum = tsum;
   R->thermo_cnt = tcnt;
@@ -610,6 +622,15 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevStat
     if (T > 0.0) sf = sqrt(1. + nd / P.tau_spec * (Ttar / T - 1.));
   }
   R->thermo_s = sf;
+  return r;
+}
+
+template <int BATCH>
+__global__ void __launch_bounds__(kKickThreads) k_spec_kick(DevParams P, DevState S, int apply,
+                                                             double Ttar) {
+  pdl_wait();
+  pdl_trigger();
+  spec_kick_chunk<BATCH>(P, S, blockIdx.x, apply, Ttar, 0);
 }
 
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
@@ -619,6 +640,124 @@ cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState
   // a programmatic dependent of the force kernels before it
   return launch_k(P.nrep > 1 ? k_spec_kick<1> : k_spec_kick<0>, nb, kKickThreads, 0, L.stream,
                   L.pdl && apply, P, S, apply, Ttar);
+}
+
+// ---- the kick of a step fused with the drift of the next -----------------
+// One persistent grid of at most as many blocks as the device holds at once
+// takes the chunks of kKickThreads atoms in turn: it kicks every chunk (the
+// kick above, completion tickets and all), waits at a grid barrier, then
+// drifts every chunk with the dt and thermostat factor just derived (the
+// drift above). The barrier is the kick's own completion: the warp that
+// finalizes the step's reductions (for a batch, the last of the replicas'
+// final warps) also decides whether the step loop goes on, sets the graph's
+// conditions (the rebuild IF node's to 0, the loop's WHILE node's when the
+// kernel ends a step pair), resets the force counters and releases the
+// others by advancing a generation counter; they spin on it with a bounded
+// wait (kKdSpinLimit polls, then a time-out flag that the host reports as
+// FIBMD_ETIMEOUT, and no drift). When the loop stops, nothing drifts and the
+// state is that of a completed step. A block whose chunk moved an atom half
+// the skin sets the rebuild condition to 1.
+constexpr long long kKdSpinLimit = 1ll << 22;  // ~0.5 s with the back-off below
+
+__device__ __forceinline__ void kd_release(const DevState& S, LoopCtl* loop,
+                                           cudaGraphConditionalHandle hif,
+                                           cudaGraphConditionalHandle hwhile, int last_of_pair) {
+  DevScalars* sc = S.sc;
+  reset_force_counters(S);
+  int cont = 1;
+  if (last_of_pair) {
+    const long long r = loop->pairs - 1;
+    loop->pairs = r;
+    loop->pairs_run += 1;
+    cont = (r > 0 && ((volatile DevScalars*)sc)->time < loop->t_stop) ? 1 : 0;
+    cudaGraphSetConditional(hwhile, (unsigned)cont);
+  }
+  cudaGraphSetConditional(hif, 0u);
+  sc->kd_cont = cont;
+  __threadfence();
+  atomicAdd(&sc->kd_gen, 1u);
+}
+
+template <int BATCH>
+__global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState S, double Ttar,
+                                                           LoopCtl* loop,
+                                                           cudaGraphConditionalHandle hif,
+                                                           cudaGraphConditionalHandle hwhile,
+                                                           int last_of_pair) {
+  const int nchunk = (P.N + kKickThreads - 1) / kKickThreads;
+  DevScalars* sc = S.sc;
+  __shared__ unsigned gen0;
+  __shared__ int go;
+  // the generation before this block's chunks can complete the step
+  if (threadIdx.x == 0) gen0 = ((volatile DevScalars*)sc)->kd_gen;
+  __syncthreads();
+  int it = 0;
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x, it++) {
+    const int r = spec_kick_chunk<BATCH>(P, S, c, 1, Ttar, it & 1);
+    if (r >= 0) {
+      bool release = true;
+      if (BATCH) {
+        __threadfence();
+        release = atomicAdd(&sc->kd_reps, 1u) == (unsigned)(P.nrep - 1);
+        if (release) sc->kd_reps = 0u;
+      }
+      if (release) {
+        __threadfence();
+        kd_release(S, loop, hif, hwhile, last_of_pair);
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    long long n = 0;
+    int ok = 1;
+    while (((volatile DevScalars*)sc)->kd_gen == gen0) {
+      if (++n > kKdSpinLimit) {
+        ok = 0;
+        atomicOr(&sc->kd_timeout, 1);
+        break;
+      }
+      __nanosleep(100);
+    }
+    __threadfence();
+    go = ok && ((volatile DevScalars*)sc)->kd_cont;
+  }
+  __syncthreads();
+  if (!go) return;
+  // the drift of the next step uses the force just computed (the host swaps
+  // the two buffers after a kick; here the kick zeroed the older one)
+  DevState Sn = S;
+  Sn.frc = S.frc_new;
+  Sn.frc_new = S.frc;
+  for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
+    const bool any = spec_drift_chunk<BATCH>(P, Sn, c);
+    if (threadIdx.x == 0 && any) {
+      sc->need_rebuild = 1;
+      cudaGraphSetConditional(hif, 1u);
+    }
+  }
+}
+
+// Blocks of k_spec_kd the device holds at once (the grid of every launch is
+// at most this, so that all of its blocks are resident together).
+int spec_kd_resident_blocks(int nrep, int sms) {
+  int per_sm = 0;
+  const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, nrep > 1 ? k_spec_kd<1> : k_spec_kd<0>, kKickThreads, 0);
+  if (e != cudaSuccess || per_sm < 1) return 0;
+  return per_sm * sms;
+}
+
+cudaError_t launch_spec_kd(const Launch& L, const DevParams& P, const DevState& S, double Ttar,
+                           LoopCtl* loop, cudaGraphConditionalHandle hif,
+                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks) {
+  const int nchunk = (P.N + kKickThreads - 1) / kKickThreads;
+  if (nchunk > kMaxRedBlocks || max_blocks < 1) return cudaErrorInvalidConfiguration;
+  const int nb = min(nchunk, max_blocks);
+  if (P.nrep > 1)
+    k_spec_kd<1><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair);
+  else
+    k_spec_kd<0><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair);
+  return cudaGetLastError();
 }
 
 // ---- dose: successive impacts without host round trips ---------------------

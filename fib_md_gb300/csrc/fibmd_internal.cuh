@@ -154,6 +154,10 @@ struct DevScalars {
   int need_rebuild;
   int removed_count;   // spec: lattice atoms removed (sputtered)
   int ions_removed;    //       ions removed (backscattered)
+  unsigned kd_gen;     // fused kick-drift: barrier generation
+  unsigned kd_reps;    //                   replicas finalized this step
+  int kd_cont;         //                   the step loop goes on (drift)
+  int kd_timeout;      //                   a barrier wait gave up
   unsigned long long rebuilds;  // list builds since creation
   unsigned int ticket[8];
   unsigned long long counters[4];
@@ -478,6 +482,13 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
                               bool pdl_first = false);
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
+// the kick of a step fused with the drift of the next (a grid of at most
+// max_blocks resident blocks); in a graph, hif is the following rebuild IF
+// node's handle and, when last_of_pair, hwhile the step loop's WHILE node
+cudaError_t launch_spec_kd(const Launch& L, const DevParams& P, const DevState& S, double Ttar,
+                           LoopCtl* loop, cudaGraphConditionalHandle hif,
+                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks);
+int spec_kd_resident_blocks(int nrep, int sms);
 // fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
 cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,
                             cudaGraphConditionalHandle h, bool pdl = false);

@@ -338,3 +338,52 @@ def test_force_stage_switch_and_autotune(gpu_lib):
     c.steps(2, 1200, 0, 0.0, 300.0)  # tunes before each 1000 steps
     assert c.get_option("stage") in (8, 10, 1)
     assert c.get_option("autotune") == 1
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_fused_kick_drift_matches_unfused(gpu_lib, precision):
+    """The graph's fused kick + next drift (one persistent kernel with a grid
+    barrier) runs the same steps as the unfused graph: positions within
+    1e-8 A (the force sums' order differs), the same time and rebuilds,
+    across calls of odd and even step counts."""
+    s, X, V = _spec_system(precision=precision)
+    a = _ctx(s, X, V, precision, graph=True)
+    b = _ctx(s, X, V, precision, graph=True)
+    b.set_option("fuse", 0)
+    assert a.get_option("fuse") == 1 and b.get_option("fuse") == 0
+    la, ta, lb, tb = 0, 0.0, 0, 0.0
+    for n in (120, 37, 60):
+        la, ta, _, _ = a.steps(2, n, la, ta, 300.0)
+        lb, tb, _, _ = b.steps(2, n, lb, tb, 300.0)
+    Xa, _, _ = a.download()
+    Xb, _, _ = b.download()
+    assert la == lb == 217 and abs(ta - tb) <= 1e-12 * tb
+    assert np.abs(Xa - Xb).max() < 1e-18
+    assert a.work_counters()[4] == b.work_counters()[4]
+    assert np.array_equal(a.get_tags(), b.get_tags())
+
+
+def test_fused_barrier_timeout_is_reported(gpu_lib):
+    """The fused kernel's grid barrier gives up after a bounded wait: with a
+    grid larger than the blocks the device holds at once (the kd_grid test
+    hook; a 256k-atom slab has more chunks than resident blocks), the
+    resident blocks' waits run out, the call returns FIBMD_ETIMEOUT and the
+    context stays usable: after a fresh upload it steps normally."""
+    import bench
+    import fib_md_gb300 as fm
+
+    w = bench.make_workload((40, 40, 20), list_skin_A=0.6)
+    g = bench.make_ctx(w, 1)
+    resident = int(g.get_option("kd_grid"))
+    nchunk = (w["params"].Natm + 255) // 256
+    assert 0 < resident < nchunk
+    g.set_option("kd_grid", nchunk)
+    with pytest.raises(fm.FibmdError) as e:
+        g.steps(2, 2, 0, 0.0, 300.0)
+    assert e.value.code == fm._abi.ETIMEOUT and "grid barrier" in str(e.value)
+    g.set_option("kd_grid", 0)
+    bench.fresh_state(g, w)
+    lt, t, _, _ = g.steps(2, 20, 0, 0.0, 300.0)
+    X, _, _ = g.download()
+    assert lt == 20 and t > 0 and np.isfinite(X).all()
+    g.close()
