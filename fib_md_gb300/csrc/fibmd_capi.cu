@@ -145,6 +145,15 @@ static Launch launch_of(const fibmd_ctx* ctx) {
   return L;
 }
 
+// The fused kick-drift runs when allowed ("fuse") and, unless the kd_grid
+// test hook sets its grid, only where every chunk gets a block of its own
+// in one resident wave (measured: no faster where blocks take two chunks)
+static bool fuse_in_use(const fibmd_ctx* ctx) {
+  if (!ctx->fuse || ctx->kd_blocks <= 0) return false;
+  const int nchunk = (ctx->P.N + kKickThreads - 1) / kKickThreads;
+  return ctx->kd_grid > 0 || nchunk <= ctx->kd_blocks;
+}
+
 static cudaEvent_t get_event(fibmd_ctx* ctx) {
   if (!ctx->pool.empty()) {
     cudaEvent_t e = ctx->pool.back();
@@ -1334,7 +1343,7 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
   } else if (!std::strcmp(key, "pdl")) {
     *value = ctx->pdl ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "fuse")) {
-    *value = (ctx->fuse && ctx->kd_blocks > 0) ? 1.0 : 0.0;
+    *value = fuse_in_use(ctx) ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "kd_grid")) {
     *value = (double)(ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks);
   } else if (!std::strcmp(key, "stage")) {
@@ -1421,7 +1430,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   if (!ctx->cap2) CK(cudaStreamCreateWithFlags(&ctx->cap2, cudaStreamNonBlocking));
   const DevParams& P = ctx->P;
   const double Ttar = ctx->p.Ttar1;
-  const bool fused = ctx->fuse && ctx->kd_blocks > 0;
+  const bool fused = fuse_in_use(ctx);
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
   ctx->graph = g;

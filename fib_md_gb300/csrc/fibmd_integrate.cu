@@ -460,6 +460,8 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
 // partials is a long dependent chain. Sums run in a fixed order
 // (deterministic). The replica's last warp derives dt and the Berendsen
 // factor.
+constexpr int kKickOneGroup = 256;  // chunks of a replica counted in one level
+
 // Warp max of non-negative doubles held as bits: redux.sync on the high
 // words, then on the low words of the lanes holding the high maximum.
 __device__ __forceinline__ unsigned long long warp_max_bits(unsigned long long v) {
@@ -548,9 +550,13 @@ __device__ __forceinline__ int spec_kick_chunk(const DevParams& P, const DevStat
   const int r = BATCH ? __shfl_sync(0xffffffffu, rep_of_flags(fl), 0) : 0;
   const Geo& G = S.geo[r];
   const int nblk = G.blk_end - G.blk_begin;
-  const int grp = (c - G.blk_begin) / kKickGroup;
-  const int gsize = min(kKickGroup, nblk - grp * kKickGroup);
-  const int ngrp = (nblk + kKickGroup - 1) / kKickGroup;
+  // a replica of at most kKickOneGroup chunks counts completion in one
+  // group (one level: its last chunk combines every chunk's partial), a
+  // larger one in groups of kKickGroup chunks
+  const int gw = nblk <= kKickOneGroup ? nblk : kKickGroup;
+  const int grp = (c - G.blk_begin) / gw;
+  const int gsize = min(gw, nblk - grp * gw);
+  const int ngrp = (nblk + gw - 1) / gw;
   // group slots of different replicas never share an index
   const int gidx = G.blk_begin / kKickGroup + r + grp;
   const size_t gstride = (size_t)kMaxRedBlocks / kKickGroup + P.nrep + 2;
@@ -569,11 +575,13 @@ __device__ __forceinline__ int spec_kick_chunk(const DevParams& P, const DevStat
   m = 0ull;
   a = 0.0;
   cnt = 0;
-  if (lane < gsize) {
-    const int b = G.blk_begin + grp * kKickGroup + lane;
-    m = (unsigned long long)__double_as_longlong(__ldcg(S.partials + b));
-    cnt = (int)__ldcg(S.partials + 2 * kMaxRedBlocks + b);
-    if (cnt) a = __ldcg(S.partials + kMaxRedBlocks + b);
+  for (int q = lane; q < gsize; q += 32) {
+    const int b = G.blk_begin + grp * gw + q;
+    const unsigned long long x = (unsigned long long)__double_as_longlong(__ldcg(S.partials + b));
+    m = x > m ? x : m;
+    const int cq = (int)__ldcg(S.partials + 2 * kMaxRedBlocks + b);
+    if (cq) a += __ldcg(S.partials + kMaxRedBlocks + b);
+    cnt += cq;
   }
   kick_combine(m, a, cnt);
   double* gp = S.group_part;

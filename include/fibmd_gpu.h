@@ -293,9 +293,11 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    launched as programmatic dependents of the kernel before them, so each
    is dispatched during its predecessor's tail and waits in hardware for its
    completion; a graph that cannot be captured so is captured with plain
-   launches and the option reads 0 afterwards), "fuse" (default 1: the
-   graph runs each step's kick and the next step's drift as one persistent
-   kernel whose blocks meet at a grid barrier with a bounded wait; a wait
+   launches and the option reads 0 afterwards), "fuse" (default 1: where
+   every chunk of 256 atoms gets a block in one resident wave, the graph
+   runs each step's kick and the next step's drift as one persistent
+   kernel whose blocks meet at a grid barrier with a bounded wait; reads 1
+   where that is in use; a wait
    that gives up ends the call with FIBMD_ETIMEOUT and leaves the state
    invalid until the next upload) and "kd_grid" (that kernel's grid; 0, the
    default, is the number of its blocks the device holds at once, which

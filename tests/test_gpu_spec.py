@@ -377,11 +377,14 @@ def test_fused_barrier_timeout_is_reported(gpu_lib):
     resident = int(g.get_option("kd_grid"))
     nchunk = (w["params"].Natm + 255) // 256
     assert 0 < resident < nchunk
+    assert g.get_option("fuse") == 0  # more chunks than resident blocks: unfused
     g.set_option("kd_grid", nchunk)
+    assert g.get_option("fuse") == 1
     with pytest.raises(fm.FibmdError) as e:
         g.steps(2, 2, 0, 0.0, 300.0)
     assert e.value.code == fm._abi.ETIMEOUT and "grid barrier" in str(e.value)
     g.set_option("kd_grid", 0)
+    g.set_option("fuse", 1)
     bench.fresh_state(g, w)
     lt, t, _, _ = g.steps(2, 20, 0, 0.0, 300.0)
     X, _, _ = g.download()
