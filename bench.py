@@ -62,11 +62,13 @@ def parse():
     ap.add_argument("--no-config1", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--list-skin", type=float, default=0.6,
-                    help="spec-mode list skin in Angstrom (0: the reference's list radii). "
-                         "The fastest atom moves dx_max per step, so the skin sets the "
-                         "rebuild interval against the list length the force kernel scans; "
-                         "0.6 A (a rebuild every ~6 steps of the cascade) measured fastest")
+    ap.add_argument("--list-skin", type=float, default=-1.0,
+                    help="spec-mode list skin in Angstrom; negative (the default): the "
+                         "library's run-time tuning, which starts from 0.6 A and re-times "
+                         "0.45, 0.6 and 0.81 A on the current state; 0: the reference's "
+                         "list radii; positive: that start value (still tuned unless the "
+                         "context's skin_tune option is 0). The oracle runs take the start "
+                         "value (0.6 A for a negative one)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the step loop launch by launch (for a profiler's launch list)")
     ap.add_argument("--ensemble-replicas", type=int, default=256)
@@ -160,6 +162,19 @@ def make_ctx(w, precision):
     return g
 
 
+def skin_text(skin_A):
+    if skin_A < 0:
+        return "tuned at run time (start 0.6 A, candidates 0.45, 0.6, 0.81 A)"
+    if skin_A == 0:
+        return "reference radii"
+    return f"tuned at run time (start {skin_A} A)"
+
+
+def oracle_skin(skin_A):
+    """The oracle's list skin (A): the start of the GPU run's tuning."""
+    return 0.6 if skin_A < 0 else skin_A
+
+
 def workload_config(args, cells, N):
     """The `config` object of both arms' JSON lines (static: what is run)."""
     return {
@@ -169,7 +184,7 @@ def workload_config(args, cells, N):
         "window": f"MD steps 1-{args.md_steps} of the cascade from the ion's start; every "
                   "bench step starts from the seeded initial state",
         "md_steps_per_step": args.md_steps, "mode": "spec",
-        "list_skin_A": args.list_skin if args.list_skin > 0 else "reference radii",
+        "list_skin": skin_text(args.list_skin),
         "seed": 2001,
         "parallelism": "replicas (one cascade per GPU)",
         "l2": "flushed before every timed step",
@@ -305,6 +320,7 @@ def bench_ours(args, rank, world, dist):
         barrier()
         wall = time.perf_counter() - w0
     stage_end = int(g.get_option("stage"))
+    skin_end = g.get_option("skin")
     X_end, _, _ = g.download()
     value, t_dev, atom_steps = replica_rate(dist, float(N) * args.md_steps * args.steps,
                                             sum(times), "cuda")
@@ -432,9 +448,11 @@ def bench_ours(args, rank, world, dist):
         "data": "synthetic (seeded)",
         "config": workload_config(args, cells, N),
         "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
-        "force_stage": {"autotune": "before every 1000 steps among 8 or 10 staged legs per "
-                                    "thread and 8 lanes per centre (1)",
-                        "at_end": stage_end},
+        "autotune": {"force_path": "before every 1000 steps among 8 or 10 staged legs per "
+                                   "thread and 8 lanes per centre (1)",
+                     "force_path_at_end": stage_end,
+                     "list_skin": skin_text(args.list_skin),
+                     "list_skin_at_end_A": skin_end},
         "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
                  "window": "the same", "mixed_over_fp64": value / value64,
                  "ms_per_step": 1e3 * sum(t64) / n64,
@@ -523,6 +541,7 @@ def bench_large(args):
     secs = a.elapsed_time(b) / 1e3
     rebuilds = g.work_counters()[4] - rb0
     stage_end = int(g.get_option("stage"))
+    skin_end = g.get_option("skin")
     # the main force kernel timed live over a launch-by-launch segment
     g.set_option("graph", 0)
     g.set_option("kernel_timing", 1)
@@ -543,7 +562,7 @@ def bench_large(args):
         "config": "Si slab 64x64x32 unit cells (1,048,576 Si + 1 Ga), 30 keV Ga at normal "
                   f"incidence on the slab centre, {args.large_steps} variable-dt steps, "
                   "mixed precision, CUDA-graph step loop, list skin "
-                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+                  f"{skin_text(args.list_skin)}",
         "atoms": N, "md_steps": args.large_steps,
         "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
         "simulated_ps": t_sim * 1e12,
@@ -551,6 +570,7 @@ def bench_large(args):
         "force_stage": "autotuned every 1000 steps among 8 or 10 staged legs per thread "
                        "and 8 lanes per centre (1); "
                        f"{stage_end} at the end",
+        "list_skin_at_end_A": skin_end,
         "fp32_pipe": {"kernel": "k_force<mixed>", "achieved_tflops": f32, "peak_tflops": fp32_peak,
                       "frac": f32 / fp32_peak, "force_kernel_us": 1e6 * fk,
                       "peak_source": "measured in this run (FFMA loop)"},
@@ -690,10 +710,11 @@ def run_ensemble_batch(slabs, precision, steps):
     stats = [(int(sp[r]), float(dp[r]), int(dc[r])) for r in range(len(slabs))]
     atoms = int(b.natm.sum())
     stage = int(b.get_option("stage"))
+    skin = b.get_option("skin")
     b.close()
     return {"wall_s": wall, "atoms": atoms, "padded_atoms": int(b.N), "rebuilds": int(rebuilds),
             "removed": removed.tolist(), "sim_time_s": t_sim.tolist(), "stats": stats,
-            "force_stage": stage}
+            "force_stage": stage, "list_skin_A": skin}
 
 
 def run_plain(slab, steps):
@@ -756,7 +777,7 @@ def bench_ensemble(args):
     return {
         "config": f"{nrep} impacts, U{{6..12}}^2 x 10 unit-cell slabs, U(0.5,5) keV Ga, "
                   f"U(0,30) deg, {steps} variable-dt steps each, one batch context, list skin "
-                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+                  f"{skin_text(args.list_skin)}",
         "impacts_per_hour": {"mixed_batched": ih(mixed), "fp64_batched": ih(fp64),
                              "fp64_plain": 3600.0 / plain_s},
         "mixed_batched_over_fp64_plain": ih(mixed) * plain_s / 3600.0,
@@ -768,6 +789,7 @@ def bench_ensemble(args):
         "atoms": mixed["atoms"], "padded_atoms": mixed["padded_atoms"],
         "rebuild_fraction": {"mixed": mixed["rebuilds"] / steps, "fp64": fp64["rebuilds"] / steps},
         "mixed_force_stage_at_end": mixed["force_stage"],
+        "list_skin_at_end_A": {"mixed": mixed["list_skin_A"], "fp64": fp64["list_skin_A"]},
         "mixed_vs_fp64_two_sample": cmp,
         "statistically_consistent_95": ok,
         "timing": "wall clock from upload of the initial states to the downloaded final states",
@@ -819,7 +841,7 @@ def bench_dose(args):
                   "impacts at normal incidence in a 30x30 A window (seed 4001), 3000 steps "
                   "then 2 ps relaxation each, atoms 15 A above the surface removed, one "
                   "device-side dose call, list skin "
-                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+                  f"{skin_text(args.list_skin)}",
         "impacts": n,
         "impacts_per_hour": {"mixed": 3600.0 * n / mixed["wall_s"]},
         "wall_s": {"mixed": mixed["wall_s"]},
@@ -919,7 +941,7 @@ def dose_study(args):
         "config": "20x20x12 unit cells (38,400 Si), 2 keV Ga at normal incidence at seeded "
                   "uniform points of a 30x30 A window, 3000 steps then 2 ps of relaxation per "
                   "impact, atoms 15 A above the surface removed, spec mode, list skin "
-                  f"{args.list_skin} A, device-side dose calls of {args.dose_chunk} impacts",
+                  f"{skin_text(args.list_skin)}, device-side dose calls of {args.dose_chunk} impacts",
         "seeds": seeds,
         "full_dose": {"seed": seeds[0], "precision": "mixed", **runs[seeds[0]]["mixed"]},
         "comparison": {
@@ -983,7 +1005,7 @@ def bench_config1(args, repeats=3, cpu_sample=200):
     import oracle_ffi as of
 
     ow = oracle_workload(cells, seed=1001, energy_eV=500.0, polar_deg=0.0,
-                         list_skin_A=args.list_skin)
+                         list_skin_A=oracle_skin(args.list_skin))
     p = ow["params"].copy()
     o = of.Oracle(p)
     o.load(ow["X"], ow["V"], ow["Xi"], ow["mass"], ow["atype"], ow["xsides"])
@@ -998,7 +1020,7 @@ def bench_config1(args, repeats=3, cpu_sample=200):
         "config": f"8x8x8 unit cells ({N - 1} Si + 1 Ga), 500 eV Ga at normal incidence 10 A "
                   f"above the surface, seed 1001, 300 K, {steps} variable-dt steps from the "
                   "ion's start, spec mode, list skin "
-                  f"{args.list_skin if args.list_skin > 0 else 'reference radii'}",
+                  f"{skin_text(args.list_skin)}",
         **res,
         "cpu_oracle": {"atom_steps_per_s": cpu, "cores": nthreads, "kind": "port",
                        "algorithm": CPU_ALGORITHM,
@@ -1017,7 +1039,7 @@ def _oracle_cascade(cells, list_skin_A, nthreads):
     sys.path.insert(0, str(ROOT / "tests"))
     import oracle_ffi as of
 
-    w = oracle_workload(cells, list_skin_A=list_skin_A)
+    w = oracle_workload(cells, list_skin_A=oracle_skin(list_skin_A))
     p = w["params"].copy()
     p.mode = 1
     o = of.Oracle(p)

@@ -97,6 +97,24 @@ struct fibmd_ctx {
   int kd_grid = 0;         // option "kd_grid": its grid size instead (tests)
   int graph_fuse = -1;
   LoopCtl* d_loop = nullptr;
+  // spec mode: the candidate list skins, each with its parameters and
+  // per-replica geometry (cell grids differ with the list radius); the one
+  // in use is skin_cur, re-chosen by timing ("skin_tune")
+  struct SkinSet {
+    double skin = 0.0;
+    DevParams P;
+    std::vector<Geo> geo;
+    Geo* d_geo = nullptr;
+  };
+  std::vector<SkinSet> skins;
+  int skin_cur = 0;
+  bool skin_tune = true;
+  int graph_skin = -1;
+  long long graph_chunks = 0;  // tuning chunks run (the skin's re-tuning cadence)
+  double umax = 0.0;           // the 2-body table's extent
+  int tab_last = 0;
+  std::vector<fibmd_replica> reps;       // a batch's replicas
+  std::vector<long long> rep_begin;      // and their first atoms
   // replicas: one for a single system, several for a batched ensemble
   Geo geo0;                 // the single system's geometry
   std::vector<Geo> geo;     // per replica (uploaded to S.geo)
@@ -152,6 +170,29 @@ static bool fuse_in_use(const fibmd_ctx* ctx) {
   if (!ctx->fuse || ctx->kd_blocks <= 0) return false;
   const int nchunk = (ctx->P.N + kKickThreads - 1) / kKickThreads;
   return ctx->kd_grid > 0 || nchunk <= ctx->kd_blocks;
+}
+
+// Switches to candidate skin k: its parameters and geometry; the next step
+// rebuilds the lists for the new radius (and the step graph is captured
+// again, the parameters being kernel arguments).
+static int set_skin(fibmd_ctx* ctx, int k) {
+  if (k == ctx->skin_cur) return FIBMD_OK;
+  const fibmd_ctx::SkinSet& set = ctx->skins[(size_t)k];
+  const int nfired = ctx->P.nfired;
+  ctx->P = set.P;
+  ctx->P.nfired = nfired;
+  ctx->geo = set.geo;
+  ctx->S.geo = set.d_geo;
+  ctx->skin_cur = k;
+  const int one = 1;
+  const cudaError_t e = cudaMemcpyAsync(&ctx->S.sc->need_rebuild, &one, sizeof(int),
+                                        cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    ctx->err = std::string("set_skin: ") + cudaGetErrorString(e);
+    return FIBMD_ECUDA;
+  }
+  return FIBMD_OK;
 }
 
 static cudaEvent_t get_event(fibmd_ctx* ctx) {
@@ -238,6 +279,9 @@ static void list_radii(const fibmd_params& p, double* rc, double* rclj) {
 }
 
 constexpr double kRemoveBelow = 10.0e-10;  // m below the lowest plane
+// spec mode's list skin when the parameters ask for it to be chosen
+// (list_skin < 0): the start of the run-time tuning
+constexpr double kDefaultSkin = 0.6e-10;
 
 int derive_geo(const fibmd_params& p, const double Lb[3], double remove_z, Geo& G, char* err,
                int errlen) {
@@ -465,9 +509,81 @@ static int derive_params(fibmd_ctx* ctx) {
   double umax = 0.0;
   int last = 0;
   build_ref_table(p, ctx->tab.data(), ctx->tabu.data(), &umax, &last);
+  ctx->umax = umax;
+  ctx->tab_last = last;
   char err[256] = "";
   const int rc = derive_dev_params(p, ctx->impact, umax, last, ctx->P, ctx->geo0, err, sizeof err);
   if (rc) return fail(ctx, rc, "%s", err);
+  return FIBMD_OK;
+}
+
+// Parameters and per-replica geometry of the context with list skin `skin`
+// (a single system, or the batch whose replicas ctx->reps holds).
+static int derive_skin(const fibmd_ctx* ctx, double skin, fibmd_ctx::SkinSet& out, char* err,
+                       int errlen) {
+  fibmd_params q = ctx->p;
+  q.list_skin = skin;
+  Geo g0;
+  int rc = derive_dev_params(q, ctx->impact, ctx->umax, ctx->tab_last, out.P, g0, err, errlen);
+  if (rc) return rc;
+  out.skin = skin;
+  if (ctx->reps.empty()) {
+    out.geo.assign(1, g0);
+    return FIBMD_OK;
+  }
+  const int nrep = (int)ctx->reps.size();
+  out.geo.resize((size_t)nrep);
+  long long cells = 0, nion = 0;
+  int reach = 1;
+  for (int r = 0; r < nrep; r++) {
+    const fibmd_replica& R = ctx->reps[(size_t)r];
+    Geo& G = out.geo[(size_t)r];
+    rc = derive_geo(q, R.Lb, R.remove_z, G, err, errlen);
+    if (rc) return rc;
+    G.cell_off = (int)cells;
+    cells += G.ncell;
+    G.atom_begin = (int)ctx->rep_begin[(size_t)r];
+    G.atom_end = (int)(ctx->rep_begin[(size_t)r] + R.natm);
+    G.blk_begin = G.atom_begin / kKickThreads;
+    G.blk_end = (G.atom_end + kKickThreads - 1) / kKickThreads;
+    reach = std::max(reach, G.mol_reach);
+    nion += R.natm - R.nsg;
+  }
+  if (cells > (1ll << 30)) {
+    std::snprintf(err, (size_t)errlen, "batch: %lld cells", cells);
+    return FIBMD_EINVAL;
+  }
+  out.P.nrep = nrep;
+  out.P.nion = (int)nion;
+  out.P.nfired = q.Natm;
+  out.P.ncell = (int)cells;
+  out.P.mol_reach = reach;
+  return FIBMD_OK;
+}
+
+// The candidate skins: spec mode with a list skin takes 0.75, 1 and 1.35
+// times the start value (a candidate whose radius leaves the 2-body table is
+// dropped); otherwise the one set of the parameters as given.
+static int derive_skins(fibmd_ctx* ctx) {
+  const double s0 = ctx->p.list_skin;
+  std::vector<double> cand;
+  if (ctx->p.mode == FIBMD_MODE_SPEC && s0 > 0.0) cand = {0.75 * s0, s0, 1.35 * s0};
+  else cand = {s0};
+  ctx->skins.clear();
+  char err[256] = "";
+  for (double sk : cand) {
+    fibmd_ctx::SkinSet set;
+    const int rc = derive_skin(ctx, sk, set, err, sizeof err);
+    if (rc) {
+      if (sk == s0) return fail(ctx, rc, "%s", err);
+      continue;
+    }
+    if (sk == s0) ctx->skin_cur = (int)ctx->skins.size();
+    ctx->skins.push_back(set);
+  }
+  const fibmd_ctx::SkinSet& cur = ctx->skins[(size_t)ctx->skin_cur];
+  ctx->P = cur.P;
+  ctx->geo = cur.geo;
   return FIBMD_OK;
 }
 
@@ -623,7 +739,9 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
   // the parameters are checked (host arithmetic only) before the device is
   ctx = new fibmd_ctx();
   ctx->p = *p;
+  if (ctx->p.mode == FIBMD_MODE_SPEC && ctx->p.list_skin < 0.0) ctx->p.list_skin = kDefaultSkin;
   int rc = derive_params(ctx);
+  if (rc == FIBMD_OK) rc = derive_skins(ctx);
   if (rc) {
     set_noctx_error(ctx->err.c_str());
     delete ctx;
@@ -635,7 +753,6 @@ int fibmd_gpu_create(const fibmd_params* p, fibmd_ctx** out) {
     delete ctx;
     return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
   }
-  ctx->geo.assign(1, ctx->geo0);
   ctx->rep_of.assign((size_t)p->Natm, 0);
   std::vector<int> ions;
   for (int i = p->Nsg; i < p->Natm; i++) ions.push_back(i);
@@ -657,7 +774,10 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   DevState& S = ctx->S;
   std::memset(&S, 0, sizeof S);
   S.N = (int)N;
-  int nscan = (ctx->P.ncell + 1 + 1023) / 1024;
+  // the cell arrays hold the largest grid of the candidate skins
+  int max_cells = 0;
+  for (const auto& k : ctx->skins) max_cells = std::max(max_cells, k.P.ncell);
+  int nscan = (max_cells + 1 + 1023) / 1024;
 #define AL(ptr, n)                       \
   do {                                   \
     int r_ = dalloc(ctx, &(ptr), (n));   \
@@ -678,8 +798,8 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   AL(S.inv_mass, N);
   AL(S.atype, N);
   AL(S.flags, N);
-  AL(S.cell_count, (size_t)ctx->P.ncell + 1);
-  AL(S.cell_start, (size_t)ctx->P.ncell + 1);
+  AL(S.cell_count, (size_t)max_cells + 1);
+  AL(S.cell_start, (size_t)max_cells + 1);
   AL(S.cell_atoms, N);
   AL(S.posq_cell, N);
   AL(S.atom_cell, N);
@@ -712,11 +832,10 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
     return FIBMD_ECUDA;
   }
   AL(S.sc, R);
-  Geo* geo = nullptr;
+  for (auto& k : ctx->skins) AL(k.d_geo, R);
   int* ion_list = nullptr;
-  AL(geo, R);
   AL(ion_list, ions.size());
-  S.geo = geo;
+  S.geo = ctx->skins[(size_t)ctx->skin_cur].d_geo;
   S.ion_list = ion_list;
   AL(ctx->d_stage, 3 * N);
   AL(ctx->d_ke, N);
@@ -733,7 +852,8 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
                   cudaMemcpyHostToDevice, ctx->stream);
   cudaMemcpyAsync(tabu, ctx->tabu.data(), sizeof(double) * ctx->tabu.size(),
                   cudaMemcpyHostToDevice, ctx->stream);
-  cudaMemcpyAsync(geo, ctx->geo.data(), sizeof(Geo) * R, cudaMemcpyHostToDevice, ctx->stream);
+  for (auto& k : ctx->skins)
+    cudaMemcpyAsync(k.d_geo, k.geo.data(), sizeof(Geo) * R, cudaMemcpyHostToDevice, ctx->stream);
   if (!ions.empty())
     cudaMemcpyAsync(ion_list, ions.data(), sizeof(int) * ions.size(), cudaMemcpyHostToDevice,
                     ctx->stream);
@@ -784,6 +904,8 @@ int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica*
   if (e != cudaSuccess || ndev == 0)
     return fail(nullptr, FIBMD_ECUDA, "no CUDA device: %s", cudaGetErrorString(e));
 
+  if (off / kKickThreads > kMaxRedBlocks) return fail(nullptr, FIBMD_EINVAL, "batch: too many atoms");
+
   fibmd_ctx* ctx = new fibmd_ctx();
   fibmd_params q = *p;
   q.Natm = (int)off;
@@ -791,48 +913,24 @@ int fibmd_gpu_batch_create(const fibmd_params* p, int nrep, const fibmd_replica*
   q.Nlj = (int)nion;
   for (int d = 0; d < 3; d++) q.Lb[d] = reps[0].Lb[d];
   q.remove_z = reps[0].remove_z;
+  if (q.list_skin < 0.0) q.list_skin = kDefaultSkin;
   ctx->p = q;
+  ctx->reps.assign(reps, reps + nrep);
+  ctx->rep_begin = begin;
   int rc = derive_params(ctx);
+  if (rc == FIBMD_OK) rc = derive_skins(ctx);
   if (rc) {
     set_noctx_error(ctx->err.c_str());
     delete ctx;
     return rc;
   }
-  ctx->geo.resize((size_t)nrep);
   ctx->rep_of.assign((size_t)off, -1);
   std::vector<int> ions;
-  long long cells = 0;
-  int reach = 1;
   for (int r = 0; r < nrep; r++) {
-    char err[256] = "";
-    Geo& G = ctx->geo[(size_t)r];
-    rc = derive_geo(q, reps[r].Lb, reps[r].remove_z, G, err, sizeof err);
-    if (rc) {
-      set_noctx_error(err);
-      delete ctx;
-      return rc;
-    }
-    G.cell_off = (int)cells;
-    cells += G.ncell;
-    G.atom_begin = (int)begin[r];
-    G.atom_end = (int)(begin[r] + reps[r].natm);
-    G.blk_begin = G.atom_begin / kKickThreads;
-    G.blk_end = (G.atom_end + kKickThreads - 1) / kKickThreads;
-    reach = std::max(reach, G.mol_reach);
+    const Geo& G = ctx->geo[(size_t)r];
     for (int i = G.atom_begin; i < G.atom_end; i++) ctx->rep_of[(size_t)i] = r;
     for (int i = G.atom_begin + reps[r].nsg; i < G.atom_end; i++) ions.push_back(i);
   }
-  if (cells > (1ll << 30) || off / kKickThreads > kMaxRedBlocks) {
-    set_noctx_error("batch: too many cells or atoms");
-    delete ctx;
-    return FIBMD_EINVAL;
-  }
-  DevParams& P = ctx->P;
-  P.nrep = nrep;
-  P.nion = (int)ions.size();
-  P.nfired = (int)off;
-  P.ncell = (int)cells;
-  P.mol_reach = reach;
   return finish_create(ctx, ions, out);
 }
 
@@ -1068,6 +1166,7 @@ int fibmd_gpu_set_impact(fibmd_ctx* ctx, int impact) {
   if (!ctx || impact < 0) return FIBMD_EINVAL;
   ctx->impact = impact;
   ctx->P.nfired = ctx->p.Nsg + impact;
+  for (auto& k : ctx->skins) k.P.nfired = ctx->P.nfired;
   return FIBMD_OK;
 }
 
@@ -1313,6 +1412,17 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->pdl = value != 0.0;
   } else if (!std::strcmp(key, "fuse")) {
     ctx->fuse = value != 0.0;
+  } else if (!std::strcmp(key, "skin_tune")) {
+    ctx->skin_tune = value != 0.0;
+  } else if (!std::strcmp(key, "skin")) {
+    // one of the candidate skins (Angstrom); fixes it (no more tuning)
+    int k = -1;
+    for (size_t q = 0; q < ctx->skins.size(); q++)
+      if (std::fabs(ctx->skins[q].skin * 1e10 - value) < 1e-6) k = (int)q;
+    if (k < 0) return fail(ctx, FIBMD_EINVAL, "skin %g A is not one of the candidates", value);
+    ctx->skin_tune = false;
+    int rc = set_skin(ctx, k);
+    if (rc) return rc;
   } else if (!std::strcmp(key, "kd_grid")) {
     if (value < 0.0 || value > (double)kMaxRedBlocks)
       return fail(ctx, FIBMD_EINVAL, "kd_grid %g out of range", value);
@@ -1344,6 +1454,12 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = ctx->pdl ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "fuse")) {
     *value = fuse_in_use(ctx) ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "skin_tune")) {
+    *value = ctx->skin_tune ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "skin")) {
+    *value = ctx->skins[(size_t)ctx->skin_cur].skin * 1e10;
+  } else if (!std::strcmp(key, "skin_candidates")) {
+    *value = (double)ctx->skins.size();
   } else if (!std::strcmp(key, "kd_grid")) {
     *value = (double)(ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks);
   } else if (!std::strcmp(key, "stage")) {
@@ -1549,6 +1665,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_nfired = P.nfired;
   ctx->graph_pdl = ctx->pdl ? 1 : 0;
   ctx->graph_fuse = ctx->fuse ? 1 : 0;
+  ctx->graph_skin = ctx->skin_cur;
   return FIBMD_OK;
 }
 
@@ -1615,7 +1732,7 @@ static int tune_stage(fibmd_ctx* ctx) {
 static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
       ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
-      ctx->graph_fuse != (ctx->fuse ? 1 : 0)) {
+      ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {
       // a device or driver without programmatic edges in conditional
@@ -1630,6 +1747,51 @@ static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   CK(launch_loop_set(ctx->stream, ctx->d_loop, ctx->S.sc, pairs, relax));
   CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
   return FIBMD_OK;
+}
+
+constexpr long long kSkinTrialPairs = 20;      // step pairs timed per candidate skin
+constexpr long long kSkinTuneEvery = 5;        // tuning chunks between skin tunings
+constexpr long long kSkinTuneMinSteps = 2000;  // shorter calls keep the skin in use
+
+// The list skin, re-chosen on the current state: each candidate runs one
+// step pair (its forced list rebuild and graph capture) and then
+// kSkinTrialPairs pairs timed with CUDA events, the one in use last; the
+// fastest per step is kept if it beats the one in use by 3 %. The trial
+// steps are steps of the run: with any of the skins the lists hold every
+// pair inside the cutoffs, so the trajectory does not depend on the choice.
+// *pairs_run receives the step pairs taken.
+static int tune_skin(fibmd_ctx* ctx, long long* pairs_run) {
+  *pairs_run = 0;
+  const int n = (int)ctx->skins.size();
+  const int start = ctx->skin_cur;
+  cudaEvent_t a = get_event(ctx), b = get_event(ctx);
+  std::vector<float> ms((size_t)n, 0.f);
+  int rc = FIBMD_OK;
+  for (int q = 0; q < n && rc == FIBMD_OK; q++) {
+    const int k = (start + 1 + q) % n;
+    rc = set_skin(ctx, k);
+    if (rc == FIBMD_OK) rc = run_spec_graph(ctx, 1);
+    if (rc) break;
+    cudaEventRecord(a, ctx->stream);
+    rc = run_spec_graph(ctx, kSkinTrialPairs);
+    if (rc) break;
+    cudaEventRecord(b, ctx->stream);
+    const cudaError_t e = cudaEventSynchronize(b);
+    if (e != cudaSuccess) {
+      rc = fail(ctx, FIBMD_ECUDA, "skin tuning: %s", cudaGetErrorString(e));
+      break;
+    }
+    cudaEventElapsedTime(&ms[(size_t)k], a, b);
+    *pairs_run += 1 + kSkinTrialPairs;
+  }
+  ctx->pool.push_back(a);
+  ctx->pool.push_back(b);
+  if (rc) return rc;
+  int best = start;
+  for (int k = 0; k < n; k++)
+    if (ms[(size_t)k] < ms[(size_t)best]) best = k;
+  if (ms[(size_t)best] < 0.97f * ms[(size_t)start]) rc = set_skin(ctx, best);
+  return rc;
 }
 
 static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double* time,
@@ -1654,8 +1816,20 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     // in chunks of kTuneSteps steps, before each of which the binary32 force
     // kernel's stage size is re-chosen on the current state
     const bool tune = ctx->autotune && P.precision == FIBMD_PREC_MIXED && ctx->lists_built;
+    // and in long calls, before every kSkinTuneEvery-th chunk, the list skin
+    const bool stune = ctx->skin_tune && ctx->skins.size() > 1 && ctx->lists_built &&
+                       todo >= kSkinTuneMinSteps;
     for (long long pairs = todo / 2; pairs > 0;) {
-      const long long chunk = tune ? std::min(pairs, kTuneSteps / 2) : pairs;
+      if (stune && ctx->graph_chunks % kSkinTuneEvery == 0 &&
+          pairs > (long long)ctx->skins.size() * (kSkinTrialPairs + 1)) {
+        CK(cudaStreamSynchronize(ctx->stream));
+        long long pr = 0;
+        int rs = tune_skin(ctx, &pr);
+        if (rs) return rs;
+        pairs -= pr;
+      }
+      const long long chunk = (tune || stune) ? std::min(pairs, kTuneSteps / 2) : pairs;
+      ctx->graph_chunks++;
       if (tune) {
         CK(cudaStreamSynchronize(ctx->stream));
         int rt = tune_stage(ctx);

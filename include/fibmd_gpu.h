@@ -132,8 +132,11 @@ typedef struct fibmd_params {
   double mixed_mol_fp64_r;   /* Moliere pairs closer than this (m) stay fp64  */
 
   /* spec mode: list radius = interaction cutoff + list_skin (m) for the SW
-     list (cutoff 0.999*a*sigma) and the Moliere list (2.5*sigma); <= 0
-     keeps the reference's radii (listfac 1.1). Spec mode always finds every
+     list (cutoff 0.999*a*sigma) and the Moliere list (2.5*sigma); 0 keeps
+     the reference's radii (listfac 1.1); < 0 starts from 0.6 A. With a
+     skin, the context also derives 0.75 and 1.35 times it and, in long
+     step calls, re-times the three on the current state and keeps the
+     fastest (options "skin_tune", "skin"). Spec mode always finds every
      Moliere pair (the reference's 27-cell stencil misses those beyond one
      cell). With remove_z > 0 (and remove_z + list radius < Lb(3)) spec mode
      treats z as an open axis: positions are not wrapped in z, the cell
@@ -302,7 +305,14 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    invalid until the next upload) and "kd_grid" (that kernel's grid; 0, the
    default, is the number of its blocks the device holds at once, which
    every wait relies on; a larger value makes the waits give up, a hook for
-   testing the time-out). */
+   testing the time-out), "skin_tune" (default 1: in spec-mode calls of at
+   least 2000 steps, before every 5000 steps, each candidate list skin runs
+   one step pair and then 20 timed pairs of the graph step loop, and the
+   fastest per step is kept; the trial steps are steps of the run, and the
+   trajectory does not depend on the skin since the lists stay complete),
+   "skin" (reads the skin in use in Angstrom; set to one of the candidates
+   it fixes the skin: the lists are rebuilt at the next step) and
+   "skin_candidates" (read only: how many). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
 /* The current value of an option ("stage" reads the force path in use,
    which "autotune" changes as the run goes). */

@@ -174,3 +174,45 @@ def test_spec_force_256k(gpu_lib, ion):
     assert np.sqrt(np.mean(d * d)) / rms < 2e-5
     gm.close()
     o.close()
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_skin_switch_keeps_trajectory(gpu_lib, graph):
+    """The list skin changed in the middle of a run (one of the context's
+    candidates, 0.75 x the start): the next step rebuilds the lists with the
+    new radius and cell grid, and the trajectory stays the oracle's (which
+    keeps the start skin) within 1e-8 A over 100 steps of the cascade."""
+    slab = config1(ion_height_A=1.5)
+    o = of.spec_oracle(slab)
+    g = gpu_ctx(slab, graph=graph)
+    assert g.get_option("skin_candidates") == 3 and abs(g.get_option("skin") - 0.6) < 1e-9
+    lt, t, T = 0, 0.0, 300.0
+    lt, t, T, _ = g.steps(2, 50, lt, t, T)
+    g.set_option("skin", 0.45)
+    assert abs(g.get_option("skin") - 0.45) < 1e-9 and g.get_option("skin_tune") == 0
+    lt, t, T, _ = g.steps(2, 50, lt, t, T)
+    for _ in range(100):
+        o.spec_step()
+    X, _, _ = g.download()
+    assert lt == 100 and abs(t - o.spec_scalars()["time"]) <= DT_RTOL * t
+    assert np.abs(X - o.X).max() < TRAJ_ATOL_M
+    g.close()
+    o.close()
+
+
+def test_skin_tuner_chooses_a_candidate(gpu_lib):
+    """A long call (at least 2000 steps) with the skin left to the context
+    (list_skin < 0: start 0.6 A) re-times the three candidates and keeps one;
+    the run goes on through the trial steps (the step count is the one asked
+    for)."""
+    p = of.params_default()
+    p.list_skin = -1.0
+    slab = of.spec_slab((8, 8, 8), 1001, 500.0, 0.0, params=p)
+    g = gpu_ctx(slab, graph=True, precision=1)
+    assert abs(g.get_option("skin") - 0.6) < 1e-9 and g.get_option("skin_tune") == 1
+    lt, t, _, _ = g.steps(2, 2400, 0, 0.0, 300.0)
+    assert lt == 2400 and t > 0
+    assert min(abs(g.get_option("skin") - s) for s in (0.45, 0.6, 0.81)) < 1e-9
+    X, _, _ = g.download()
+    assert np.isfinite(X).all()
+    g.close()
