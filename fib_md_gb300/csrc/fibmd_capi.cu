@@ -86,6 +86,12 @@ struct fibmd_ctx {
   // each chunk of kTuneSteps spec-mode steps
   int stage = kStageSmall;
   bool autotune = true;
+  // atoms per block of the binary32 force kernel (128 or 64, tuned with the
+  // force path) and of the pair-list build (64, 128 or 256, tuned with the
+  // skin); the graph is captured again when one changes
+  int force_block = 128;
+  int build_block = 128;
+  int graph_force_block = -1, graph_build_block = -1;
   // programmatic dependent launch of the step loop's kernels (option "pdl";
   // off by default: measured no faster on the graph step loop)
   bool pdl = false;
@@ -109,6 +115,7 @@ struct fibmd_ctx {
   std::vector<SkinSet> skins;
   int skin_cur = 0;
   bool skin_tune = true;
+  bool build_tune = true;   // the build's block size, tuned with the skin
   int graph_skin = -1;
   long long graph_chunks = 0;  // tuning chunks run (the skin's re-tuning cadence)
   double umax = 0.0;           // the 2-body table's extent
@@ -160,6 +167,8 @@ static Launch launch_of(const fibmd_ctx* ctx) {
   L.sms = ctx->sms;
   L.stage = ctx->stage;
   L.pdl = ctx->pdl;
+  L.force_block = ctx->force_block;
+  L.build_block = ctx->build_block;
   return L;
 }
 
@@ -1414,6 +1423,16 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->fuse = value != 0.0;
   } else if (!std::strcmp(key, "skin_tune")) {
     ctx->skin_tune = value != 0.0;
+  } else if (!std::strcmp(key, "force_block")) {
+    if (value != 64.0 && value != 128.0)
+      return fail(ctx, FIBMD_EINVAL, "force_block must be 64 or 128");
+    ctx->force_block = (int)value;
+    ctx->autotune = false;
+  } else if (!std::strcmp(key, "build_block")) {
+    if (value != 64.0 && value != 128.0 && value != 256.0)
+      return fail(ctx, FIBMD_EINVAL, "build_block must be 64, 128 or 256");
+    ctx->build_block = (int)value;
+    ctx->build_tune = false;
   } else if (!std::strcmp(key, "skin")) {
     // one of the candidate skins (Angstrom); fixes it (no more tuning)
     int k = -1;
@@ -1456,6 +1475,10 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = fuse_in_use(ctx) ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "skin_tune")) {
     *value = ctx->skin_tune ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "force_block")) {
+    *value = (double)ctx->force_block;
+  } else if (!std::strcmp(key, "build_block")) {
+    *value = (double)ctx->build_block;
   } else if (!std::strcmp(key, "skin")) {
     *value = ctx->skins[(size_t)ctx->skin_cur].skin * 1e10;
   } else if (!std::strcmp(key, "skin_candidates")) {
@@ -1666,6 +1689,8 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_pdl = ctx->pdl ? 1 : 0;
   ctx->graph_fuse = ctx->fuse ? 1 : 0;
   ctx->graph_skin = ctx->skin_cur;
+  ctx->graph_force_block = ctx->force_block;
+  ctx->graph_build_block = ctx->build_block;
   return FIBMD_OK;
 }
 
@@ -1681,9 +1706,11 @@ constexpr long long kTuneSteps = 1000;  // spec-mode steps between stage re-tuni
 // Device time (ms) of three force evaluations with the given stage, each a
 // launch of a captured graph as the step loop runs it, so that a path of
 // fewer kernels is credited with the launch gaps it saves.
-static int time_force_graph(fibmd_ctx* ctx, int stage, cudaEvent_t a, cudaEvent_t b, float* ms) {
+static int time_force_graph(fibmd_ctx* ctx, int stage, int block, cudaEvent_t a, cudaEvent_t b,
+                            float* ms) {
   Launch L = launch_of(ctx);
   L.stage = stage;
+  L.force_block = block;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   const cudaError_t e = launch_force(L, ctx->P, ctx->S, false, false, false);
@@ -1712,27 +1739,37 @@ static int tune_stage(fibmd_ctx* ctx) {
   if (ctx->P.precision != FIBMD_PREC_MIXED || !ctx->autotune || !ctx->lists_built)
     return FIBMD_OK;
   cudaEvent_t a = get_event(ctx), b = get_event(ctx);
-  const int stages[3] = {kStageSmall, kStageLarge, kStageGroup};
-  float ms[3] = {0.f, 0.f, 0.f};
+  // (force path, centres per block): one thread per centre with the small
+  // or large stage in blocks of 128 or 64, or eight lanes per centre
+  constexpr int kCand = 5;
+  const int stages[kCand] = {kStageSmall, kStageSmall, kStageLarge, kStageLarge, kStageGroup};
+  const int blocks[kCand] = {128, 64, 128, 64, 128};
+  float ms[kCand] = {};
   int rc = FIBMD_OK;
-  for (int q = 0; q < 3 && rc == FIBMD_OK; q++) rc = time_force_graph(ctx, stages[q], a, b, &ms[q]);
+  for (int q = 0; q < kCand && rc == FIBMD_OK; q++)
+    rc = time_force_graph(ctx, stages[q], blocks[q], a, b, &ms[q]);
   ctx->pool.push_back(a);
   ctx->pool.push_back(b);
   if (rc) return rc;
   // switch only for a clear gain: a switch recaptures the step graph
   int cur = 0, best = 0;
-  for (int q = 0; q < 3; q++) {
-    if (stages[q] == ctx->stage) cur = q;
+  for (int q = 0; q < kCand; q++) {
+    if (stages[q] == ctx->stage && (stages[q] == kStageGroup || blocks[q] == ctx->force_block))
+      cur = q;
     if (ms[q] < ms[best]) best = q;
   }
-  if (ms[best] < 0.97f * ms[cur]) ctx->stage = stages[best];
+  if (ms[best] < 0.97f * ms[cur]) {
+    ctx->stage = stages[best];
+    ctx->force_block = blocks[best];
+  }
   return FIBMD_OK;
 }
 
 static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
       ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
-      ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur) {
+      ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur ||
+      ctx->graph_force_block != ctx->force_block || ctx->graph_build_block != ctx->build_block) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {
       // a device or driver without programmatic edges in conditional
@@ -1794,6 +1831,37 @@ static int tune_skin(fibmd_ctx* ctx, long long* pairs_run) {
   return rc;
 }
 
+// The pair-list build's atoms per block, re-chosen on the current state:
+// two list builds timed with CUDA events for each of 64, 128 and 256 (the
+// lists are those of the current positions whichever builds them); kept
+// if 3 % faster than the one in use.
+static int tune_build(fibmd_ctx* ctx) {
+  const int cand[3] = {64, 128, 256};
+  float ms[3] = {};
+  cudaEvent_t a = get_event(ctx), b = get_event(ctx);
+  cudaError_t e = cudaSuccess;
+  for (int q = 0; q < 3 && e == cudaSuccess; q++) {
+    Launch L = launch_of(ctx);
+    L.build_block = cand[q];
+    e = launch_build_lists(L, ctx->P, ctx->S, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(a, ctx->stream);
+    for (int r = 0; r < 2 && e == cudaSuccess; r++) e = launch_build_lists(L, ctx->P, ctx->S, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(b, ctx->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms[q], a, b);
+  }
+  ctx->pool.push_back(a);
+  ctx->pool.push_back(b);
+  if (e != cudaSuccess) return fail(ctx, FIBMD_ECUDA, "build tuning: %s", cudaGetErrorString(e));
+  int cur = 1, best = 0;
+  for (int q = 0; q < 3; q++) {
+    if (cand[q] == ctx->build_block) cur = q;
+    if (ms[q] < ms[best]) best = q;
+  }
+  if (ms[best] < 0.97f * ms[cur]) ctx->build_block = cand[best];
+  return FIBMD_OK;
+}
+
 static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double* time,
                       double* temp, int* reason) {
   const Launch L = launch_of(ctx);
@@ -1825,6 +1893,10 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
         CK(cudaStreamSynchronize(ctx->stream));
         long long pr = 0;
         int rs = tune_skin(ctx, &pr);
+        if (rs == FIBMD_OK && ctx->build_tune) {
+          CK(cudaStreamSynchronize(ctx->stream));
+          rs = tune_build(ctx);
+        }
         if (rs) return rs;
         pairs -= pr;
       }

@@ -268,16 +268,18 @@ __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevSta
 // ions (an ion has a few dozen listed pairs, both orders), at least two
 inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P.nion + 1) / 2)); }
 
-template <bool ENERGY, bool COUNT, int LEGS>
-__global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevState S) {
+// BLK centres per block (128, or 64 chosen by the context's tuning); the
+// resident threads per SM are the same for both (896)
+template <bool ENERGY, bool COUNT, int LEGS, int BLK>
+__global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
   // the last mol_blocks blocks evaluate the Moliere list (a few dozen pairs
   // per ion), which saves a launch per step
-  const int nbm = (P.N + kBlock32 - 1) / kBlock32;
+  const int nbm = (P.N + BLK - 1) / BLK;
   if ((int)blockIdx.x >= nbm) {
-    moliere_entries<true, ENERGY>(P, S, ((int)blockIdx.x - nbm) * kBlock32 + threadIdx.x,
-                                  ((int)gridDim.x - nbm) * kBlock32);
+    moliere_entries<true, ENERGY>(P, S, ((int)blockIdx.x - nbm) * BLK + threadIdx.x,
+                                  ((int)gridDim.x - nbm) * BLK);
     return;
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -285,12 +287,12 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
   // of a leg; B = (1/r, g) of a leg; I = neighbour index | type << 30. Vector
   // accesses keep the shared-memory instruction count low.
   float4* sA = reinterpret_cast<float4*>(smem_raw);
-  float2* sB = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * LEGS * kBlock32);
+  float2* sB = reinterpret_cast<float2*>(smem_raw + sizeof(float4) * LEGS * BLK);
   int* sI = reinterpret_cast<int*>(smem_raw + (sizeof(float4) + sizeof(float2)) * LEGS *
-                                                  kBlock32);
+                                                  BLK);
   const int t = threadIdx.x;
 
-  const int i = blockIdx.x * kBlock32 + threadIdx.x;
+  const int i = blockIdx.x * BLK + threadIdx.x;
   if (i >= P.N) return;
   const int4 qi = S.posq[i];
   const int ti = qi.w & 0xff;
@@ -357,8 +359,8 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
       if (r2f > P.pre3mA2 || ((qq[u].w >> 8) & FL_REMOVED)) continue;
       const int tb = (qq[u].w & 0xff) - 1;
       if (r2f <= P.pre3lA2 && nc < LEGS) {
-        sA[nc * kBlock32 + t] = make_float4(dq.x, dq.y, dq.z, r2f);
-        sI[nc * kBlock32 + t] = jj[u] | (tb << 30);
+        sA[nc * BLK + t] = make_float4(dq.x, dq.y, dq.z, r2f);
+        sI[nc * BLK + t] = jj[u] | (tb << 30);
         nc++;
       } else {
         float rinv, E, g;
@@ -370,16 +372,16 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
   // compacted in place (slot nl <= c is written after slot c is read).
 #pragma unroll 2
   for (int c = 0; c < nc; c++) {
-    const float4 cd = sA[c * kBlock32 + t];
+    const float4 cd = sA[c * BLK + t];
     const float3 dq = make_float3(cd.x, cd.y, cd.z);
     const float r2f = cd.w;
-    const int idx = sI[c * kBlock32 + t];
+    const int idx = sI[c * BLK + t];
     float rinv, E, g;
     if (!pair_leg(dq, r2f, (unsigned)idx >> 30, &rinv, &E, &g)) continue;
     if (E > kLegEmin) {
-      sA[nl * kBlock32 + t] = make_float4(dq.x * rinv, dq.y * rinv, dq.z * rinv, E);
-      sB[nl * kBlock32 + t] = make_float2(rinv, g);
-      sI[nl * kBlock32 + t] = idx;
+      sA[nl * BLK + t] = make_float4(dq.x * rinv, dq.y * rinv, dq.z * rinv, E);
+      sB[nl * BLK + t] = make_float2(rinv, g);
+      sI[nl * BLK + t] = idx;
       nl++;
     }
   }
@@ -397,19 +399,19 @@ __global__ void __launch_bounds__(kBlock32, 7) k_force_mixed(DevParams P, DevSta
     const float thrd = (float)P.thrd;
     float cu = 0.f;
     for (int a = 0; a < nl; a++) {
-      const float4 la = sA[a * kBlock32 + t];
-      const float2 lb = sB[a * kBlock32 + t];
+      const float4 la = sA[a * BLK + t];
+      const float2 lb = sB[a * BLK + t];
       const float ax = la.x, ay = la.y, az = la.z, aE = la.w;
       const float ar = lb.x, ag = lb.y;
-      const int ia = sI[a * kBlock32 + t];
+      const int ia = sI[a * BLK + t];
       const int tbA = (unsigned)ia >> 30;
       float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
 #pragma unroll 2
       for (int b = 0; b < nl; b++) {
         if (b == a) continue;
-        const float4 lbb = sA[b * kBlock32 + t];
+        const float4 lbb = sA[b * BLK + t];
         const float bx = lbb.x, by = lbb.y, bz = lbb.z;
-        const int tbB = (unsigned)sI[b * kBlock32 + t] >> 30;
+        const int tbB = (unsigned)sI[b * BLK + t] >> 30;
         const float cs = ax * bx + ay * by + az * bz;
         const float c3 = cs + thrd;
         const float W = c3 * c3;
@@ -962,14 +964,14 @@ __global__ void k_force_begin(DevState S) {
   if (threadIdx.x < 4) S.sc->counters[threadIdx.x] = 0ull;
 }
 
-template <bool MIXED, bool ENERGY, bool COUNT, int LEGS>
+template <bool MIXED, bool ENERGY, bool COUNT, int LEGS, int BLK = kBlock32>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
-  constexpr int BLOCK = MIXED ? kBlock32 : kBlock64;
+  constexpr int BLOCK = MIXED ? BLK : kBlock64;
   const size_t smem = MIXED ? (sizeof(float) * LEGS * kLegF32 + sizeof(int) * LEGS) * BLOCK
                             : (sizeof(double) * kMaxLegs * kLegF64 +
                                sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
   void (*kern)(DevParams, DevState) = nullptr;
-  if constexpr (MIXED) kern = k_force_mixed<ENERGY, COUNT, LEGS>;
+  if constexpr (MIXED) kern = k_force_mixed<ENERGY, COUNT, LEGS, BLK>;
   else kern = k_force_fp64<ENERGY, COUNT>;
   // the dynamic shared-memory limit is a per-device attribute of the kernel:
   // set it once on each device that launches it
@@ -1043,12 +1045,18 @@ cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
       if (energy)
         return count ? force_impl<true, true, true, kStageLarge>(L, P, S)
                      : force_impl<true, true, false, kStageLarge>(L, P, S);
+      if (L.force_block == 64)
+        return count ? force_impl<true, false, true, kStageLarge, 64>(L, P, S)
+                     : force_impl<true, false, false, kStageLarge, 64>(L, P, S);
       return count ? force_impl<true, false, true, kStageLarge>(L, P, S)
                    : force_impl<true, false, false, kStageLarge>(L, P, S);
     }
     if (energy)
       return count ? force_impl<true, true, true, kStageSmall>(L, P, S)
                    : force_impl<true, true, false, kStageSmall>(L, P, S);
+    if (L.force_block == 64)
+      return count ? force_impl<true, false, true, kStageSmall, 64>(L, P, S)
+                   : force_impl<true, false, false, kStageSmall, 64>(L, P, S);
     return count ? force_impl<true, false, true, kStageSmall>(L, P, S)
                  : force_impl<true, false, false, kStageSmall>(L, P, S);
   }

@@ -428,6 +428,9 @@ struct Launch {
   cudaEvent_t force_b = nullptr;  // when kernel timing is on
   int stage = kStageSmall;        // binary32 force kernel: staged candidates
                                   // per centre (kStageSmall or kStageLarge)
+  int force_block = 128;          // its centres per block (64 or 128)
+  int build_block = 128;          // atoms per block of the pair-list build
+                                  // (64, 128 or 256)
 };
 
 // A kernel launch, with the programmatic stream-serialization attribute when

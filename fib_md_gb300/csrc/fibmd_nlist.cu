@@ -233,7 +233,7 @@ __device__ __forceinline__ bool exact_in(const Geo& G, const DevState& S, int i,
 // partner's with one atomic slot. A pair with an ion goes
 // to the Moliere pair list in both orders; with WIDE (spec mode) the ion
 // scan below lists those and ions are skipped here.
-constexpr int kBuildThreads = 128;
+constexpr int kBuildThreads = 128;  // the default block (atoms per block)
 constexpr int kBuildBuf = 24;  // buffered candidates per atom
 
 // Entries of atom x that found its list full: counted per atom, so that the
@@ -254,14 +254,16 @@ __device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, 
   return -1;
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(kBuildThreads, 7) k_build_atoms(DevParams P, DevState S,
+// BT atoms per block (64, 128 or 256, chosen by the context's tuning); the
+// resident threads per SM are the same for each (896)
+template <bool WIDE, int BT>
+__global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevState S,
                                                                    int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
-  __shared__ int buf[kBuildBuf][kBuildThreads];     // candidate slots, then partners
-  __shared__ float bufr[kBuildBuf][kBuildThreads];  // their binary32 r^2 (A^2)
+  __shared__ int buf[kBuildBuf][BT];     // candidate slots, then partners
+  __shared__ float bufr[kBuildBuf][BT];  // their binary32 r^2 (A^2)
   const int t = threadIdx.x;
-  const int h = blockIdx.x * kBuildThreads + t;
+  const int h = blockIdx.x * BT + t;
   if (h >= S.cell_start[P.ncell]) return;
   const int i = S.cell_atoms[h];
   const int4 qi = S.posq_cell[h];
@@ -465,11 +467,19 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
   k_scan_top<<<1, kScanBlock, 0, L.stream>>>(P, S, nscan, from_flag);
   k_scan_add<<<nscan, kScanBlock, 0, L.stream>>>(P, S, from_flag);
   k_cell_fill<<<nb_atoms, 256, 0, L.stream>>>(P, S, from_flag);
-  const int nb_build = (P.N + kBuildThreads - 1) / kBuildThreads;
-  if (P.mol_reach > 1)
-    k_build_atoms<true><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
-  else
-    k_build_atoms<false><<<nb_build, kBuildThreads, 0, L.stream>>>(P, S, from_flag);
+  const int bt = (L.build_block == 64 || L.build_block == 256) ? L.build_block : kBuildThreads;
+  const int nb_build = (P.N + bt - 1) / bt;
+  const bool wide = P.mol_reach > 1;
+  if (bt == 64) {
+    if (wide) k_build_atoms<true, 64><<<nb_build, 64, 0, L.stream>>>(P, S, from_flag);
+    else k_build_atoms<false, 64><<<nb_build, 64, 0, L.stream>>>(P, S, from_flag);
+  } else if (bt == 256) {
+    if (wide) k_build_atoms<true, 256><<<nb_build, 256, 0, L.stream>>>(P, S, from_flag);
+    else k_build_atoms<false, 256><<<nb_build, 256, 0, L.stream>>>(P, S, from_flag);
+  } else {
+    if (wide) k_build_atoms<true, 128><<<nb_build, 128, 0, L.stream>>>(P, S, from_flag);
+    else k_build_atoms<false, 128><<<nb_build, 128, 0, L.stream>>>(P, S, from_flag);
+  }
   if (P.mol_reach > 1 && P.nion > 0)
     k_build_ion_pairs<<<min(P.nion, 4096), 128, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);

@@ -288,7 +288,8 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    graph launch with device-side rebuild decisions, default 1; phase and
    kernel timers see only the steps run outside the graph), "autotune"
    (mixed precision: before every 1000 spec-mode steps of a graph run, and
-   before a dose, time the binary32 force paths on the current state and
+   before a dose, time the binary32 force paths (each stage with 128 or 64
+   centres per block, and eight lanes per centre) on the current state and
    keep the fastest, default 1) and "stage" (the binary32 force path: 8 or
    10 staged leg candidates per centre with one thread per centre, or 1 for
    eight lanes per centre, the faster on small systems; setting it turns
@@ -312,7 +313,11 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    trajectory does not depend on the skin since the lists stay complete),
    "skin" (reads the skin in use in Angstrom; set to one of the candidates
    it fixes the skin: the lists are rebuilt at the next step) and
-   "skin_candidates" (read only: how many). */
+   "skin_candidates" (read only: how many), "force_block" (centres per
+   block of the one-thread-per-centre binary32 force kernel, 128 or 64;
+   "autotune" times both with each stage; setting it turns "autotune" off)
+   and "build_block" (atoms per block of the pair-list build, 64, 128 or
+   256, re-timed with the skin; setting it fixes it). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
 /* The current value of an option ("stage" reads the force path in use,
    which "autotune" changes as the run goes). */

@@ -318,3 +318,37 @@ def test_many_leg_centres(gpu_lib, precision, stage):
             np.mean(np.sum(Fr ** 2, axis=1)))
         assert rms_rel < 2e-5, rms_rel
         assert _maxrel(F, Fr) < 1e-4
+
+
+def test_block_size_variants(gpu_lib):
+    """The tuned atoms-per-block variants compute the same thing: the
+    pair-list build in blocks of 64, 128 or 256 gives the oracle's pair
+    sets, and the binary32 force kernel in blocks of 64 or 128 gives forces
+    equal to binary32 rounding (the order of its binary64 atomics)."""
+    import fib_md_gb300 as fm
+
+    o = _slab()
+    o.si_nlist()
+    sw, mol = o.pairs(0), o.pairs(1)
+    for bb in (64, 128, 256):
+        g = _gpu(o, impact=1)
+        g.set_option("build_block", bb)
+        g.si_nlist()
+        assert np.array_equal(g.get_pairs(0), sw) and np.array_equal(g.get_pairs(1), mol), bb
+        g.close()
+    p = o.p.copy()
+    p.precision = 1
+    out = {}
+    for fb in (128, 64):
+        g = fm.FibMD(p)
+        g.set_option("stage", 8)
+        g.set_option("force_block", fb)
+        g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
+        g.set_impact(1)
+        g.si_nlist()
+        out[fb] = g.si_force()
+        assert g.get_option("force_block") == fb
+        g.close()
+    # each centre's binary32 arithmetic is the same in either block size;
+    # only the order of the binary64 atomics differs
+    assert per_atom_err(out[64], out[128]) < 1e-12
