@@ -354,3 +354,32 @@ def test_block_size_variants(gpu_lib):
     # binary32 roundings (the mixed path's own error against binary64 is
     # ~1e-6 per atom, test_mixed_precision_force_error)
     assert per_atom_err(out[64], out[128]) < 1e-6
+
+
+def test_impact_loop_exit(gpu_lib):
+    """TI's impact loop (src/timeint.f90:138-147) ends at the first step
+    whose start finds time > impact*dti: the GPU's fibmd_gpu_steps (called
+    until FIBMD_STOP_DONE, resuming after the dump stops at atm_out steps)
+    and the oracle's TI take the same number of steps, end at the same time
+    and at the same positions."""
+    import fib_md_gb300 as fm
+
+    p = of.params_default()
+    p.dti = 1.0e-15  # 50 fast-regime steps of Ts_i = 2e-17 s
+    o = _slab((4, 4, 4), ion_height_A=3.0, params=p)
+    o.set_fast(True)
+    g = _gpu(o, impact=1)
+    g.ionrun(1)
+    o.si_nlist()
+    g.si_nlist()
+    o.F[:] = o.si_force()
+    g.si_force()
+    n_o, lt_o, t_o, _ = o.TI(1, 0, 0.0, 0, 300.0, max_steps=1000)
+    lt, t, T, why, calls = 0, 0.0, 300.0, 0, 0
+    while not why & fm.STOP_DONE:
+        lt, t, T, why = g.steps(1, 1000, lt, t, T)
+        calls += 1
+        assert calls < 20
+    assert 50 <= n_o <= 51 and lt == lt_o == n_o + 1 and t == t_o
+    X, _, _ = g.download()
+    assert np.abs(X - o.X).max() < TRAJ_ATOL_M
