@@ -321,6 +321,8 @@ def bench_ours(args, rank, world, dist):
         wall = time.perf_counter() - w0
     stage_end = int(g.get_option("stage"))
     skin_end = g.get_option("skin")
+    blocks_end = {"force_block": int(g.get_option("force_block")),
+                  "build_block": int(g.get_option("build_block"))}
     X_end, _, _ = g.download()
     value, t_dev, atom_steps = replica_rate(dist, float(N) * args.md_steps * args.steps,
                                             sum(times), "cuda")
@@ -452,7 +454,8 @@ def bench_ours(args, rank, world, dist):
                                    "thread and 8 lanes per centre (1)",
                      "force_path_at_end": stage_end,
                      "list_skin": skin_text(args.list_skin),
-                     "list_skin_at_end_A": skin_end},
+                     "list_skin_at_end_A": skin_end,
+                     "atoms_per_block_at_end": blocks_end},
         "fp64": {"value": value64, "unit": "atom-steps/s", "steps": n64,
                  "window": "the same", "mixed_over_fp64": value / value64,
                  "ms_per_step": 1e3 * sum(t64) / n64,
