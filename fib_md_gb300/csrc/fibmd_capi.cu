@@ -91,7 +91,8 @@ struct fibmd_ctx {
   // skin); the graph is captured again when one changes
   int force_block = 128;
   int build_block = 128;
-  int graph_force_block = -1, graph_build_block = -1;
+  int graph_force_block = -1, graph_build_block = -1, graph_uniform = -1;
+  int uniform = 0;  // the uploaded lattice holds no Ge
   // programmatic dependent launch of the step loop's kernels (option "pdl";
   // off by default: measured no faster on the graph step loop)
   bool pdl = false;
@@ -523,6 +524,7 @@ static int derive_params(fibmd_ctx* ctx) {
   char err[256] = "";
   const int rc = derive_dev_params(p, ctx->impact, umax, last, ctx->P, ctx->geo0, err, sizeof err);
   if (rc) return fail(ctx, rc, "%s", err);
+  ctx->P.uniform = ctx->uniform;
   return FIBMD_OK;
 }
 
@@ -535,6 +537,7 @@ static int derive_skin(const fibmd_ctx* ctx, double skin, fibmd_ctx::SkinSet& ou
   Geo g0;
   int rc = derive_dev_params(q, ctx->impact, ctx->umax, ctx->tab_last, out.P, g0, err, errlen);
   if (rc) return rc;
+  out.P.uniform = ctx->uniform;
   out.skin = skin;
   if (ctx->reps.empty()) {
     out.geo.assign(1, g0);
@@ -1062,9 +1065,11 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   Launch L = launch_of(ctx);
   std::vector<int8_t> t8((size_t)N);
   std::vector<uint32_t> fl((size_t)N);
+  int uniform = 1;
   for (int i = 0; i < N; i++) {
     if (atype[i] < 1 || atype[i] > 3)
       return fail(ctx, FIBMD_EINVAL, "atype(%d) = %d is not 1, 2 or 3", i + 1, atype[i]);
+    if (atype[i] == 2) uniform = 0;
     t8[i] = (int8_t)atype[i];
     fl[i] = replica_flags(ctx, i, xsides[i] > 0 ? FL_FROZEN : 0u);
   }
@@ -1098,6 +1103,10 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
+  // a slab without Ge takes the binary32 force kernel's single-species path
+  ctx->uniform = uniform;
+  ctx->P.uniform = uniform;
+  for (auto& k : ctx->skins) k.P.uniform = uniform;
   return FIBMD_OK;
 }
 
@@ -1691,6 +1700,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_skin = ctx->skin_cur;
   ctx->graph_force_block = ctx->force_block;
   ctx->graph_build_block = ctx->build_block;
+  ctx->graph_uniform = ctx->P.uniform;
   return FIBMD_OK;
 }
 
@@ -1769,7 +1779,8 @@ static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
   if (!ctx->graph_exec || ctx->graph_frc != ctx->S.frc || ctx->graph_nfired != ctx->P.nfired ||
       ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
       ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur ||
-      ctx->graph_force_block != ctx->force_block || ctx->graph_build_block != ctx->build_block) {
+      ctx->graph_force_block != ctx->force_block || ctx->graph_build_block != ctx->build_block ||
+      ctx->graph_uniform != ctx->P.uniform) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {
       // a device or driver without programmatic edges in conditional

@@ -269,8 +269,10 @@ __device__ __forceinline__ void moliere_entries(const DevParams& P, const DevSta
 inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P.nion + 1) / 2)); }
 
 // BLK centres per block (128, or 64 chosen by the context's tuning); the
-// resident threads per SM are the same for both (896)
-template <bool ENERGY, bool COUNT, int LEGS, int BLK>
+// resident threads per SM are the same for both (896). UNI: every lattice
+// atom is Si (P.uniform), so the per-species constants are the [0] entries,
+// read directly rather than through a computed index.
+template <bool ENERGY, bool COUNT, int LEGS, int BLK, bool UNI = false>
 __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
@@ -299,7 +301,7 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
   if (ti >= 3 || ((qi.w >> 8) & FL_REMOVED)) return;
   const int n = S.n_sw[i];
   if (n == 0) return;
-  const int ta = ti - 1;
+  const int ta = UNI ? 0 : ti - 1;
   const Geo& G = S.geo[rep_of_w(qi.w)];
   const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
   const float al = (float)P.al, cut = (float)P.cut3, gm = (float)P.gam;
@@ -311,15 +313,18 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
 
   // One listed pair inside the SW cutoff: its 2-body force on the centre and
   // its leg parameters. Returns false outside the cutoff.
-  auto pair_leg = [&](const float3& dq, float r2f, int tb, float* rinv_o, float* E_o,
+  // The exponentials and the reciprocal use the hardware approximations
+  // (a few binary32 ulps, inside the binary32 path's stated error).
+  auto pair_leg = [&](const float3& dq, float r2f, int tb_in, float* rinv_o, float* E_o,
                       float* g_o) -> bool {
+    const int tb = UNI ? 0 : tb_in;
     const float rinv = rsqrtf(r2f);
     const float r = r2f * rinv;
     const float is = P.isigA[ta][tb];
     const float ue = r * is;
     if (!(ue < cut)) return false;
-    const float inv = __frcp_rn(ue - al);
-    const float ex = expf(inv);
+    const float inv = __fdividef(1.0f, ue - al);
+    const float ex = __expf(inv);
     const float iu = P.sigA[ta][tb] * rinv;  // 1/u
     const float u2 = iu * iu;
     const float u4 = u2 * u2;
@@ -332,7 +337,7 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
     if (COUNT) cnt_pairs++;
     if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
     *rinv_o = rinv;
-    *E_o = expf(gm * inv);
+    *E_o = __expf(gm * inv);
     *g_o = -gm * inv * inv * is;
     return true;
   };
@@ -415,7 +420,7 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
         const float cs = ax * bx + ay * by + az * bz;
         const float c3 = cs + thrd;
         const float W = c3 * c3;
-        const float pref = P.lepsA[ta][tbA][tbB] * aE * lbb.w;
+        const float pref = P.lepsA[ta][UNI ? 0 : tbA][UNI ? 0 : tbB] * aE * lbb.w;
         const float s2 = 2.0f * c3;
         const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
         afx += pref * (wa * ax + sa * bx);
@@ -971,19 +976,25 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
                             : (sizeof(double) * kMaxLegs * kLegF64 +
                                sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
   void (*kern)(DevParams, DevState) = nullptr;
-  if constexpr (MIXED) kern = k_force_mixed<ENERGY, COUNT, LEGS, BLK>;
-  else kern = k_force_fp64<ENERGY, COUNT>;
+  const int uni = (MIXED && !ENERGY && P.uniform) ? 1 : 0;
+  if constexpr (MIXED) {
+    if constexpr (!ENERGY) kern = uni ? k_force_mixed<ENERGY, COUNT, LEGS, BLK, true>
+                                      : k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
+    else kern = k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
+  } else {
+    kern = k_force_fp64<ENERGY, COUNT>;
+  }
   // the dynamic shared-memory limit is a per-device attribute of the kernel:
   // set it once on each device that launches it
-  static std::atomic<unsigned long long> attr_devices{0};
+  static std::atomic<unsigned long long> attr_devices[2] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   const unsigned long long bit = 1ull << (dev & 63);
-  if (!(attr_devices.load() & bit)) {
+  if (!(attr_devices[uni].load() & bit)) {
     const cudaError_t ea =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (ea != cudaSuccess) return ea;
-    attr_devices.fetch_or(bit);
+    attr_devices[uni].fetch_or(bit);
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
   kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(P, S);

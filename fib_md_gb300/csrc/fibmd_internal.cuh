@@ -72,6 +72,7 @@ __device__ __forceinline__ int posq_w(int8_t type, uint32_t fl) {
 // Derived constants handed to every kernel by value.
 struct DevParams {
   int N, Nsg, nfired;  // atoms with index >= nfired are unfired ions
+  int uniform;         // every lattice atom is Si (type 1): set at upload
   int nrep;            // replicas (1: a single system)
   int nion;            // ions (entries of DevState::ion_list)
   int mode, precision;
