@@ -69,6 +69,11 @@ def parse():
                          "list radii; positive: that start value (still tuned unless the "
                          "context's skin_tune option is 0). The oracle runs take the start "
                          "value (0.6 A for a negative one)")
+    ap.add_argument("--reactions", type=int, default=0,
+                    help="1: the mixed context's binary32 force path stores the 3-body "
+                         "reactions and gathers them per atom instead of adding them by "
+                         "binary64 atomics (the option 'reactions'; slower on GB300, for "
+                         "comparison)")
     ap.add_argument("--no-graph", action="store_true",
                     help="run the step loop launch by launch (for a profiler's launch list)")
     ap.add_argument("--ensemble-replicas", type=int, default=256)
@@ -311,6 +316,7 @@ def bench_ours(args, rank, world, dist):
     g = make_ctx(w, fm.PREC_MIXED)
     g.set_option("timers", 0)
     g.set_option("graph", 0 if args.no_graph else 1)
+    g.set_option("reactions", args.reactions)
     stream = torch.cuda.ExternalStream(g.stream_ptr)
     run_windows(g, w, torch, stream, args.warmup, args.md_steps, flush)
     barrier()
@@ -451,8 +457,10 @@ def bench_ours(args, rank, world, dist):
         "config": workload_config(args, cells, N),
         "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
         "autotune": {"force_path": "before every 1000 steps among 8 or 10 staged legs per "
-                                   "thread and 8 lanes per centre (1)",
+                                   "thread (in blocks of 128 or 64) and 8 lanes per centre (1)",
                      "force_path_at_end": stage_end,
+                     "force_reactions": "stored and gathered per atom" if args.reactions
+                                        else "binary64 atomics",
                      "list_skin": skin_text(args.list_skin),
                      "list_skin_at_end_A": skin_end,
                      "atoms_per_block_at_end": blocks_end},
@@ -1181,6 +1189,8 @@ def main():
 
         w = make_workload(cells, list_skin_A=args.list_skin)
         g = make_ctx(w, fm.PREC_FP64 if args.profile == "fp64" else fm.PREC_MIXED)
+        if args.reactions and args.profile != "fp64":
+            g.set_option("reactions", 1)
         if args.profile == "step":
             # the window's first min(md_steps, 300) mixed spec-mode steps
             # launch by launch (every kernel of the step loop)

@@ -93,6 +93,12 @@ struct fibmd_ctx {
   int build_block = 128;
   int graph_force_block = -1, graph_build_block = -1, graph_uniform = -1;
   int uniform = 0;  // the uploaded lattice holds no Ge
+  bool react = false;  // binary32 path: stored reactions instead of atomics
+  int graph_react = -1;
+  // step graph: the many-leg kernel in an IF node that the force kernel
+  // opens (off: the node's evaluation costs more than the empty launch)
+  bool heavy_if = false;
+  int graph_heavy_if = -1;
   // programmatic dependent launch of the step loop's kernels (option "pdl";
   // off by default: measured no faster on the graph step loop)
   bool pdl = false;
@@ -170,6 +176,7 @@ static Launch launch_of(const fibmd_ctx* ctx) {
   L.pdl = ctx->pdl;
   L.force_block = ctx->force_block;
   L.build_block = ctx->build_block;
+  L.react = ctx->react;
   return L;
 }
 
@@ -817,6 +824,12 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   AL(S.atom_cell, N);
   AL(S.scan_blocks, (size_t)nscan + 1);
   AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
+  if (ctx->P.precision == FIBMD_PREC_MIXED && ctx->P.max_sw <= kReactMaxList) {
+    AL(S.rev_sw, (size_t)ctx->P.max_sw * N);
+    AL(S.legpos, N);
+    AL(S.react, (size_t)kStageLarge * N);
+    AL(S.fown, N);
+  }
   AL(S.n_sw, N);
   AL(S.sw_extra, N);
   AL(S.mol_pairs, (size_t)ctx->P.mol_cap);
@@ -1432,6 +1445,13 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->fuse = value != 0.0;
   } else if (!std::strcmp(key, "skin_tune")) {
     ctx->skin_tune = value != 0.0;
+  } else if (!std::strcmp(key, "heavy_if")) {
+    ctx->heavy_if = value != 0.0;
+  } else if (!std::strcmp(key, "reactions")) {
+    if (value != 0.0 && !ctx->S.react)
+      return fail(ctx, FIBMD_EINVAL,
+                  "stored reactions need mixed precision and max_sw_nbrs <= %d", kReactMaxList);
+    ctx->react = value != 0.0;
   } else if (!std::strcmp(key, "force_block")) {
     if (value != 64.0 && value != 128.0)
       return fail(ctx, FIBMD_EINVAL, "force_block must be 64 or 128");
@@ -1484,6 +1504,10 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = fuse_in_use(ctx) ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "skin_tune")) {
     *value = ctx->skin_tune ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "heavy_if")) {
+    *value = ctx->heavy_if ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "reactions")) {
+    *value = ctx->react ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "force_block")) {
     *value = (double)ctx->force_block;
   } else if (!std::strcmp(key, "build_block")) {
@@ -1601,9 +1625,9 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     cudaError_t e_ = (call);                                \
     if (e_ != cudaSuccess) return abort_capture(e_, what);  \
   } while (0)
-  // an IF node on the capture's current dependencies, its body the list
-  // rebuild (captured on the second stream), made the new dependency
-  auto add_rebuild_if = [&](cudaGraphConditionalHandle hi) -> cudaError_t {
+  // an IF node on the capture's current dependencies, its body what body()
+  // launches on the second stream (L2), made the new dependency
+  auto add_if = [&](cudaGraphConditionalHandle hi, auto body) -> cudaError_t {
     cudaStreamCaptureStatus st;
     cudaGraph_t cg = nullptr;
     const cudaGraphNode_t* deps = nullptr;
@@ -1625,11 +1649,24 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     e = cudaStreamBeginCaptureToGraph(ctx->cap2, ib, nullptr, nullptr, 0,
                                       cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
-    const cudaError_t eb = launch_build_lists(L2, P, Sx, 0);
+    const cudaError_t eb = body();
     cudaGraph_t tmp = nullptr;
     const cudaError_t ee = cudaStreamEndCapture(ctx->cap2, &tmp);
     return eb != cudaSuccess ? eb : ee;
   };
+  auto add_rebuild_if = [&](cudaGraphConditionalHandle hi) -> cudaError_t {
+    return add_if(hi, [&] { return launch_build_lists(L2, P, Sx, 0); });
+  };
+  // With the option "heavy_if", the many-leg kernel of each step sits in an
+  // IF node: the force kernel opens it when a centre has more legs than its
+  // stage (a cascade core), the kernel before the force closes it, so steps
+  // without such centres skip the launch. The eight-lanes-per-centre path
+  // has no such centres. Off by default: on the 256k cascade the step took
+  // 101.3 us with the nodes against 91.8 us with a plain launch every step.
+  const bool heavy_if =
+      ctx->heavy_if && !(P.precision == FIBMD_PREC_MIXED && ctx->stage == kStageGroup);
+  Launch L2h = L2;
+  L2h.pdl = false;
   cudaGraphNodeParams wp = {};
   wp.type = cudaGraphNodeTypeConditional;
   wp.conditional.handle = hw;
@@ -1658,6 +1695,11 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CK(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp));
   }
   cudaGraph_t body = wp.conditional.phGraph_out[0];
+  // (a handle that no IF node uses fails the instantiation)
+  cudaGraphConditionalHandle hh[2] = {0, 0};
+  if (heavy_if)
+    for (int half = 0; half < 2; half++)
+      CK(cudaGraphConditionalHandleCreate(&hh[half], body, 0, cudaGraphCondAssignDefault));
   CK(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
                                    cudaStreamCaptureModeThreadLocal));
   for (int half = 0; half < 2; half++) {
@@ -1666,19 +1708,30 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     CKC(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, nullptr, nullptr, nullptr), "info");
     cudaGraphConditionalHandle hi;
     CKC(cudaGraphConditionalHandleCreate(&hi, cg, 0, cudaGraphCondAssignDefault), "handle");
+    Launch Lf = L;
+    Lf.heavy_if = heavy_if;
+    Lf.heavy_handle = hh[half];
+    auto force = [&]() -> cudaError_t {
+      cudaError_t e = launch_force(Lf, P, Sx, false, false, true);
+      if (e == cudaSuccess && heavy_if)
+        e = add_if(hh[half], [&] { return launch_force_heavy(L2h, P, Sx); });
+      return e;
+    };
     if (fused) {
-      CKC(launch_force(L, P, Sx, false, false, true), "force");
+      CKC(force(), "force");
       CKC(launch_spec_kd(L, P, Sx, Ttar, ctx->d_loop, hi, hw, half == 1,
-                         ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks),
+                         ctx->kd_grid > 0 ? ctx->kd_grid : ctx->kd_blocks,
+                         heavy_if ? &hh[1 - half] : nullptr),
           "kick-drift");
       CKC(add_rebuild_if(hi), "rebuild");
     } else {
       // the drift's last block sets the rebuild condition; the second
       // step's drift follows the first step's kick as its programmatic
       // dependent
-      CKC(launch_spec_drift(L, P, Sx, Ttar, &hi, half == 1), "drift");
+      CKC(launch_spec_drift(L, P, Sx, Ttar, &hi, half == 1, heavy_if ? &hh[half] : nullptr),
+          "drift");
       CKC(add_rebuild_if(hi), "rebuild");
-      CKC(launch_force(L, P, Sx, false, false, true), "force");
+      CKC(force(), "force");
       CKC(launch_spec_kick(L, P, Sx, Ttar, 1), "kick");
     }
     std::swap(Sx.frc, Sx.frc_new);
@@ -1701,6 +1754,8 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_force_block = ctx->force_block;
   ctx->graph_build_block = ctx->build_block;
   ctx->graph_uniform = ctx->P.uniform;
+  ctx->graph_react = ctx->react ? 1 : 0;
+  ctx->graph_heavy_if = ctx->heavy_if ? 1 : 0;
   return FIBMD_OK;
 }
 
@@ -1716,11 +1771,12 @@ constexpr long long kTuneSteps = 1000;  // spec-mode steps between stage re-tuni
 // Device time (ms) of three force evaluations with the given stage, each a
 // launch of a captured graph as the step loop runs it, so that a path of
 // fewer kernels is credited with the launch gaps it saves.
-static int time_force_graph(fibmd_ctx* ctx, int stage, int block, cudaEvent_t a, cudaEvent_t b,
-                            float* ms) {
+static int time_force_graph(fibmd_ctx* ctx, int stage, int block, bool react, cudaEvent_t a,
+                            cudaEvent_t b, float* ms) {
   Launch L = launch_of(ctx);
   L.stage = stage;
   L.force_block = block;
+  L.react = react;
   cudaGraph_t g = nullptr;
   CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
   const cudaError_t e = launch_force(L, ctx->P, ctx->S, false, false, false);
@@ -1751,13 +1807,16 @@ static int tune_stage(fibmd_ctx* ctx) {
   cudaEvent_t a = get_event(ctx), b = get_event(ctx);
   // (force path, centres per block): one thread per centre with the small
   // or large stage in blocks of 128 or 64, or eight lanes per centre
+  // (the stored-reaction form is not a candidate: its gather pass runs its
+  // binary64 sums on the SM's FP64 pipe, where the atomics have the L2 do
+  // them, and costs several times the atomics it saves)
   constexpr int kCand = 5;
   const int stages[kCand] = {kStageSmall, kStageSmall, kStageLarge, kStageLarge, kStageGroup};
   const int blocks[kCand] = {128, 64, 128, 64, 128};
   float ms[kCand] = {};
   int rc = FIBMD_OK;
   for (int q = 0; q < kCand && rc == FIBMD_OK; q++)
-    rc = time_force_graph(ctx, stages[q], blocks[q], a, b, &ms[q]);
+    rc = time_force_graph(ctx, stages[q], blocks[q], ctx->react, a, b, &ms[q]);
   ctx->pool.push_back(a);
   ctx->pool.push_back(b);
   if (rc) return rc;
@@ -1780,7 +1839,8 @@ static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
       ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
       ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur ||
       ctx->graph_force_block != ctx->force_block || ctx->graph_build_block != ctx->build_block ||
-      ctx->graph_uniform != ctx->P.uniform) {
+      ctx->graph_uniform != ctx->P.uniform || ctx->graph_react != (ctx->react ? 1 : 0) ||
+      ctx->graph_heavy_if != (ctx->heavy_if ? 1 : 0)) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {
       // a device or driver without programmatic edges in conditional

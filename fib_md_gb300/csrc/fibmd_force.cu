@@ -79,8 +79,13 @@ struct LegSmem {
   __device__ __forceinline__ int& idx(int l) { return j[l * BLOCK + threadIdx.x]; }
 };
 
+// set_hh: the step graph runs the many-leg kernel in an IF node whose
+// condition hh a centre that goes to it sets (the node stays closed in the
+// many steps without such centres).
 template <bool ENERGY, bool COUNT>
-__global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S) {
+__global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S,
+                                                         cudaGraphConditionalHandle hh,
+                                                         int set_hh) {
   pdl_wait();
   pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -183,6 +188,7 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
     // the warp-per-centre kernel evaluates this centre's angle terms
     const int slot = atomicAdd(&S.sc->heavy_count, 1);
     S.heavy_list[slot] = i;
+    if (set_hh) cudaGraphSetConditional(hh, 1u);
   } else {
     const double thrd = P.thrd;
     double cfx = 0, cfy = 0, cfz = 0, cu = 0;
@@ -271,9 +277,13 @@ inline int mol_blocks(const DevParams& P) { return std::max(2, std::min(1024, (P
 // BLK centres per block (128, or 64 chosen by the context's tuning); the
 // resident threads per SM are the same for both (896). UNI: every lattice
 // atom is Si (P.uniform), so the per-species constants are the [0] entries,
-// read directly rather than through a computed index.
-template <bool ENERGY, bool COUNT, int LEGS, int BLK, bool UNI = false>
-__global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, DevState S) {
+// read directly rather than through a computed index. REACT: the reactions
+// on the legs and the centre's own force are stored (S.react, S.fown,
+// S.legpos) for k_force_gather instead of added by binary64 atomics.
+template <bool ENERGY, bool COUNT, int LEGS, int BLK, bool UNI = false, bool REACT = false>
+__global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, DevState S,
+                                                                cudaGraphConditionalHandle hh,
+                                                                int set_hh) {
   pdl_wait();
   pdl_trigger();
   // the last mol_blocks blocks evaluate the Moliere list (a few dozen pairs
@@ -298,9 +308,14 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
   if (i >= P.N) return;
   const int4 qi = S.posq[i];
   const int ti = qi.w & 0xff;
-  if (ti >= 3 || ((qi.w >> 8) & FL_REMOVED)) return;
   const int n = S.n_sw[i];
-  if (n == 0) return;
+  if (ti >= 3 || ((qi.w >> 8) & FL_REMOVED) || n == 0) {
+    if (REACT) {
+      S.legpos[i] = 0ull;
+      S.fown[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
   const int ta = UNI ? 0 : ti - 1;
   const Geo& G = S.geo[rep_of_w(qi.w)];
   const float qinvA[3] = {G.qinvA[0], G.qinvA[1], G.qinvA[2]};
@@ -365,7 +380,8 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
       const int tb = (qq[u].w & 0xff) - 1;
       if (r2f <= P.pre3lA2 && nc < LEGS) {
         sA[nc * BLK + t] = make_float4(dq.x, dq.y, dq.z, r2f);
-        sI[nc * BLK + t] = jj[u] | (tb << 30);
+        // the partner, or with stored reactions its list position
+        sI[nc * BLK + t] = (REACT ? k0 + u : jj[u]) | (tb << 30);
         nc++;
       } else {
         float rinv, E, g;
@@ -397,9 +413,12 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
   // binary64 atomic costs one conversion
   const float convf = (float)P.f_evA_to_N;
   double ue_J = 0.0;
+  unsigned long long lpos = 0ull;  // legpos of the centre (REACT)
   if (nl > kMaxLegs) {
     const int slot = atomicAdd(&S.sc->heavy_count, 1);
     S.heavy_list[slot] = i;
+    if (set_hh) cudaGraphSetConditional(hh, 1u);
+    lpos = kLegsHeavy << 60;
   } else {
     const float thrd = (float)P.thrd;
     float cu = 0.f;
@@ -429,8 +448,13 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
         if (ENERGY) ae += pref * W;
         if (COUNT && b > a && pref != 0.f) cnt_ang++;
       }
-      atomic_add3(S.frc_new, ia & 0x3fffffff, (double)(convf * afx), (double)(convf * afy),
-                  (double)(convf * afz));
+      if (REACT) {
+        S.react[(size_t)a * P.N + i] = make_float4(afx, afy, afz, 0.f);
+        lpos |= (unsigned long long)(ia & 63) << (6 * a);
+      } else {
+        atomic_add3(S.frc_new, ia & 0x3fffffff, (double)(convf * afx), (double)(convf * afy),
+                    (double)(convf * afz));
+      }
       fx -= afx;
       fy -= afy;
       fz -= afz;
@@ -441,8 +465,14 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
       }
     }
     if (ENERGY) ue_J = P.e_eV_to_J * (double)cu / 6.0;
+    lpos |= (unsigned long long)nl << 60;
   }
-  atomic_add3(S.frc_new, i, (double)(convf * fx), (double)(convf * fy), (double)(convf * fz));
+  if (REACT) {
+    S.legpos[i] = lpos;
+    S.fown[i] = make_float4(fx, fy, fz, 0.f);
+  } else {
+    atomic_add3(S.frc_new, i, (double)(convf * fx), (double)(convf * fy), (double)(convf * fz));
+  }
   if (ENERGY) {
     const double e = P.e_eV_to_J * (double)ui + ue_J;
     if (e != 0.0) atomicAdd(&S.epot[i], e);
@@ -510,9 +540,8 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
 }
 
 // Centres with more than kMaxLegs active legs (compressed cascade regions,
-// damaged slabs): a group of lanes per centre, 8 in binary32 (four centres
-// per warp) and the whole warp in binary64 (whose leg stage is twice the
-// size). The group first computes every listed leg and stages the active
+// damaged slabs): a group of lanes per centre, 8 or 32 in binary32 and the
+// whole warp in binary64 (k_force_heavy chooses). The group first computes every listed leg and stages the active
 // ones in shared memory, then takes legs as rows: a lane sums its leg's
 // reaction over every other leg in registers and scatters it once. Each
 // angle term is evaluated in both of its rows, which costs less than
@@ -523,22 +552,16 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
 constexpr int kHeavyWarps = 4;
 constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
-template <bool MIXED, bool ENERGY>
-__global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
-  pdl_wait();
-  pdl_trigger();
-  // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
-  using R = typename std::conditional<MIXED, float, double>::type;
-  constexpr int GROUP = MIXED ? 8 : 32;  // lanes per centre
-  constexpr int GPW = 32 / GROUP;        // centres per warp
-  constexpr int NG = kHeavyWarps * GPW;  // centres per block
-  __shared__ R sl[NG][6][kHeavyLegs];
-  __shared__ int sj[NG][kHeavyLegs];
-  __shared__ int snl[NG];
+// One pass over the many-leg centres with GROUP lanes per centre (stages in
+// sl/sj/snl: kHeavyWarps * 32 / GROUP of them).
+template <bool MIXED, bool ENERGY, int GROUP, typename R>
+__device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState& S, int cnt,
+                                              R (*sl)[6][kHeavyLegs], int (*sj)[kHeavyLegs],
+                                              int* snl) {
+  constexpr int GPW = 32 / GROUP;  // centres per warp
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int gl = lane % GROUP;               // lane within the group
-  const int sg = w * GPW + lane / GROUP;     // the group's stage
-  const int cnt = *((volatile int*)&S.sc->heavy_count);
+  const int gl = lane % GROUP;            // lane within the group
+  const int sg = w * GPW + lane / GROUP;  // the group's stage
   const double conv = MIXED ? P.f_evA_to_N : 1.0;
   const double econv = MIXED ? P.e_eV_to_J : 1.0;
   // warp-uniform loop: every lane takes part in the group reductions
@@ -660,6 +683,32 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
     }
     __syncwarp();
   }
+}
+
+// Binary32: eight lanes per centre (four centres per warp) where the centres
+// outnumber the grid's warps (damaged slabs, cascade cores of a batch), the
+// whole warp per centre where they fit in one pass (a few cascade-core
+// centres: the pass is then as long as one centre's chain, which the wider
+// group shortens). Binary64: the whole warp (its leg stage is twice the size).
+template <bool MIXED, bool ENERGY>
+__global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
+  // binary32 legs in mixed mode (Angstrom, eV), binary64 otherwise
+  using R = typename std::conditional<MIXED, float, double>::type;
+  constexpr int NG = kHeavyWarps * (MIXED ? 4 : 1);  // stages: centres per block at most
+  __shared__ R sl[NG][6][kHeavyLegs];
+  __shared__ int sj[NG][kHeavyLegs];
+  __shared__ int snl[NG];
+  const int cnt = *((volatile int*)&S.sc->heavy_count);
+  if (cnt == 0) return;
+  if constexpr (MIXED) {
+    if (cnt > (int)gridDim.x * kHeavyWarps) {
+      heavy_centres<MIXED, ENERGY, 8>(P, S, cnt, sl, sj, snl);
+      return;
+    }
+  }
+  heavy_centres<MIXED, ENERGY, 32>(P, S, cnt, sl, sj, snl);
 }
 
 // Binary32 force with eight lanes per centre for every centre (four centres
@@ -961,6 +1010,55 @@ __global__ void k_force_moliere(DevParams P, DevState S) {
                                  gridDim.x * blockDim.x);
 }
 
+// The second pass of the stored-reaction form: atom m adds its own centre
+// force and, for each SW partner j of which it is a leg, the reaction that
+// j's centre stored for it, each converted to N and summed in binary64 into
+// the force buffer (which holds the Moliere and many-leg atomics). A centre
+// of the many-leg kernel looks through its whole list, since its legs are
+// not recorded; a partner of the many-leg kernel added its reactions itself.
+// Being a leg is symmetric (the same binary32 distance both ways), so every
+// stored reaction is gathered exactly once.
+__global__ void __launch_bounds__(256) k_force_gather(DevParams P, DevState S) {
+  pdl_wait();
+  pdl_trigger();
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= P.N) return;
+  const unsigned long long lp = S.legpos[m];
+  const int cnt = (int)(lp >> 60);
+  const float4 fo = S.fown[m];
+  if (cnt == 0 && fo.x == 0.f && fo.y == 0.f && fo.z == 0.f) return;
+  const float convf = (float)P.f_evA_to_N;
+  const size_t N = (size_t)P.N;
+  double fx = (double)(convf * fo.x), fy = (double)(convf * fo.y), fz = (double)(convf * fo.z);
+  auto gather = [&](int k) {
+    const int j = S.nbr_sw[(size_t)k * N + m];
+    const int r = S.rev_sw[(size_t)k * N + m];
+    if (r < 0) return;
+    const unsigned long long lj = S.legpos[j];
+    const int cj = (int)(lj >> 60);
+    if (cj > kStageLarge) return;
+    for (int b = 0; b < cj; b++) {
+      if ((int)((lj >> (6 * b)) & 63ull) == r) {
+        const float4 R = S.react[(size_t)b * N + j];
+        fx += (double)(convf * R.x);
+        fy += (double)(convf * R.y);
+        fz += (double)(convf * R.z);
+        return;
+      }
+    }
+  };
+  if (cnt == (int)kLegsHeavy) {
+    const int n = min(S.n_sw[m], P.max_sw);
+    for (int k = 0; k < n; k++) gather(k);
+  } else {
+    for (int a = 0; a < cnt; a++) gather((int)((lp >> (6 * a)) & 63ull));
+  }
+  double4_32a& F = S.frc_new[m];
+  F.x += fx;
+  F.y += fy;
+  F.z += fz;
+}
+
 __global__ void k_force_begin(DevState S) {
   if (threadIdx.x == 0) {
     S.sc->heavy_count = 0;
@@ -969,35 +1067,56 @@ __global__ void k_force_begin(DevState S) {
   if (threadIdx.x < 4) S.sc->counters[threadIdx.x] = 0ull;
 }
 
+// A group of lanes per many-leg centre; the count is known only on the
+// device, so the grid covers thousands of centres (cascade cores of a batch)
+// in one round and idle warps return at once.
+template <bool MIXED, bool ENERGY>
+static cudaError_t heavy_impl(const Launch& L, const DevParams& P, const DevState& S, bool pdl) {
+  const int side = L.sms > 0 ? L.sms : 152;
+  const int heavy_blocks =
+      std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
+  return launch_k(k_force_heavy<MIXED, ENERGY>, heavy_blocks, 32 * kHeavyWarps, 0, L.stream, pdl,
+                  P, S);
+}
+
 template <bool MIXED, bool ENERGY, bool COUNT, int LEGS, int BLK = kBlock32>
 static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevState& S) {
   constexpr int BLOCK = MIXED ? BLK : kBlock64;
   const size_t smem = MIXED ? (sizeof(float) * LEGS * kLegF32 + sizeof(int) * LEGS) * BLOCK
                             : (sizeof(double) * kMaxLegs * kLegF64 +
                                sizeof(int) * (kMaxLegs + kCandF64)) * BLOCK;
-  void (*kern)(DevParams, DevState) = nullptr;
+  void (*kern)(DevParams, DevState, cudaGraphConditionalHandle, int) = nullptr;
   const int uni = (MIXED && !ENERGY && P.uniform) ? 1 : 0;
+  // stored reactions: only where the context allocated their buffers
+  const int react = (MIXED && !ENERGY && L.react && S.react) ? 1 : 0;
   if constexpr (MIXED) {
-    if constexpr (!ENERGY) kern = uni ? k_force_mixed<ENERGY, COUNT, LEGS, BLK, true>
-                                      : k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
-    else kern = k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
+    if constexpr (!ENERGY) {
+      if (react) kern = uni ? k_force_mixed<ENERGY, COUNT, LEGS, BLK, true, true>
+                            : k_force_mixed<ENERGY, COUNT, LEGS, BLK, false, true>;
+      else kern = uni ? k_force_mixed<ENERGY, COUNT, LEGS, BLK, true>
+                      : k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
+    } else {
+      kern = k_force_mixed<ENERGY, COUNT, LEGS, BLK, false>;
+    }
   } else {
     kern = k_force_fp64<ENERGY, COUNT>;
   }
   // the dynamic shared-memory limit is a per-device attribute of the kernel:
   // set it once on each device that launches it
-  static std::atomic<unsigned long long> attr_devices[2] = {};
+  static std::atomic<unsigned long long> attr_devices[4] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   const unsigned long long bit = 1ull << (dev & 63);
-  if (!(attr_devices[uni].load() & bit)) {
+  const int variant = uni + 2 * react;
+  if (!(attr_devices[variant].load() & bit)) {
     const cudaError_t ea =
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (ea != cudaSuccess) return ea;
-    attr_devices[uni].fetch_or(bit);
+    attr_devices[variant].fetch_or(bit);
   }
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
-  kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(P, S);
+  kern<<<(P.N + BLOCK - 1) / BLOCK + (MIXED ? mol_blocks(P) : 0), BLOCK, smem, L.stream>>>(
+      P, S, L.heavy_handle, L.heavy_if ? 1 : 0);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   const int side = L.sms > 0 ? L.sms : 152;
   // the kernels after the main one are programmatic dependents (L.pdl)
@@ -1005,13 +1124,10 @@ static cudaError_t force_impl(const Launch& L, const DevParams& P, const DevStat
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && !MIXED)
     e = launch_k(k_force_moliere<MIXED, ENERGY>, side, 128, 0, L.stream, pdl, P, S);
-  // a group of lanes per many-leg centre; the count is known only on the
-  // device, so the grid covers thousands of centres (cascade cores of a
-  // batch) in one round and idle warps return at once
-  const int heavy_blocks = std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
-  if (e == cudaSuccess)
-    e = launch_k(k_force_heavy<MIXED, ENERGY>, heavy_blocks, 32 * kHeavyWarps, 0, L.stream, pdl,
-                 P, S);
+  // the many-leg centres (the step graph adds this launch in an IF node)
+  if (e == cudaSuccess && !L.heavy_if) e = heavy_impl<MIXED, ENERGY>(L, P, S, pdl);
+  if (e == cudaSuccess && react)
+    e = launch_k(k_force_gather, (P.N + 255) / 256, 256, 0, L.stream, pdl, P, S);
   if (e == cudaSuccess && P.mode == FIBMD_MODE_REF)
     e = launch_k(k_force_stale<ENERGY>, side, 64, 0, L.stream, pdl, P, S);
   return e;
@@ -1032,6 +1148,11 @@ static cudaError_t group_impl(const Launch& L, const DevParams& P, const DevStat
     e = launch_k(k_force_stale<ENERGY>, side, 64, 0, L.stream, L.pdl && !L.force_b, P, S);
   }
   return e;
+}
+
+cudaError_t launch_force_heavy(const Launch& L, const DevParams& P, const DevState& S) {
+  if (P.precision == FIBMD_PREC_MIXED) return heavy_impl<true, false>(L, P, S, L.pdl);
+  return heavy_impl<false, false>(L, P, S, L.pdl);
 }
 
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S, bool energy,

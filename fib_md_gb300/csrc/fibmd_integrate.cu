@@ -394,7 +394,8 @@ __device__ __forceinline__ bool spec_drift_chunk(const DevParams& P, const DevSt
         atomicAdd(at < 3 ? &R->removed_count : &R->ions_removed, 1);
       }
       S.pos[i] = x;
-      S.vel[i] = v;
+      // the velocity changes here only by the thermostat, pinning or removal
+      if ((fl & (FL_THERMO | FL_FROZEN)) || removed) S.vel[i] = v;
       const int4 q = make_int4((int)(unsigned)k[0], (int)(unsigned)k[1], (int)(unsigned)k[2],
                                posq_w(at, fl));
       S.posq[i] = q;
@@ -425,22 +426,29 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevSta
 // Sets the graph's rebuild condition from the drift's flag. A kernel of its
 // own rather than a last-block ticket in the drift: a same-address atomic
 // from each of ~1000 blocks serialises in L2 for longer than a launch.
-__global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond) {
+// With has_heavy, it also closes the step's many-leg IF node (heavy), which
+// the force kernel opens when it finds such a centre.
+__global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond,
+                            cudaGraphConditionalHandle heavy, int has_heavy) {
   pdl_wait();
   pdl_trigger();
-  if (threadIdx.x == 0)
+  if (threadIdx.x == 0) {
     cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
+    if (has_heavy) cudaGraphSetConditional(heavy, 0u);
+  }
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
                               double Ttar, const cudaGraphConditionalHandle* cond,
-                              bool pdl_first) {
+                              bool pdl_first, const cudaGraphConditionalHandle* heavy) {
   (void)Ttar;
   const int nb = (P.N + kKickThreads - 1) / kKickThreads;
   cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, kKickThreads, 0,
                            L.stream, L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
-  if (e == cudaSuccess && cond) e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond);
+  if (e == cudaSuccess && cond)
+    e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond,
+                 heavy ? *heavy : cudaGraphConditionalHandle(0), heavy ? 1 : 0);
   return e;
 }
 
@@ -669,9 +677,12 @@ constexpr long long kKdSpinLimit = 1ll << 22;  // ~0.5 s with the back-off below
 
 __device__ __forceinline__ void kd_release(const DevState& S, LoopCtl* loop,
                                            cudaGraphConditionalHandle hif,
-                                           cudaGraphConditionalHandle hwhile, int last_of_pair) {
+                                           cudaGraphConditionalHandle hwhile, int last_of_pair,
+                                           cudaGraphConditionalHandle hheavy, int has_heavy) {
   DevScalars* sc = S.sc;
   reset_force_counters(S);
+  // the next step's many-leg IF node: closed until its force opens it
+  if (has_heavy) cudaGraphSetConditional(hheavy, 0u);
   int cont = 1;
   if (last_of_pair) {
     const long long r = loop->pairs - 1;
@@ -691,7 +702,9 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
                                                            LoopCtl* loop,
                                                            cudaGraphConditionalHandle hif,
                                                            cudaGraphConditionalHandle hwhile,
-                                                           int last_of_pair) {
+                                                           int last_of_pair,
+                                                           cudaGraphConditionalHandle hheavy,
+                                                           int has_heavy) {
   const int nchunk = (P.N + kKickThreads - 1) / kKickThreads;
   DevScalars* sc = S.sc;
   __shared__ unsigned gen0;
@@ -711,7 +724,7 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
       }
       if (release) {
         __threadfence();
-        kd_release(S, loop, hif, hwhile, last_of_pair);
+        kd_release(S, loop, hif, hwhile, last_of_pair, hheavy, has_heavy);
       }
     }
   }
@@ -757,14 +770,19 @@ int spec_kd_resident_blocks(int nrep, int sms) {
 
 cudaError_t launch_spec_kd(const Launch& L, const DevParams& P, const DevState& S, double Ttar,
                            LoopCtl* loop, cudaGraphConditionalHandle hif,
-                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks) {
+                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks,
+                           const cudaGraphConditionalHandle* heavy) {
   const int nchunk = (P.N + kKickThreads - 1) / kKickThreads;
   if (nchunk > kMaxRedBlocks || max_blocks < 1) return cudaErrorInvalidConfiguration;
   const int nb = min(nchunk, max_blocks);
+  const cudaGraphConditionalHandle hh = heavy ? *heavy : cudaGraphConditionalHandle(0);
+  const int has = heavy ? 1 : 0;
   if (P.nrep > 1)
-    k_spec_kd<1><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair);
+    k_spec_kd<1><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair,
+                                                    hh, has);
   else
-    k_spec_kd<0><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair);
+    k_spec_kd<0><<<nb, kKickThreads, 0, L.stream>>>(P, S, Ttar, loop, hif, hwhile, last_of_pair,
+                                                    hh, has);
   return cudaGetLastError();
 }
 

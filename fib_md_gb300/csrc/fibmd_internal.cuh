@@ -203,6 +203,17 @@ struct DevState {
   int* n_sw;
   int* sw_extra;     // per atom: SW partners beyond the max_sw slots (overflow)
   int2* mol_pairs;
+  // binary32 path with stored reactions (allocated for mixed precision with
+  // at most kReactMaxList list slots): rev_sw holds, per list entry (i, k),
+  // the slot of i in the partner's list; legpos[i] the list positions of the
+  // centre's staged legs (6 bits each, leg count in bits 60-63, kLegsHeavy
+  // for a centre of the many-leg kernel); react[a * N + i] the 3-body
+  // reaction the centre exerts on its leg a (eV/A); fown[i] the centre's own
+  // force from its terms (eV/A)
+  int* rev_sw;
+  unsigned long long* legpos;
+  float4* react;
+  float4* fown;
   // stale-list and heavy-centre work lists
   uint8_t* fast_flag;
   int* fast_list;
@@ -419,6 +430,8 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
 constexpr int kStageSmall = 8;
 constexpr int kStageLarge = 10;
 constexpr int kStageGroup = 1;
+constexpr int kReactMaxList = 64;  // list slots addressable by legpos's 6-bit fields
+constexpr unsigned long long kLegsHeavy = 15;  // legpos count code of a many-leg centre
 
 struct Launch {
   cudaStream_t stream;
@@ -432,6 +445,14 @@ struct Launch {
   int force_block = 128;          // its centres per block (64 or 128)
   int build_block = 128;          // atoms per block of the pair-list build
                                   // (64, 128 or 256)
+  bool react = false;             // binary32 path: reactions stored per leg
+                                  // and gathered per atom (no force atomics
+                                  // from the centres of the main kernel)
+  bool heavy_if = false;          // launch_force leaves out the many-leg
+                                  // kernel (the caller adds it in an IF node
+                                  // whose condition heavy_handle the main
+                                  // kernel sets when it finds such a centre)
+  cudaGraphConditionalHandle heavy_handle = 0;
 };
 
 // A kernel launch, with the programmatic stream-serialization attribute when
@@ -463,6 +484,8 @@ cudaError_t launch_count_triplets(const Launch& L, const DevParams& P, const Dev
 // counters and the kick has zeroed the accumulation buffer
 cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
                          bool energy, bool count, bool spec_step = false);
+// the many-leg kernel alone (forces, no energy), for the step graph's IF node
+cudaError_t launch_force_heavy(const Launch& L, const DevParams& P, const DevState& S);
 // fibmd_integrate.cu
 cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S,
                                double Ts, double Tau, double Ttar);
@@ -481,17 +504,21 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // cond (in a captured graph): the IF handle the rebuild hangs on
 // pdl_first: the drift may itself be launched as a programmatic dependent of
 // the kernel before it (a kick); the condition kernel always is (L.pdl)
+// heavy (with cond): the IF handle of the step's many-leg kernel, closed here
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
                               double Ttar, const cudaGraphConditionalHandle* cond = nullptr,
-                              bool pdl_first = false);
+                              bool pdl_first = false,
+                              const cudaGraphConditionalHandle* heavy = nullptr);
 cudaError_t launch_spec_kick(const Launch& L, const DevParams& P, const DevState& S,
                              double Ttar, int apply);
 // the kick of a step fused with the drift of the next (a grid of at most
 // max_blocks resident blocks); in a graph, hif is the following rebuild IF
-// node's handle and, when last_of_pair, hwhile the step loop's WHILE node
+// node's handle and, when last_of_pair, hwhile the step loop's WHILE node;
+// heavy: the IF handle of the next step's many-leg kernel, closed here
 cudaError_t launch_spec_kd(const Launch& L, const DevParams& P, const DevState& S, double Ttar,
                            LoopCtl* loop, cudaGraphConditionalHandle hif,
-                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks);
+                           cudaGraphConditionalHandle hwhile, int last_of_pair, int max_blocks,
+                           const cudaGraphConditionalHandle* heavy = nullptr);
 int spec_kd_resident_blocks(int nrep, int sms);
 // fibmd_graph.cu: device-side conditions of the CUDA-graph step loop
 cudaError_t launch_loop_ctl(cudaStream_t s, LoopCtl* loop, const DevScalars* sc,

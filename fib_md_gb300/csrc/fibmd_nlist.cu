@@ -320,6 +320,10 @@ __global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevSt
           if (si >= 0) S.nbr_sw[(size_t)si * stride + i] = j;
           const int sj = list_slot(P, S, j);
           if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
+          if (S.rev_sw) {
+            if (si >= 0) S.rev_sw[(size_t)si * stride + i] = sj;
+            if (sj >= 0) S.rev_sw[(size_t)sj * stride + j] = si;
+          }
         } else {
           buf[na][t] = j;
           na++;
@@ -392,6 +396,11 @@ __global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevSt
       if (k < keep) S.nbr_sw[(size_t)(base + k) * stride + i] = j;
       const int sj = list_slot(P, S, j);
       if (sj >= 0) S.nbr_sw[(size_t)sj * stride + j] = i;
+      // each entry's slot in the partner's list (-1 where a list overflowed)
+      if (S.rev_sw) {
+        if (k < keep) S.rev_sw[(size_t)(base + k) * stride + i] = sj;
+        if (sj >= 0) S.rev_sw[(size_t)sj * stride + j] = k < keep ? base + k : -1;
+      }
     }
   }
   S.posq_build[i] = (WIDE && ti == 3) ? S.posq[i] : qi;

@@ -317,7 +317,16 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    block of the one-thread-per-centre binary32 force kernel, 128 or 64;
    "autotune" times both with each stage; setting it turns "autotune" off)
    and "build_block" (atoms per block of the pair-list build, 64, 128 or
-   256, re-timed with the skin; setting it fixes it). */
+   256, re-timed with the skin; setting it fixes it), "reactions" (mixed
+   precision with max_sw_nbrs <= 64 only; default 0: each centre of the
+   one-thread-per-centre kernel adds its force and the 3-body reactions on
+   its legs by binary64 atomics; 1: it stores them and a second pass
+   gathers them per atom, summing in binary64 on the SM, which on this part
+   is slower than the atomics; FIBMD_EINVAL where the context holds no
+   buffers for it) and "heavy_if" (default 0; 1: the step graph runs the
+   many-leg kernel in an IF node that the force kernel opens when it finds
+   a centre with more legs than its stage, which skips the launch in steps
+   without such centres but costs more per step than the launch it saves). */
 int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value);
 /* The current value of an option ("stage" reads the force path in use,
    which "autotune" changes as the run goes). */

@@ -66,6 +66,45 @@ def test_graph_loop_matches_plain_steps(gpu_lib, precision):
     assert ca[4] == cb[4] and ca[4] > 1  # same number of skin-triggered rebuilds
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_many_leg_centres(gpu_lib, precision):
+    """A compressed knot (the 12 second neighbours of an interior atom pulled
+    25 % inwards: 16 legs on its centre, more than either path's stage) that
+    flies apart over the run: the CUDA-graph loop with the option heavy_if
+    (its many-leg kernel in an IF node that the force kernel opens) runs the
+    same steps as the launch-by-launch loop, which launches that kernel
+    every step. In
+    binary64 to 1e-8 A after 60 steps; in binary32, whose binary64 atomic
+    sums of a knot's wide range of terms round in the order they arrive
+    (which the knot's chaos amplifies), to 1e-6 A after 20 steps, where a
+    step without the knot's 3-body forces would be off by ~1e-3 A."""
+    s, X, V = _spec_system(nc=(6, 6, 4), ion_eV=0.0, precision=precision)
+    X[-1] = X[-1] + np.array([0.0, 0.0, 30e-10])  # keep the ion away
+    nsg = s.params.Nsg
+    mid = 0.5 * (X[:nsg].max(axis=0) + X[:nsg].min(axis=0))
+    c = int(np.argmin(np.linalg.norm(X[:nsg] - mid, axis=1)))
+    d = np.linalg.norm(X[:nsg] - X[c], axis=1)
+    shell = np.argsort(d)[5:17]
+    X[shell] = X[c] + 0.75 * (X[shell] - X[c])
+    a = _ctx(s, X, V, precision, graph=True)
+    b = _ctx(s, X, V, precision, graph=False)
+    for g in (a, b):
+        g.set_option("autotune", 0)
+    a.set_option("heavy_if", 1)
+    assert a.get_option("heavy_if") == 1
+    assert a.work_counters()[5] >= 1  # many-leg centres at the start
+    n, tol_x, tol_t = (60, 1e-18, 1e-12) if precision == 0 else (20, 1e-16, 1e-9)
+    la, ta, _, _ = a.steps(2, n, 0, 0.0, 300.0)
+    lb, tb, _, _ = b.steps(2, n, 0, 0.0, 300.0)
+    Xa, _, _ = a.download()
+    Xb, _, _ = b.download()
+    assert la == lb == n
+    assert abs(ta - tb) <= tol_t * tb
+    assert np.abs(Xa - Xb).max() < tol_x
+    a.close()
+    b.close()
+
+
 def _energy(g):
     X, V, F = g.download()
     _, u, U = g.si_force_energy()
@@ -73,13 +112,17 @@ def _energy(g):
     return U + 0.5 * np.sum(mass[:, None] * V * V)
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_nve_energy_conservation(gpu_lib, precision):
+@pytest.mark.parametrize("precision,reactions", [(0, 0), (1, 0), (1, 1)])
+def test_nve_energy_conservation(gpu_lib, precision, reactions):
     """No thermostat, no fixed layers, no ion impact: the velocity-Verlet
-    total energy is conserved to a small fraction of the thermal energy."""
+    total energy is conserved to a small fraction of the thermal energy (in
+    binary32 also with the stored-reaction form of the force, where a
+    reaction gathered twice or not at all would break it)."""
     s, X, V = _spec_system(nc=(6, 6, 4), ion_eV=0.0, precision=precision)
     X[-1] = X[-1] + np.array([0.0, 0.0, 30e-10])  # keep the ion away
     g = _ctx(s, X, V, precision)
+    if precision:
+        g.set_option("reactions", reactions)
     g._mass = s.mass
     E0 = _energy(g)
     lt, t, _, _ = g.steps(2, 2000, 0, 0.0, 300.0)

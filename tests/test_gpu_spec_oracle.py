@@ -216,3 +216,46 @@ def test_skin_tuner_chooses_a_candidate(gpu_lib):
     X, _, _ = g.download()
     assert np.isfinite(X).all()
     g.close()
+
+
+def test_stored_reactions_match_atomics(gpu_lib):
+    """The binary32 path's atomic-free form (option "reactions": each centre
+    stores the 3-body reactions on its legs and its own force, and a second
+    pass gathers them per atom in binary64) against the binary64-atomic form
+    and the oracle. The 256k slab with thermal noise, the ion in contact and
+    a compressed knot (the 12 second neighbours of an interior atom pulled
+    20 % inwards) whose centres go to the many-leg kernel: per atom within
+    1e-6 of the atomic form (the same binary32 terms from another
+    instantiation, binary64 sums in another order), the oracle's RMS bar."""
+    p = of.params_default()
+    p.list_skin = 0.6e-10
+    slab = of.spec_slab((40, 40, 20), 2001, 5000.0, 7.0, params=p)
+    nsg = slab["params"].Nsg
+    rs = np.random.default_rng(23)
+    X = slab["X"]
+    X[:nsg] += rs.normal(scale=0.08e-10, size=(nsg, 3))
+    mid = 0.5 * (X[:nsg].max(axis=0) + X[:nsg].min(axis=0))
+    c = int(np.argmin(np.linalg.norm(X[:nsg] - mid, axis=1)))
+    d = np.linalg.norm(X[:nsg] - X[c], axis=1)
+    shell = np.argsort(d)[5:17]
+    X[shell] = X[c] + 0.8 * (X[shell] - X[c])
+    top = int(np.argmax(X[:nsg, 2]))
+    X[nsg] = X[top] + np.array([0.3e-10, 0.2e-10, 1.6e-10])
+    o = of.spec_oracle(slab)
+    Fr = o.F.copy()
+    F = {}
+    for react in (0, 1):
+        g = gpu_ctx(slab, precision=1)
+        g.set_option("stage", 8)
+        g.set_option("force_block", 128)
+        g.set_option("reactions", react)
+        assert g.get_option("reactions") == react
+        F[react] = g.si_force()
+        if react:
+            assert g.work_counters()[5] >= 1  # many-leg centres took part
+        g.close()
+    o.close()
+    assert per_atom_err(F[1], F[0]) < 1e-6
+    rms = np.sqrt(np.mean(np.sum(Fr * Fr, axis=1)))
+    d = np.linalg.norm(F[1] - Fr, axis=1)
+    assert np.sqrt(np.mean(d * d)) / rms < 2e-5
