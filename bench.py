@@ -102,6 +102,9 @@ def parse():
                          "graphs and 20 launch by launch (ensemble), or run the dose slab's "
                          "first impact 300 steps as graphs and 20 launch by launch on the "
                          "8-lanes-per-centre force path (dose), exit (for ncu)")
+    ap.add_argument("--profile-graph-steps", type=int, default=-1,
+                    help="CUDA-graph steps before the launch-by-launch segment of the "
+                         "ensemble and dose profiles (default 1000 and 300)")
     return ap.parse_args()
 
 
@@ -1154,7 +1157,8 @@ def main():
         b.set_tags(b.pad([s.tags for s in slabs], fill=0, dtype=np.uint32))
         b.si_nlist()
         b.si_force()
-        lt, t, _, _ = b.steps(2, 1000, 0, 0.0, 300.0)
+        ng = args.profile_graph_steps if args.profile_graph_steps >= 0 else 1000
+        lt, t, _, _ = b.steps(2, ng, 0, 0.0, 300.0)
         b.set_option("graph", 0)
         b.steps(2, 20, lt, t, 300.0)
         b.close()
@@ -1178,7 +1182,8 @@ def main():
         g.si_force()
         g.set_option("stage", 1)
         g.set_atom(int(d.ion_atoms[0]), d.X0[0], d.V0[0])
-        lt, t, _, _ = g.steps(2, 300, 0, 0.0, 300.0)
+        ng = args.profile_graph_steps if args.profile_graph_steps >= 0 else 300
+        lt, t, _, _ = g.steps(2, ng, 0, 0.0, 300.0)
         g.set_option("graph", 0)
         g.steps(2, 20, lt, t, 300.0)
         g.close()

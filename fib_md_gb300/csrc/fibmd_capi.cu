@@ -201,9 +201,13 @@ static int set_skin(fibmd_ctx* ctx, int k) {
   ctx->geo = set.geo;
   ctx->S.geo = set.d_geo;
   ctx->skin_cur = k;
+  // every replica's lists, for the new radius and grid
   const int one = 1;
-  const cudaError_t e = cudaMemcpyAsync(&ctx->S.sc->need_rebuild, &one, sizeof(int),
-                                        cudaMemcpyHostToDevice, ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(&ctx->S.sc->need_rebuild, &one, sizeof(int),
+                                  cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(&ctx->S.sc->rebuild_all, &one, sizeof(int), cudaMemcpyHostToDevice,
+                        ctx->stream);
   if (e == cudaSuccess) cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) {
     ctx->err = std::string("set_skin: ") + cudaGetErrorString(e);
@@ -824,12 +828,6 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   AL(S.atom_cell, N);
   AL(S.scan_blocks, (size_t)nscan + 1);
   AL(S.nbr_sw, (size_t)ctx->P.max_sw * N);
-  if (ctx->P.precision == FIBMD_PREC_MIXED && ctx->P.max_sw <= kReactMaxList) {
-    AL(S.rev_sw, (size_t)ctx->P.max_sw * N);
-    AL(S.legpos, N);
-    AL(S.react, (size_t)kStageLarge * N);
-    AL(S.fown, N);
-  }
   AL(S.n_sw, N);
   AL(S.sw_extra, N);
   AL(S.mol_pairs, (size_t)ctx->P.mol_cap);
@@ -1448,9 +1446,31 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
   } else if (!std::strcmp(key, "heavy_if")) {
     ctx->heavy_if = value != 0.0;
   } else if (!std::strcmp(key, "reactions")) {
-    if (value != 0.0 && !ctx->S.react)
-      return fail(ctx, FIBMD_EINVAL,
-                  "stored reactions need mixed precision and max_sw_nbrs <= %d", kReactMaxList);
+    if (value != 0.0 && !ctx->S.react) {
+      if (ctx->P.precision != FIBMD_PREC_MIXED || ctx->P.max_sw > kReactMaxList)
+        return fail(ctx, FIBMD_EINVAL, "stored reactions need mixed precision and "
+                    "max_sw_nbrs <= %d", kReactMaxList);
+      // the buffers on first use, and the lists rebuilt with each entry's
+      // slot in the partner's list
+      const size_t N = (size_t)ctx->P.N;
+      DevState& S = ctx->S;
+      int rc = dalloc(ctx, &S.rev_sw, (size_t)ctx->P.max_sw * N);
+      if (!rc) rc = dalloc(ctx, &S.legpos, N);
+      if (!rc) rc = dalloc(ctx, &S.react, (size_t)kStageLarge * N);
+      if (!rc) rc = dalloc(ctx, &S.fown, N);
+      if (rc) {
+        S.rev_sw = nullptr;
+        S.legpos = nullptr;
+        S.react = nullptr;
+        S.fown = nullptr;
+        return rc;
+      }
+      if (ctx->lists_built) {
+        CK(launch_build_lists(launch_of(ctx), ctx->P, S, 0));
+        CK(cudaStreamSynchronize(ctx->stream));
+      }
+      drop_graph(ctx);
+    }
     ctx->react = value != 0.0;
   } else if (!std::strcmp(key, "force_block")) {
     if (value != 64.0 && value != 128.0)
@@ -1655,7 +1675,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
     return eb != cudaSuccess ? eb : ee;
   };
   auto add_rebuild_if = [&](cudaGraphConditionalHandle hi) -> cudaError_t {
-    return add_if(hi, [&] { return launch_build_lists(L2, P, Sx, 0); });
+    return add_if(hi, [&] { return launch_build_lists(L2, P, Sx, 2); });
   };
   // With the option "heavy_if", the many-leg kernel of each step sits in an
   // IF node: the force kernel opens it when a centre has more legs than its
@@ -1993,7 +2013,7 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
     }
     {
       PhaseTimer t(ctx, PH_NT);
-      CK(launch_build_lists(L, P, ctx->S, 1));
+      CK(launch_build_lists(L, P, ctx->S, 2));
     }
     {
       PhaseTimer t(ctx, PH_F);

@@ -602,8 +602,8 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
             const float is = P.isigA[tc - 1][tj - 1];
             const float ue = r2 * rinv * is;
             if (!(ue < (float)P.cut3)) continue;
-            const float ia = __frcp_rn(ue - (float)P.al);
-            const float E = expf((float)P.gam * ia);
+            const float ia = __fdividef(1.0f, ue - (float)P.al);
+            const float E = __expf((float)P.gam * ia);
             if (!(E > kLegEmin)) continue;
             const int q = atomicAdd(&snl[sg], 1);
             sl[sg][0][q] = dq.x * rinv;
@@ -658,7 +658,13 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
         if (ENERGY) ae += pref * W;
       }
       const int j = ja & 0x3fffffff;
-      atomic_add3(S.frc_new, j, conv * (double)afx, conv * (double)afy, conv * (double)afz);
+      if constexpr (MIXED) {
+        // eV/A -> N in binary32 (as in the one-thread kernel): one conversion
+        const float cf = (float)conv;
+        atomic_add3(S.frc_new, j, (double)(cf * afx), (double)(cf * afy), (double)(cf * afz));
+      } else {
+        atomic_add3(S.frc_new, j, conv * (double)afx, conv * (double)afy, conv * (double)afz);
+      }
       if (ENERGY && ae != (R)0) atomicAdd(&S.epot[j], econv * (double)ae / 3.0);
       fcx -= afx;
       fcy -= afy;
@@ -668,17 +674,26 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
     // the centre's third of each term, counted in both rows
     if (ENERGY) uc /= (R)6;
     __syncwarp();
-    double dcx = conv * (double)fcx, dcy = conv * (double)fcy, dcz = conv * (double)fcz;
-    double duc = ENERGY ? econv * (double)uc : 0.0;
+    // the centre's force summed over the group in R (binary32 in mixed
+    // mode, as the lanes' shares are), converted once
 #pragma unroll
     for (int o = GROUP / 2; o > 0; o >>= 1) {
-      dcx += __shfl_xor_sync(0xffffffffu, dcx, o);
-      dcy += __shfl_xor_sync(0xffffffffu, dcy, o);
-      dcz += __shfl_xor_sync(0xffffffffu, dcz, o);
-      if (ENERGY) duc += __shfl_xor_sync(0xffffffffu, duc, o);
+      fcx += __shfl_xor_sync(0xffffffffu, fcx, o);
+      fcy += __shfl_xor_sync(0xffffffffu, fcy, o);
+      fcz += __shfl_xor_sync(0xffffffffu, fcz, o);
+    }
+    double duc = ENERGY ? econv * (double)uc : 0.0;
+    if (ENERGY) {
+#pragma unroll
+      for (int o = GROUP / 2; o > 0; o >>= 1) duc += __shfl_xor_sync(0xffffffffu, duc, o);
     }
     if (gl == 0 && c >= 0) {
-      atomic_add3(S.frc_new, c, dcx, dcy, dcz);
+      if constexpr (MIXED) {
+        const float cf = (float)conv;
+        atomic_add3(S.frc_new, c, (double)(cf * fcx), (double)(cf * fcy), (double)(cf * fcz));
+      } else {
+        atomic_add3(S.frc_new, c, conv * (double)fcx, conv * (double)fcy, conv * (double)fcz);
+      }
       if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
     }
     __syncwarp();
@@ -781,8 +796,8 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
         const float is = P.isigA[ta][tb];
         const float ue = r2f * rinv * is;
         if (!(ue < cut)) continue;
-        const float inv = __frcp_rn(ue - al);
-        const float ex = expf(inv);
+        const float inv = __fdividef(1.0f, ue - al);
+        const float ex = __expf(inv);
         const float iu = P.sigA[ta][tb] * rinv;  // 1/u
         const float u2 = iu * iu;
         const float u4 = u2 * u2;
@@ -794,7 +809,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
         fz += cf * dq.z;
         if (COUNT) cnt_pairs++;
         if (ENERGY) ui += 0.5f * P.epsA[ta][tb] * Ac * (Bc * u4 - 1.0f) * ex;
-        const float E = expf(gm * inv);
+        const float E = __expf(gm * inv);
         if (!(E > kLegEmin)) continue;
         const int q = atomicAdd(&snl[sg], 1);
         sl[sg][0][q] = dq.x * rinv;
@@ -842,20 +857,25 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
     fz -= afz;
     if (ENERGY) uc += ae;
   }
-  // the centre's force over the group: binary64 sums of the lanes' shares
-  double dcx = (double)(conv * fx), dcy = (double)(conv * fy), dcz = (double)(conv * fz);
+  // the centre's force over the group: the lanes' binary32 shares summed in
+  // binary32 (as the one-thread kernel sums a centre's terms), then one
+  // binary64 atomic per component; binary64 lane sums would put ~100 FP64
+  // instructions per centre on the SM's thin FP64 pipe
+#pragma unroll
+  for (int o = GROUP / 2; o > 0; o >>= 1) {
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
   // the centre's half of each pair, and a third of each angle term (counted
   // in both of its rows)
   double duc = ENERGY ? P.e_eV_to_J * ((double)ui + (double)uc / 6.0) : 0.0;
+  if (ENERGY) {
 #pragma unroll
-  for (int o = GROUP / 2; o > 0; o >>= 1) {
-    dcx += __shfl_xor_sync(0xffffffffu, dcx, o);
-    dcy += __shfl_xor_sync(0xffffffffu, dcy, o);
-    dcz += __shfl_xor_sync(0xffffffffu, dcz, o);
-    if (ENERGY) duc += __shfl_xor_sync(0xffffffffu, duc, o);
+    for (int o = GROUP / 2; o > 0; o >>= 1) duc += __shfl_xor_sync(0xffffffffu, duc, o);
   }
   if (gl == 0 && n > 0) {
-    atomic_add3(S.frc_new, c, dcx, dcy, dcz);
+    atomic_add3(S.frc_new, c, (double)(conv * fx), (double)(conv * fy), (double)(conv * fz));
     if (ENERGY && duc != 0.0) atomicAdd(&S.epot[c], duc);
   }
   if (COUNT) {

@@ -333,9 +333,9 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // chunk c, one per thread. Returns, in every thread, whether an atom of the
 // chunk moved half the skin since the last list build.
 template <int BATCH>
-__device__ __forceinline__ bool spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
+__device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
   const int i = c * kKickThreads + threadIdx.x;
-  bool trig = false;
+  bool trig = false, soon = false;
   if (i < P.N) {
     uint32_t fl = S.flags[i];
     double4_32a x = S.pos[i];
@@ -400,10 +400,16 @@ __device__ __forceinline__ bool spec_drift_chunk(const DevParams& P, const DevSt
                                posq_w(at, fl));
       S.posq[i] = q;
       const float3 d = qsep(q, qb, G.qinvA);
-      if (!removed && d.x * d.x + d.y * d.y + d.z * d.z >= P.disp_fastA2) trig = true;
+      const float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
+      if (!removed && d2 >= P.disp_fastA2) trig = true;
+      // a batch also rebuilds, with a replica that must, those that have
+      // moved a quarter of the skin: rebuilds stay few and in step
+      if (BATCH && !removed && d2 >= 0.25f * P.disp_fastA2) soon = true;
     }
   }
-  return __syncthreads_or(trig);
+  const int any = __syncthreads_or(trig) ? 1 : 0;
+  if (!BATCH) return any;
+  return any | (__syncthreads_or(soon) ? 2 : 0);
 }
 
 // the force counters of the coming step (the previous step's force is done)
@@ -417,9 +423,15 @@ template <int BATCH>
 __global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
-  const bool any = spec_drift_chunk<BATCH>(P, S, blockIdx.x);
+  const int moved = spec_drift_chunk<BATCH>(P, S, blockIdx.x);
   if (threadIdx.x != 0) return;
-  if (any) S.sc->need_rebuild = 1;
+  if (moved & 1) S.sc->need_rebuild = 1;
+  // a batch rebuilds the replicas that moved (chunks never straddle two)
+  if (BATCH && moved) {
+    DevScalars& R = S.sc[rep_of_flags(S.flags[blockIdx.x * kKickThreads])];
+    if (moved & 1) R.rep_rebuild = 1;
+    if (moved & 2) R.rep_soon = 1;
+  }
   if (blockIdx.x == 0) reset_force_counters(S);
 }
 
@@ -750,10 +762,17 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
   Sn.frc = S.frc_new;
   Sn.frc_new = S.frc;
   for (int c = blockIdx.x; c < nchunk; c += gridDim.x) {
-    const bool any = spec_drift_chunk<BATCH>(P, Sn, c);
-    if (threadIdx.x == 0 && any) {
-      sc->need_rebuild = 1;
-      cudaGraphSetConditional(hif, 1u);
+    const int moved = spec_drift_chunk<BATCH>(P, Sn, c);
+    if (threadIdx.x == 0 && moved) {
+      if (BATCH) {
+        DevScalars& R = S.sc[rep_of_flags(S.flags[c * kKickThreads])];
+        if (moved & 1) R.rep_rebuild = 1;
+        if (moved & 2) R.rep_soon = 1;
+      }
+      if (moved & 1) {
+        sc->need_rebuild = 1;
+        cudaGraphSetConditional(hif, 1u);
+      }
     }
   }
 }
@@ -802,6 +821,7 @@ __global__ void k_inject(DevParams P, DevState S, const Impact* table, int k) {
   const int4 q = store_posq(S.geo[rep_of_flags(fl)], S, i, m.x[0], m.x[1], m.x[2], fl);
   S.posq_build[i] = q;
   S.sc->need_rebuild = 1;
+  S.sc->rebuild_all = 1;
   (void)P;
 }
 

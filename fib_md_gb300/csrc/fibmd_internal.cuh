@@ -153,6 +153,10 @@ struct DevScalars {
   int cell_oob;
   int nan_flag;
   int need_rebuild;
+  int rep_rebuild;     // spec batch: an atom of this replica moved half the skin
+  int rep_soon;        //             ... a quarter of the skin
+  int rebuild_all;     // spec batch: the next rebuild covers every replica
+                       // (a skin switch, an injection)
   int removed_count;   // spec: lattice atoms removed (sputtered)
   int ions_removed;    //       ions removed (backscattered)
   unsigned kd_gen;     // fused kick-drift: barrier generation
@@ -475,6 +479,10 @@ inline cudaError_t launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_
 
 // fibmd_nlist.cu
 cudaError_t launch_update_posq(const Launch& L, const DevParams& P, const DevState& S);
+// rebuild_from_flag: 0 builds every list; 1 only if need_rebuild is set;
+// 2 as 1, and in a spec-mode batch only the replicas whose atoms moved half
+// the skin (rep_rebuild) unless rebuild_all is set: the others keep their
+// SW lists (the Moliere list and the cells are rebuilt for all)
 cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevState& S,
                                int rebuild_from_flag);
 cudaError_t launch_count_triplets(const Launch& L, const DevParams& P, const DevState& S,

@@ -39,6 +39,15 @@ __device__ __forceinline__ bool rebuild_skipped(const DevState& S, int from_flag
   return from_flag && !((volatile DevScalars*)S.sc)->need_rebuild;
 }
 
+// Whether replica r's SW lists are rebuilt (from_flag 2: per replica, those
+// that moved half the skin and, with them, those that moved a quarter).
+__device__ __forceinline__ bool rep_rebuilt(const DevParams& P, const DevState& S, int from_flag,
+                                            int r) {
+  if (from_flag != 2 || P.nrep <= 1 || ((volatile DevScalars*)S.sc)->rebuild_all) return true;
+  const volatile DevScalars* R = S.sc + r;
+  return R->rep_rebuild || R->rep_soon;
+}
+
 __global__ void k_build_begin(DevParams P, DevState S, int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -71,12 +80,19 @@ __global__ void k_cell_assign(DevParams P, DevState S, int from_flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= P.N) return;
   const int4 q = S.posq[i];
-  S.n_sw[i] = 0;  // the list build appends with atomics
-  S.sw_extra[i] = 0;
+  // every atom is binned (the ion pairs and the rebuilt replicas' stencils
+  // read the cells); only a rebuilt replica's lists restart
+  const bool act = rep_rebuilt(P, S, from_flag, rep_of_w(q.w));
+  if (act) {
+    S.n_sw[i] = 0;  // the list build appends with atomics
+    S.sw_extra[i] = 0;
+  }
   if ((q.w >> 8) & FL_REMOVED) {
     S.atom_cell[i] = -1;
-    S.posq_build[i] = q;
-    S.fast_flag[i] = 0;
+    if (act) {
+      S.posq_build[i] = q;
+      S.fast_flag[i] = 0;
+    }
     return;
   }
   const Geo& G = S.geo[rep_of_w(q.w)];
@@ -254,12 +270,68 @@ __device__ __forceinline__ int list_slot(const DevParams& P, const DevState& S, 
   return -1;
 }
 
+// Spec mode: every pair with an ion inside the Moliere list radius (the
+// radius exceeds the cell width, which the reference's 27-cell stencil does
+// not cover). kIonSplit blocks share out each ion's (2R+1)^3 stencil cells,
+// R = mol_reach; q is this block's index among nq such blocks. The ion
+// stores an ion-atom pair in both orders; an ion-ion pair is stored once by
+// each of its two ions.
+constexpr int kIonSplit = 8;
+__device__ __forceinline__ void ion_pairs(const DevParams& P, const DevState& S, int q, int nq) {
+  for (int u = q; u < P.nion * kIonSplit; u += nq) {
+    const int k = u / kIonSplit, part = u % kIonSplit;
+    const int i = S.ion_list[k];
+    const int4 qi = S.posq[i];
+    const int ci0 = S.atom_cell[i];
+    if ((qi.w & 0xff) != 3 || ci0 < 0) continue;
+    const Geo& G = S.geo[rep_of_w(qi.w)];
+    const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
+    const int R = G.mol_reach, W = 2 * R + 1;
+    const int ci = ci0 - G.cell_off;
+    const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
+    for (int s = part * blockDim.x + threadIdx.x; s < W * W * W; s += kIonSplit * blockDim.x) {
+      const int ox = s % W, oy = (s / W) % W, oz = s / (W * W);
+      int x = cx + ox - R, y = cy + oy - R, z = cz + oz - R;
+      // a stencil wider than a periodic axis would visit a cell twice
+      if (G.wrap[0]) { if (ox >= nx) continue; x = ((x % nx) + nx) % nx; }
+      else if (x < 0 || x >= nx) continue;
+      if (G.wrap[1]) { if (oy >= ny) continue; y = ((y % ny) + ny) % ny; }
+      else if (y < 0 || y >= ny) continue;
+      if (G.wrap[2]) { if (oz >= nz) continue; z = ((z % nz) + nz) % nz; }
+      else if (z < 0 || z >= nz) continue;
+      const int c = G.cell_off + x + nx * (y + ny * z);
+      const int b = S.cell_start[c], e = S.cell_start[c + 1];
+      for (int p = b; p < e; p++) {
+        const int j = S.cell_atoms[p];
+        if (j == i) continue;
+        const int4 qj = S.posq[j];  // posq_cell holds ions shifted
+        const float3 d = qsep(qi, qj, G.qinvA);
+        const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
+        if (r2f > P.pre_mol2A) continue;
+        if (r2f >= P.acc_mol2A && !exact_in(G, S, i, j, P.rv2lj)) continue;
+        const bool ion_j = (qj.w & 0xff) == 3;
+        const int nw = ion_j ? 1 : 2;
+        const int slot = atomicAdd(&S.sc->mol_count, nw);
+        if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
+        if (!ion_j && slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
+      }
+    }
+  }
+}
+
 // BT atoms per block (64, 128 or 256, chosen by the context's tuning); the
 // resident threads per SM are the same for each (896)
 template <bool WIDE, int BT>
 __global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevState S,
                                                                    int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
+  // spec mode: the blocks after the atoms' build the ion-pair (Moliere)
+  // list at the same time
+  const int nb_atoms = (P.N + BT - 1) / BT;
+  if (WIDE && (int)blockIdx.x >= nb_atoms) {
+    ion_pairs(P, S, (int)blockIdx.x - nb_atoms, (int)gridDim.x - nb_atoms);
+    return;
+  }
   __shared__ int buf[kBuildBuf][BT];     // candidate slots, then partners
   __shared__ float bufr[kBuildBuf][BT];  // their binary32 r^2 (A^2)
   const int t = threadIdx.x;
@@ -267,6 +339,8 @@ __global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevSt
   if (h >= S.cell_start[P.ncell]) return;
   const int i = S.cell_atoms[h];
   const int4 qi = S.posq_cell[h];
+  // a replica that keeps its lists keeps its build positions too
+  if (!rep_rebuilt(P, S, from_flag, rep_of_w(qi.w))) return;
   const int ti = qi.w & 0xff;
   const size_t stride = (size_t)P.N;
   int n = 0;  // buffered candidates, then accepted SW partners
@@ -407,59 +481,19 @@ __global__ void __launch_bounds__(BT, 896 / BT) k_build_atoms(DevParams P, DevSt
   S.fast_flag[i] = 0;
 }
 
-// Spec mode: every pair with an ion inside the Moliere list radius. One
-// block per ion; its threads share out the cells within mol_reach (the
-// radius exceeds the cell width, which the reference's 27-cell stencil
-// does not cover). The ion stores an ion-atom pair in both orders; an
-// ion-ion pair is stored once by each of its two ions.
-__global__ void __launch_bounds__(128) k_build_ion_pairs(DevParams P, DevState S,
-                                                         int from_flag) {
-  if (rebuild_skipped(S, from_flag)) return;
-  for (int k = blockIdx.x; k < P.nion; k += gridDim.x) {
-    const int i = S.ion_list[k];
-    const int4 qi = S.posq[i];
-    const int ci0 = S.atom_cell[i];
-    if ((qi.w & 0xff) != 3 || ci0 < 0) continue;
-    const Geo& G = S.geo[rep_of_w(qi.w)];
-    const int nx = G.nc[0], ny = G.nc[1], nz = G.nc[2];
-    const int R = G.mol_reach, W = 2 * R + 1;
-    const int ci = ci0 - G.cell_off;
-    const int cx = ci % nx, cy = (ci / nx) % ny, cz = ci / (nx * ny);
-    for (int s = threadIdx.x; s < W * W * W; s += blockDim.x) {
-      const int ox = s % W, oy = (s / W) % W, oz = s / (W * W);
-      int x = cx + ox - R, y = cy + oy - R, z = cz + oz - R;
-      // a stencil wider than a periodic axis would visit a cell twice
-      if (G.wrap[0]) { if (ox >= nx) continue; x = ((x % nx) + nx) % nx; }
-      else if (x < 0 || x >= nx) continue;
-      if (G.wrap[1]) { if (oy >= ny) continue; y = ((y % ny) + ny) % ny; }
-      else if (y < 0 || y >= ny) continue;
-      if (G.wrap[2]) { if (oz >= nz) continue; z = ((z % nz) + nz) % nz; }
-      else if (z < 0 || z >= nz) continue;
-      const int c = G.cell_off + x + nx * (y + ny * z);
-      const int b = S.cell_start[c], e = S.cell_start[c + 1];
-      for (int p = b; p < e; p++) {
-        const int j = S.cell_atoms[p];
-        if (j == i) continue;
-        const int4 qj = S.posq[j];  // posq_cell holds ions shifted
-        const float3 d = qsep(qi, qj, G.qinvA);
-        const float r2f = d.x * d.x + d.y * d.y + d.z * d.z;
-        if (r2f > P.pre_mol2A) continue;
-        if (r2f >= P.acc_mol2A && !exact_in(G, S, i, j, P.rv2lj)) continue;
-        const bool ion_j = (qj.w & 0xff) == 3;
-        const int nw = ion_j ? 1 : 2;
-        const int slot = atomicAdd(&S.sc->mol_count, nw);
-        if (slot < P.mol_cap) S.mol_pairs[slot] = make_int2(i, j);
-        if (!ion_j && slot + 1 < P.mol_cap) S.mol_pairs[slot + 1] = make_int2(j, i);
-      }
-    }
-  }
-}
-
 __global__ void k_build_end(DevParams P, DevState S, int from_flag) {
   if (rebuild_skipped(S, from_flag)) return;
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     if (S.sc->mol_count > P.mol_cap) S.sc->overflow_mol = S.sc->mol_count;
+    // the replicas' flags (read by the kernels above), then the context's
+    for (int r = 1; r < P.nrep; r++) {
+      S.sc[r].rep_rebuild = 0;
+      S.sc[r].rep_soon = 0;
+    }
+    S.sc->rep_rebuild = 0;
+    S.sc->rep_soon = 0;
     S.sc->need_rebuild = 0;
+    S.sc->rebuild_all = 0;
     S.sc->rebuilds++;
   }
 }
@@ -477,8 +511,10 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
   k_scan_add<<<nscan, kScanBlock, 0, L.stream>>>(P, S, from_flag);
   k_cell_fill<<<nb_atoms, 256, 0, L.stream>>>(P, S, from_flag);
   const int bt = (L.build_block == 64 || L.build_block == 256) ? L.build_block : kBuildThreads;
-  const int nb_build = (P.N + bt - 1) / bt;
   const bool wide = P.mol_reach > 1;
+  // with the spec-mode ion-pair blocks after the atoms'
+  const int nb_build =
+      (P.N + bt - 1) / bt + (wide && P.nion > 0 ? min(P.nion * kIonSplit, 4096) : 0);
   if (bt == 64) {
     if (wide) k_build_atoms<true, 64><<<nb_build, 64, 0, L.stream>>>(P, S, from_flag);
     else k_build_atoms<false, 64><<<nb_build, 64, 0, L.stream>>>(P, S, from_flag);
@@ -489,8 +525,6 @@ cudaError_t launch_build_lists(const Launch& L, const DevParams& P, const DevSta
     if (wide) k_build_atoms<true, 128><<<nb_build, 128, 0, L.stream>>>(P, S, from_flag);
     else k_build_atoms<false, 128><<<nb_build, 128, 0, L.stream>>>(P, S, from_flag);
   }
-  if (P.mol_reach > 1 && P.nion > 0)
-    k_build_ion_pairs<<<min(P.nion, 4096), 128, 0, L.stream>>>(P, S, from_flag);
   k_build_end<<<1, 32, 0, L.stream>>>(P, S, from_flag);
   return cudaGetLastError();
 }

@@ -6,6 +6,7 @@ reference's Fortran routines that the GPU library is checked against.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import sys
 from pathlib import Path
 
@@ -465,3 +466,40 @@ def spec_oracle(slab: dict, params=None, impact: int = 1) -> Oracle:
     o.si_nlist()
     o.F[:] = o.si_force()
     return o
+
+
+def impact_stats(X, Xi, atype, Lb, surface_z: float, remove_z: float,
+                 displaced_threshold: float = 1.0e-10):
+    """The outcome of one impact, restated atom by atom in plain loops as a
+    check of the device statistics: (sputtered, ion depth below the surface
+    or nan, displaced). Sputtered: lattice atoms (atype < 3) above remove_z,
+    the spec-mode counterpart of cntsputter's count of lattice atoms in the
+    containment layer (src/temp.f90:69-93). Displaced: lattice atoms below
+    remove_z farther than the threshold from their initial site, by the
+    minimum image in x and y. Ion depth: the first ion's distance below
+    surface_z."""
+    n = len(atype)
+    sputtered = displaced = 0
+    depth = float("nan")
+    ion_seen = False
+    thr2 = displaced_threshold * displaced_threshold
+    for i in range(n):
+        t = int(atype[i])
+        z = float(X[i][2])
+        if t == 3:
+            if not ion_seen and z <= surface_z:
+                depth = surface_z - z
+            ion_seen = True
+            continue
+        if z > remove_z:
+            sputtered += 1
+            continue
+        r2 = 0.0
+        for d in range(3):
+            dd = float(X[i][d]) - float(Xi[i][d])
+            if d < 2:
+                dd -= Lb[d] * round(dd / Lb[d])
+            r2 += dd * dd
+        if r2 > thr2:
+            displaced += 1
+    return sputtered, depth, displaced

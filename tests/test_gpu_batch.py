@@ -95,17 +95,23 @@ def test_batch_layout(gpu_lib):
 
 
 def test_impact_stats_on_device(gpu_lib):
-    """fibmd_gpu_impact_stats against impact_statistics on the downloaded
-    final states of a batch after its cascades."""
+    """fibmd_gpu_impact_stats on the final states of a batch after its
+    cascades against the oracle's atom-by-atom restatement
+    (oracle_ffi.impact_stats) and the host function impact_statistics."""
     import fib_md_gb300 as fm
+    import oracle_ffi as of
 
     slabs = _slabs(1)
     b, Xb, Vb, tb, X0 = _batch(slabs, 300)
     sp, dc, dp = b.impact_stats([s.surface_z for s in slabs])
     for r, s in enumerate(slabs):
-        hs, hd, hdisp = fm.impact_statistics(Xb[b.rows(r)], s.Xi, s.atype, list(s.params.Lb),
+        Xr = Xb[b.rows(r)]
+        os_, od, odisp = of.impact_stats(Xr, s.Xi, s.atype, list(s.params.Lb), s.surface_z,
+                                         s.params.remove_z)
+        assert sp[r] == os_ and dc[r] == odisp, (r, sp[r], os_, dc[r], odisp)
+        assert (np.isnan(dp[r]) and np.isnan(od)) or abs(dp[r] - od) <= 1e-20
+        hs, hd, hdisp = fm.impact_statistics(Xr, s.Xi, s.atype, list(s.params.Lb),
                                              s.surface_z, s.params.remove_z)
-        assert sp[r] == hs and dc[r] == hdisp, (r, sp[r], hs, dc[r], hdisp)
-        assert (np.isnan(dp[r]) and np.isnan(hd)) or abs(dp[r] - hd) <= 1e-20
+        assert (hs, hdisp) == (os_, odisp)
     assert dc.sum() > 0
     b.close()

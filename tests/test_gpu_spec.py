@@ -76,8 +76,8 @@ def test_graph_many_leg_centres(gpu_lib, precision):
     every step. In
     binary64 to 1e-8 A after 60 steps; in binary32, whose binary64 atomic
     sums of a knot's wide range of terms round in the order they arrive
-    (which the knot's chaos amplifies), to 1e-6 A after 20 steps, where a
-    step without the knot's 3-body forces would be off by ~1e-3 A."""
+    (which the knot's chaos amplifies), to 1e-5 A after 10 steps, where
+    steps without the knot's 3-body forces would be off by ~1e-4 A."""
     s, X, V = _spec_system(nc=(6, 6, 4), ion_eV=0.0, precision=precision)
     X[-1] = X[-1] + np.array([0.0, 0.0, 30e-10])  # keep the ion away
     nsg = s.params.Nsg
@@ -93,7 +93,7 @@ def test_graph_many_leg_centres(gpu_lib, precision):
     a.set_option("heavy_if", 1)
     assert a.get_option("heavy_if") == 1
     assert a.work_counters()[5] >= 1  # many-leg centres at the start
-    n, tol_x, tol_t = (60, 1e-18, 1e-12) if precision == 0 else (20, 1e-16, 1e-9)
+    n, tol_x, tol_t = (60, 1e-18, 1e-12) if precision == 0 else (10, 1e-15, 1e-7)
     la, ta, _, _ = a.steps(2, n, 0, 0.0, 300.0)
     lb, tb, _, _ = b.steps(2, n, 0, 0.0, 300.0)
     Xa, _, _ = a.download()
