@@ -459,7 +459,7 @@ def bench_ours(args, rank, world, dist):
         "data": "synthetic (seeded)",
         "config": workload_config(args, cells, N),
         "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
-        "autotune": {"force_path": "before every 1000 steps among 8 or 10 staged legs per "
+        "autotune": {"force_path": "before every 1000 steps among 6 or 10 staged legs per "
                                    "thread (in blocks of 128 or 64) and 8 lanes per centre (1)",
                      "force_path_at_end": stage_end,
                      "force_reactions": "stored and gathered per atom" if args.reactions
@@ -581,7 +581,7 @@ def bench_large(args):
         "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
         "simulated_ps": t_sim * 1e12,
         "rebuild_fraction": rebuilds / float(args.large_steps),
-        "force_stage": "autotuned every 1000 steps among 8 or 10 staged legs per thread "
+        "force_stage": "autotuned every 1000 steps among 6 or 10 staged legs per thread "
                        "and 8 lanes per centre (1); "
                        f"{stage_end} at the end",
         "list_skin_at_end_A": skin_end,

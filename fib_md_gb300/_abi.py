@@ -114,6 +114,7 @@ SIGNATURES = {
     "fibmd_gpu_regime": (_I, [_VP, _DP, _IP]),
     "fibmd_gpu_timers": (_I, [_VP, _DP, _DP, _DP, _DP, _LLP, _I]),
     "fibmd_gpu_work_counters": (_I, [_VP, _LLP]),
+    "fibmd_gpu_virial": (_I, [_VP, _DP, _DP]),
     "fibmd_gpu_stream": (_VP, [_VP]),
     "fibmd_gpu_set_option": (_I, [_VP, C.c_char_p, _D]),
     "fibmd_gpu_get_option": (_I, [_VP, C.c_char_p, _DP]),

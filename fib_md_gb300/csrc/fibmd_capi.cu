@@ -57,6 +57,8 @@ struct fibmd_ctx {
   double* d_stage = nullptr;   // 3N doubles
   double* d_ke = nullptr;      // N doubles (xyz frames)
   unsigned long long* d_u64 = nullptr;
+  double* d_vir = nullptr;       // 6 doubles (virial), allocated on first use
+  double* d_vir_atom = nullptr;  // 6 N doubles (per-atom virial), on first use
   std::vector<void*> allocs;
   std::vector<double> tab, tabu;
   // regime (prms.f90 module variables)
@@ -1369,6 +1371,28 @@ int fibmd_gpu_force(fibmd_ctx* ctx, double* F_out, double* u_out, double* Utot) 
   int rc = sync_scalars(ctx);
   if (rc) return rc;
   return check_list_status(ctx);
+}
+
+int fibmd_gpu_virial(fibmd_ctx* ctx, double W[6], double* w_atom) {
+  if (!ctx || !W) return FIBMD_EINVAL;
+  if (!ctx->lists_built) return fail(ctx, FIBMD_ESTATE, "virial before nlist");
+  const size_t N = (size_t)ctx->P.N;
+  if (!ctx->d_vir) {
+    int rc = dalloc(ctx, &ctx->d_vir, 6);
+    if (rc) return rc;
+  }
+  if (w_atom && !ctx->d_vir_atom) {
+    int rc = dalloc(ctx, &ctx->d_vir_atom, 6 * N);
+    if (rc) return rc;
+  }
+  double* d_atom = w_atom ? ctx->d_vir_atom : nullptr;
+  CK(launch_virial(launch_of(ctx), ctx->P, ctx->S, d_atom, ctx->d_vir));
+  CK(cudaMemcpyAsync(W, ctx->d_vir, 6 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (w_atom)
+    CK(cudaMemcpyAsync(w_atom, d_atom, 6 * sizeof(double) * N, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FIBMD_OK;
 }
 
 int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[6]) {

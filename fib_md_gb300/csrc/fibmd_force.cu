@@ -539,6 +539,156 @@ __device__ __forceinline__ bool angle_term(const DevParams& P, int tc, const Leg
   return true;
 }
 
+// ---- virial (an observable, binary64 in both precisions) -------------------
+// W = sum over interactions of r (x) f: for a pair, the separation from
+// the partner to the centre times the force on the centre (each side of a
+// full-list pair adds half); for an angle term, minus the separation from
+// the centre to each leg times the force on that leg. Per atom, each
+// centre's terms (and half of each of its pairs) are its own. One warp per
+// centre: lanes take the listed neighbours (2-body table force, legs staged
+// in shared memory), then the unordered leg pairs. Components xx, yy, zz,
+// xy, xz, yz, in J. The Moliere pairs are added by k_virial_mol; the
+// reference mode's stale-list angle terms are not included.
+constexpr int kVirWarps = 4;
+constexpr int kVirLegs = 64;  // >= max_sw (checked at context creation)
+__device__ __forceinline__ void vir_add(double v[6], double dx, double dy, double dz, double fx,
+                                        double fy, double fz, double s) {
+  v[0] += s * dx * fx;
+  v[1] += s * dy * fy;
+  v[2] += s * dz * fz;
+  v[3] += s * 0.5 * (dx * fy + dy * fx);
+  v[4] += s * 0.5 * (dx * fz + dz * fx);
+  v[5] += s * 0.5 * (dy * fz + dz * fy);
+}
+
+__global__ void __launch_bounds__(32 * kVirWarps) k_virial(DevParams P, DevState S,
+                                                           double* w_atom, double* w_tot) {
+  __shared__ Leg64 legs[kVirWarps][kVirLegs];
+  __shared__ int nleg[kVirWarps];
+  __shared__ double btot[kVirWarps][6];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const size_t N = (size_t)P.N;
+  double acc[6] = {0, 0, 0, 0, 0, 0};  // this warp's total (lane 0)
+  int terr = 0;
+  for (int c = blockIdx.x * kVirWarps + w; c < P.N; c += gridDim.x * kVirWarps) {
+    if (lane == 0) nleg[w] = 0;
+    __syncwarp();
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    const int4 qc = S.posq[c];
+    const int tc = qc.w & 0xff;
+    const bool live = tc < 3 && !((qc.w >> 8) & FL_REMOVED);
+    if (live) {
+      const int n = min(S.n_sw[c], P.max_sw);
+      const double4_32a pc = S.pos[c];
+      const Geo& G = S.geo[rep_of_w(qc.w)];
+      for (int k = lane; k < n; k += 32) {
+        const int j = S.nbr_sw[(size_t)k * N + c];
+        const int4 qj = S.posq[j];
+        if ((qj.w >> 8) & FL_REMOVED) continue;
+        const int tj = qj.w & 0xff;
+        const Leg64 L = make_leg(P, G, pc, S.pos[j], tc, tj);
+        const double df = table_df(P, S.tab, S.tabu, L.u, &terr);
+        if (df != 0.0) {
+          const double cf = -(df / L.r * P.epssig[tc - 1][tj - 1]);
+          vir_add(v, L.dx, L.dy, L.dz, cf * L.dx, cf * L.dy, cf * L.dz, 0.5);
+        }
+        if (L.u < P.cut3) {
+          const int q = atomicAdd(&nleg[w], 1);
+          if (q < kVirLegs) legs[w][q] = L;
+        }
+      }
+    }
+    __syncwarp();
+    const int nl = min(nleg[w], kVirLegs);
+    for (int a = lane; a < nl; a += 32) {
+      const Leg64 A = legs[w][a];
+      for (int b = a + 1; b < nl; b++) {
+        const Leg64 B = legs[w][b];
+        double fc[3], fa[3], fb[3], e;
+        if (!angle_term(P, tc, A, B, fc, fa, fb, &e)) continue;
+        vir_add(v, A.dx, A.dy, A.dz, fa[0], fa[1], fa[2], -1.0);
+        vir_add(v, B.dx, B.dy, B.dz, fb[0], fb[1], fb[2], -1.0);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    }
+    if (lane == 0) {
+      if (w_atom)
+        for (int k = 0; k < 6; k++) w_atom[(size_t)k * N + c] = v[k];
+      for (int k = 0; k < 6; k++) acc[k] += v[k];
+    }
+    __syncwarp();
+  }
+  if (lane == 0)
+    for (int k = 0; k < 6; k++) btot[w][k] = acc[k];
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double t = 0.0;
+    for (int q = 0; q < kVirWarps; q++) t += btot[q][threadIdx.x];
+    atomicAdd(&w_tot[threadIdx.x], t);
+  }
+}
+
+// The Moliere pairs' share: each list entry (i, j) adds half of r (x) f for
+// the force on i (both orders are listed); unfired ions are skipped, as in
+// the force.
+__global__ void k_virial_mol(DevParams P, DevState S, double* w_atom, double* w_tot) {
+  int cnt = *((volatile int*)&S.sc->mol_count);
+  if (cnt > P.mol_cap) cnt = P.mol_cap;
+  double v[6] = {0, 0, 0, 0, 0, 0};
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < cnt; e += gridDim.x * blockDim.x) {
+    const int2 pr = S.mol_pairs[e];
+    const int i = pr.x, j = pr.y;
+    if (!(i < P.nfired && j < P.nfired)) continue;
+    if ((S.flags[i] | S.flags[j]) & FL_REMOVED) continue;
+    const int ti = S.atype[i] - 1, tj = S.atype[j] - 1;
+    const double4_32a pi = S.pos[i], pj = S.pos[j];
+    const Geo& G = S.geo[rep_of_flags(S.flags[i])];
+    const double dx = min_image(pi.x, pj.x, G.iLb[0], G.Lb[0]);
+    const double dy = min_image(pi.y, pj.y, G.iLb[1], G.Lb[1]);
+    const double dz = min_image(pi.z, pj.z, G.iLb[2], G.Lb[2]);
+    const double r2 = dx * dx + dy * dy + dz * dz;
+    if (!(r2 < P.rlj2)) continue;
+    const double rij = sqrt(r2);
+    const double aa = P.aamol[ti][tj];
+    const double e1 = exp(-(P.amol * rij / aa)), e2 = exp(-(P.bmol * rij / aa)),
+                 e3 = exp(-(P.gmol * rij / aa));
+    const double K = P.ie0 * P.Zmol[ti] * P.Zmol[tj] * P.ec * P.ec;
+    const double fc = K / rij *
+                      ((P.Amol * e1 + P.Bmol * e2 + P.Cmol * e3) / rij +
+                       (P.Amol * P.amol / aa * e1 + P.Bmol * P.bmol / aa * e2 +
+                        P.Cmol * P.gmol / aa * e3));
+    const double fcr = fc / rij;
+    double u[6] = {0, 0, 0, 0, 0, 0};
+    vir_add(u, dx, dy, dz, fcr * dx, fcr * dy, fcr * dz, 0.5);
+    for (int k = 0; k < 6; k++) {
+      if (w_atom) atomicAdd(&w_atom[(size_t)k * (size_t)P.N + i], u[k]);
+      v[k] += u[k];
+    }
+  }
+  for (int k = 0; k < 6; k++) {
+    double t = v[k];
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if ((threadIdx.x & 31) == 0 && t != 0.0) atomicAdd(&w_tot[k], t);
+  }
+}
+
+cudaError_t launch_virial(const Launch& L, const DevParams& P, const DevState& S,
+                          double* d_atom, double* d_tot) {
+  const int side = L.sms > 0 ? L.sms : 152;
+  cudaError_t e = cudaMemsetAsync(d_tot, 0, 6 * sizeof(double), L.stream);
+  if (e == cudaSuccess && d_atom)
+    e = cudaMemsetAsync(d_atom, 0, 6 * sizeof(double) * (size_t)P.N, L.stream);
+  if (e != cudaSuccess) return e;
+  const int nb = std::max(1, std::min(8 * side, (P.N + kVirWarps - 1) / kVirWarps));
+  k_virial<<<nb, 32 * kVirWarps, 0, L.stream>>>(P, S, d_atom, d_tot);
+  k_virial_mol<<<side, 128, 0, L.stream>>>(P, S, d_atom, d_tot);
+  return cudaGetLastError();
+}
+
 // Centres with more than kMaxLegs active legs (compressed cascade regions,
 // damaged slabs): a group of lanes per centre, 8 or 32 in binary32 and the
 // whole warp in binary64 (k_force_heavy chooses). The group first computes every listed leg and stages the active

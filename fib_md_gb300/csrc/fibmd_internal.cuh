@@ -431,7 +431,7 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
 // kernel then takes), or eight lanes per centre for every centre
 // (kStageGroup, the "stage" value 1: one kernel, faster on systems too
 // small to fill the GPU one thread per centre).
-constexpr int kStageSmall = 8;
+constexpr int kStageSmall = 6;
 constexpr int kStageLarge = 10;
 constexpr int kStageGroup = 1;
 constexpr int kReactMaxList = 64;  // list slots addressable by legpos's 6-bit fields
@@ -494,6 +494,10 @@ cudaError_t launch_force(const Launch& L, const DevParams& P, const DevState& S,
                          bool energy, bool count, bool spec_step = false);
 // the many-leg kernel alone (forces, no energy), for the step graph's IF node
 cudaError_t launch_force_heavy(const Launch& L, const DevParams& P, const DevState& S);
+// the virial in binary64: d_tot (6 doubles) and, if given, d_atom (6 x N,
+// component-major)
+cudaError_t launch_virial(const Launch& L, const DevParams& P, const DevState& S,
+                          double* d_atom, double* d_tot);
 // fibmd_integrate.cu
 cudaError_t launch_side_reduce(const Launch& L, const DevParams& P, const DevState& S,
                                double Ts, double Tau, double Ttar);

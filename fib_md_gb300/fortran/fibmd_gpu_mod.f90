@@ -268,6 +268,14 @@ module fibmd_gpu_mod
        integer(c_long_long) :: counts(6)
      end function fibmd_gpu_work_counters
 
+     ! virial W(6) = xx yy zz xy xz yz (J) and the per-atom shares w_atom(natm,6)
+     integer(c_int) function fibmd_gpu_virial(ctx, w, w_atom) bind(C)
+       import
+       type(c_ptr), value :: ctx
+       real(c_double) :: w(6)
+       real(c_double) :: w_atom(*)
+     end function fibmd_gpu_virial
+
      ! successive impacts on the device: ion_atoms 1-based, x/v (nimp,3)
      integer(c_int) function fibmd_gpu_dose(ctx, nimp, ion_atoms, x, v, steps, relax_s, &
           removed_after, ions_removed_after, time_after, steps_after) bind(C)

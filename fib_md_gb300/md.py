@@ -453,6 +453,16 @@ class FibMD:
         _, u, U = self.si_force_energy()
         return U, u
 
+    def virial(self, per_atom: bool = False):
+        """The virial of the current positions (fibmd_gpu_virial): W as xx,
+        yy, zz, xy, xz, yz in J, and with per_atom the (N, 6) per-atom
+        shares (else None)."""
+        W = np.zeros(6)
+        wa = np.zeros((self.N, 6), order="F") if per_atom else None
+        self._check(self.lib.fibmd_gpu_virial(self.h, _dp(W), _dp(wa) if per_atom else None),
+                    "virial")
+        return W, wa
+
     def work_counters(self):
         c = (C.c_longlong * 6)()
         self._check(self.lib.fibmd_gpu_work_counters(self.h, c), "work_counters")

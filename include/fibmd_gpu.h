@@ -350,6 +350,19 @@ int fibmd_gpu_pipe_peaks(double* fp64_tflops, double* fp32_tflops);
    per-thread stage holds (evaluated by the warp-per-centre path). */
 int fibmd_gpu_work_counters(fibmd_ctx* ctx, long long counts[6]);
 
+/* Virial of the current positions, sum over interactions of r (x) f in J
+   (W[0..5] = xx, yy, zz, xy, xz, yz): for each pair the separation from
+   partner to atom times the force on the atom, for each 3-body term minus
+   each leg's separation from the centre times the force on that leg; the
+   Moliere pairs of fired ions included. Evaluated in binary64 from the
+   current lists in either precision (reference mode's stale-list terms
+   excluded). w_atom (Natm x 6, column-major, may be NULL): per atom, the
+   terms of which it is the centre and half of each of its pairs. The
+   reference computes no virial (src/stats.f90:34-81 reports PE, KE and
+   momentum); this is the per-atom virial the hot path's specification
+   adds to forces and energies. */
+int fibmd_gpu_virial(fibmd_ctx* ctx, double W[6], double* w_atom);
+
 /* CUDA stream the context orders its work on (cudaStream_t as void*). */
 void* fibmd_gpu_stream(fibmd_ctx* ctx);
 

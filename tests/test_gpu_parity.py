@@ -224,11 +224,11 @@ def test_regime_switch_and_parking(gpu_lib):
     assert np.abs(X - o.X).max() < TRAJ_ATOL_M
 
 
-@pytest.mark.parametrize("stage", [8, 10, 1])
+@pytest.mark.parametrize("stage", [6, 10, 1])
 def test_mixed_precision_force_error(gpu_lib, stage):
     """binary32 force arithmetic (reduced units) against the binary64 oracle;
     the 2-body term is analytic in binary32, tabulated in the reference.
-    Stages 8 and 10: one thread per centre; 1: eight lanes per centre."""
+    Stages 6 and 10: one thread per centre; 1: eight lanes per centre."""
     o = _slab()
     o.si_nlist()
     Fr = o.si_force()
@@ -266,7 +266,7 @@ def _compressed_core(scale=0.8, radius_A=6.0):
 def test_group_path_energies(gpu_lib):
     """Mixed precision: forces and per-atom energies of the eight-lanes-per-
     centre path (stage 1) against the one-thread-per-centre path with its
-    many-leg kernel (stage 8) on the compressed-core slab: the same terms
+    many-leg kernel (stage 6) on the compressed-core slab: the same terms
     summed in another order, so equal to binary32 rounding."""
     import fib_md_gb300 as fm
 
@@ -274,7 +274,7 @@ def test_group_path_energies(gpu_lib):
     p = o.p.copy()
     p.precision = 1
     out = {}
-    for stage in (8, 1):
+    for stage in (6, 1):
         g = fm.FibMD(p)
         g.set_option("stage", stage)
         g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
@@ -282,14 +282,14 @@ def test_group_path_energies(gpu_lib):
         g.si_nlist()
         out[stage] = g.si_force_energy()
         g.close()
-    (F8, u8, U8), (F1, u1, U1) = out[8], out[1]
-    assert np.isfinite(u1).all() and np.abs(u8).max() > 0
-    assert _maxrel(F1, F8) < 1e-5
-    assert _maxrel(u1, u8) < 1e-5
-    assert abs(U1 - U8) < 1e-6 * abs(U8)
+    (F6, u6, U6), (F1, u1, U1) = out[6], out[1]
+    assert np.isfinite(u1).all() and np.abs(u6).max() > 0
+    assert _maxrel(F1, F6) < 1e-5
+    assert _maxrel(u1, u6) < 1e-5
+    assert abs(U1 - U6) < 1e-6 * abs(U6)
 
 
-@pytest.mark.parametrize("precision,stage", [(0, 8), (1, 8), (1, 10), (1, 1)])
+@pytest.mark.parametrize("precision,stage", [(0, 6), (1, 6), (1, 10), (1, 1)])
 def test_many_leg_centres(gpu_lib, precision, stage):
     """Centres with more legs than the per-thread stage (the many-leg paths:
     the warp-per-centre kernel in binary64, the eight-lane groups of the
@@ -341,7 +341,7 @@ def test_block_size_variants(gpu_lib):
     out = {}
     for fb in (128, 64):
         g = fm.FibMD(p)
-        g.set_option("stage", 8)
+        g.set_option("stage", 6)
         g.set_option("force_block", fb)
         g.upload(o.X, o.V, None, o.Xi, o.mass, o.atype, o.xsides)
         g.set_impact(1)

@@ -246,7 +246,7 @@ def test_stored_reactions_match_atomics(gpu_lib):
     F = {}
     for react in (0, 1):
         g = gpu_ctx(slab, precision=1)
-        g.set_option("stage", 8)
+        g.set_option("stage", 6)
         g.set_option("force_block", 128)
         g.set_option("reactions", react)
         assert g.get_option("reactions") == react
