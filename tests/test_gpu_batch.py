@@ -115,3 +115,39 @@ def test_impact_stats_on_device(gpu_lib):
         assert (hs, hdisp) == (os_, odisp)
     assert dc.sum() > 0
     b.close()
+
+
+def test_batch_lists_hold_every_pair(gpu_lib):
+    """After 150 steps of the three cascades in one batch, whose replicas
+    rebuild their SW lists separately (those that moved half the skin and
+    those that moved a quarter), every replica's list still holds each pair
+    of its atoms inside the SW cutoff 0.999*a*sigma at the current positions
+    (minimum image in x and y), and no pair across replicas."""
+    slabs = _slabs(1)
+    b, Xb, Vb, tb, X0 = _batch(slabs, 150)
+    listed = {tuple(p) for p in b.get_pairs(0)}
+    tags = b.get_tags()
+    lo = [int(b.offsets[r]) for r in range(b.nrep)]
+    hi = [int(b.offsets[r] + b.natm[r]) for r in range(b.nrep)]
+    for (i, j) in listed:
+        ri = next(r for r in range(b.nrep) if lo[r] < i <= hi[r])
+        assert lo[ri] < j <= hi[ri], (i, j)
+    for r, sl in enumerate(slabs):
+        p = sl.params
+        rc = 0.999 * p.al * max(p.sigmaSi, p.sigmaGe)
+        Lb = np.array(p.Lb[:])
+        nsg = p.Nsg
+        X = Xb[b.rows(r)][:nsg]
+        live = (tags[b.rows(r)][:nsg] & 4) == 0
+        need = 0
+        for a in range(nsg):
+            if not live[a]:
+                continue
+            d = X[a + 1:] - X[a]
+            d[:, :2] -= Lb[:2] * np.rint(d[:, :2] / Lb[:2])
+            close = np.nonzero((np.einsum("ij,ij->i", d, d) < rc * rc) & live[a + 1:])[0]
+            for c in close:
+                need += 1
+                assert (lo[r] + a + 1, lo[r] + a + 2 + c) in listed, (r, a, c)
+        assert need > nsg  # about 2 bonds per atom in a diamond lattice
+    b.close()
