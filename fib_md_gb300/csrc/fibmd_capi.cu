@@ -844,18 +844,6 @@ static int finish_create(fibmd_ctx* ctx, const std::vector<int>& ions, fibmd_ctx
   S.tabu = tabu;
   AL(S.epot, N);
   AL(S.partials, 3 * (size_t)kMaxRedBlocks);
-  // one ticket and one partial per group of kKickGroup kick blocks of each
-  // replica (an index below kMaxRedBlocks / kKickGroup + replicas + 2); the
-  // tickets each on its own 32-byte sector
-  const size_t n_groups = (size_t)kMaxRedBlocks / kKickGroup + R + 2;
-  const size_t n_group_ticket = 8 * n_groups;
-  AL(S.group_ticket, n_group_ticket);
-  AL(S.group_part, 3 * n_groups);
-  if (cudaMemset(S.group_ticket, 0, sizeof(unsigned) * n_group_ticket) != cudaSuccess) {
-    set_noctx_error("cudaMemset failed");
-    fibmd_gpu_destroy(ctx);
-    return FIBMD_ECUDA;
-  }
   AL(S.sc, R);
   for (auto& k : ctx->skins) AL(k.d_geo, R);
   int* ion_list = nullptr;

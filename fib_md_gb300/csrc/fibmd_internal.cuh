@@ -28,7 +28,6 @@ namespace fibmd {
 constexpr int kMaxLegs = 12;       // active 3-body legs held per centre
 constexpr int kRedThreads = 256;   // threads of reduction kernels
 constexpr int kMaxRedBlocks = 16384;  // row stride of the reduction partials
-constexpr int kKickGroup = 32;     // spec kick blocks per first-level ticket
 constexpr int kKickThreads = 256;  // spec kick block; replicas start at multiples
 // Binary32 SW legs with exp(gamma/(u-a)) below this are dropped: an angle
 // term is at most lambda*eps*E_a*E_b (~45 eV E_a E_b), so such a leg moves a
@@ -164,6 +163,9 @@ struct DevScalars {
   int kd_cont;         //                   the step loop goes on (drift)
   int kd_timeout;      //                   a barrier wait gave up
   unsigned long long rebuilds;  // list builds since creation
+  unsigned long long acc_vmax2;  // spec kick: running max |v|^2 (bits), sum m v^2
+  double acc_tsum;               //            and count of the thermostat layer,
+  int acc_tcnt;                  //            cleared by the replica's last chunk
   unsigned int ticket[8];
   unsigned long long counters[4];
 };
@@ -229,8 +231,6 @@ struct DevState {
   double* epot;
   // reductions
   double* partials;
-  unsigned* group_ticket;  // spec kick: first-level tickets, 32 bytes apart
-  double* group_part;      //            group partials (3 rows)
   DevScalars* sc;    // one per replica; context-wide fields live in sc[0]
   // replicas
   const Geo* geo;    // nrep entries
