@@ -444,6 +444,10 @@ def bench_ours(args, rank, world, dist):
         bpa = float(kv.get("mixed_dram_bytes_per_atom", "0") or 0)
         if bpa > 0:
             traffic = bpa * N
+        bpl = float(kv.get("mixed_dram_bytes_per_atom_in_loop", "0") or 0)
+        traffic_loop = bpl * N if bpl > 0 else None
+    else:
+        traffic_loop = None
     out = {
         "metric": METRIC,
         "value": value,
@@ -478,7 +482,14 @@ def bench_ours(args, rank, world, dist):
                               "peak_source": "measured in this run (DFMA loop)"}},
         "roofline": {"bound": "fp32", "kernel": "k_force<mixed>", "achieved": achieved,
                      "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-                     "traffic": traffic, "flops_per_launch": flops,
+                     "traffic": traffic,
+                     "traffic_in_loop": traffic_loop,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per "
+                                       "launch of this kernel on this slab "
+                                       "(profiles/force_kernel_traffic.txt): 'traffic' with "
+                                       "ncu's cache flush before the launch, 'traffic_in_loop' "
+                                       "with the caches the step loop leaves",
+                     "flops_per_launch": flops,
                      "bytes_per_launch_algorithmic": 56 * N,
                      "force_kernel_ms": 1e3 * fk_avg, "launches": fk_n,
                      "timed_over": f"the window's first {min(args.md_steps, 1000)} steps, "
