@@ -4,10 +4,11 @@
 // 231-236), controlsidetemp (src/temp.f90:32-67), adjusttemp/temperature
 // (src/temp.f90:160-205), freezsidesN and rebox (src/tools.f90:26-51),
 // frzsptrdatms (src/temp.f90:99-127) and calc_atm (src/timeint.f90:277-298).
-// All updates are binary64 and keep the reference's operation order. Sums
-// use a deterministic two-level reduction (block partials summed in block
-// order by the last block), so repeated runs give identical thermostat
-// factors.
+// All updates are binary64 and keep the reference's operation order. The
+// reference-mode sums use a deterministic two-level reduction (block
+// partials summed in block order by the last block), so repeated runs give
+// identical thermostat factors; the spec-mode kick adds its block partials
+// with atomics (see spec_kick_chunk).
 #include "fibmd_internal.cuh"
 
 namespace fibmd {
