@@ -704,7 +704,7 @@ constexpr int kHeavyLegs = 64;  // >= max_sw (checked at context creation)
 
 // One pass over the many-leg centres with GROUP lanes per centre (stages in
 // sl/sj/snl: kHeavyWarps * 32 / GROUP of them).
-template <bool MIXED, bool ENERGY, int GROUP, typename R>
+template <bool MIXED, bool ENERGY, int GROUP, bool UNI, typename R>
 __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState& S, int cnt,
                                               R (*sl)[6][kHeavyLegs], int (*sj)[kHeavyLegs],
                                               int* snl) {
@@ -749,7 +749,7 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
             const float3 dq = qsep(qc, qq[u], G.qinvA);
             const float r2 = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
             const float rinv = rsqrtf(r2);
-            const float is = P.isigA[tc - 1][tj - 1];
+            const float is = UNI ? P.isigA[0][0] : P.isigA[tc - 1][tj - 1];
             const float ue = r2 * rinv * is;
             if (!(ue < (float)P.cut3)) continue;
             const float ia = __fdividef(1.0f, ue - (float)P.al);
@@ -798,7 +798,8 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
         const R cs = ax * bx + ay * by + az * bz;
         const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
         R lp;
-        if constexpr (MIXED) lp = P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
+        if constexpr (MIXED)
+          lp = UNI ? P.lepsA[0][0][0] : P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         const R pref = b == a ? (R)0 : lp * aE * sl[sg][4][b];
         const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
@@ -855,7 +856,7 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
 // whole warp per centre where they fit in one pass (a few cascade-core
 // centres: the pass is then as long as one centre's chain, which the wider
 // group shortens). Binary64: the whole warp (its leg stage is twice the size).
-template <bool MIXED, bool ENERGY>
+template <bool MIXED, bool ENERGY, bool UNI = false>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
@@ -869,11 +870,11 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
   if (cnt == 0) return;
   if constexpr (MIXED) {
     if (cnt > (int)gridDim.x * kHeavyWarps) {
-      heavy_centres<MIXED, ENERGY, 8>(P, S, cnt, sl, sj, snl);
+      heavy_centres<MIXED, ENERGY, 8, UNI>(P, S, cnt, sl, sj, snl);
       return;
     }
   }
-  heavy_centres<MIXED, ENERGY, 32>(P, S, cnt, sl, sj, snl);
+  heavy_centres<MIXED, ENERGY, 32, UNI>(P, S, cnt, sl, sj, snl);
 }
 
 // Binary32 force with eight lanes per centre for every centre (four centres
@@ -884,7 +885,8 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_heavy(DevParams P, D
 // force. Twice the warps of a one-thread-per-centre pass per eight atoms and
 // a fraction of its dependent chain; chosen by the force-stage autotune
 // where it is faster (tens of thousands of atoms).
-template <bool ENERGY, bool COUNT>
+// UNI: every lattice atom is Si (P.uniform): the [Si][Si] constants directly.
+template <bool ENERGY, bool COUNT, bool UNI = false>
 __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
@@ -914,7 +916,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
     tc = qc.w & 0xff;
     if (tc < 3 && !((qc.w >> 8) & FL_REMOVED)) n = S.n_sw[c];
   }
-  const int ta = tc - 1;
+  const int ta = UNI ? 0 : tc - 1;
   float fx = 0.f, fy = 0.f, fz = 0.f, ui = 0.f;
   unsigned cnt_pairs = 0, cnt_ang = 0;
   if (n > 0) {
@@ -941,7 +943,7 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
         const float3 dq = qsep(qc, qj, G.qinvA);
         const float r2f = dq.x * dq.x + dq.y * dq.y + dq.z * dq.z;
         if (r2f > P.pre3mA2 || ((qj.w >> 8) & FL_REMOVED)) continue;
-        const int tb = (qj.w & 0xff) - 1;
+        const int tb = UNI ? 0 : (qj.w & 0xff) - 1;
         const float rinv = rsqrtf(r2f);
         const float is = P.isigA[ta][tb];
         const float ue = r2f * rinv * is;
@@ -989,9 +991,9 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
       const float bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
       const float cs = ax * bx + ay * by + az * bz;
       const float c3 = cs + thrd, W = c3 * c3, s2 = 2.0f * c3;
-      const float pref =
-          b == a ? 0.f
-                 : P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30] * aE * sl[sg][4][b];
+      const float lp = UNI ? P.lepsA[0][0][0]
+                           : P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30];
+      const float pref = b == a ? 0.f : lp * aE * sl[sg][4][b];
       const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
       afx += pref * (wa * ax + sa * bx);
       afy += pref * (wa * ay + sa * by);
@@ -1245,6 +1247,9 @@ static cudaError_t heavy_impl(const Launch& L, const DevParams& P, const DevStat
   const int side = L.sms > 0 ? L.sms : 152;
   const int heavy_blocks =
       std::max(side, std::min(8 * side, (P.N / 64 + kHeavyWarps - 1) / kHeavyWarps));
+  if (MIXED && !ENERGY && P.uniform)
+    return launch_k(k_force_heavy<MIXED, ENERGY, true>, heavy_blocks, 32 * kHeavyWarps, 0,
+                    L.stream, pdl, P, S);
   return launch_k(k_force_heavy<MIXED, ENERGY>, heavy_blocks, 32 * kHeavyWarps, 0, L.stream, pdl,
                   P, S);
 }
@@ -1309,8 +1314,11 @@ template <bool ENERGY, bool COUNT>
 static cudaError_t group_impl(const Launch& L, const DevParams& P, const DevState& S) {
   constexpr int NG = kHeavyWarps * 4;  // centres per block
   if (L.force_a) cudaEventRecord(L.force_a, L.stream);
-  k_force_group<ENERGY, COUNT>
-      <<<(P.N + NG - 1) / NG + mol_blocks(P), 32 * kHeavyWarps, 0, L.stream>>>(P, S);
+  const int nb = (P.N + NG - 1) / NG + mol_blocks(P);
+  if (!ENERGY && P.uniform)
+    k_force_group<ENERGY, COUNT, true><<<nb, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
+  else
+    k_force_group<ENERGY, COUNT><<<nb, 32 * kHeavyWarps, 0, L.stream>>>(P, S);
   if (L.force_b) cudaEventRecord(L.force_b, L.stream);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && P.mode == FIBMD_MODE_REF) {
