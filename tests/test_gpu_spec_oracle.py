@@ -28,7 +28,7 @@ FORCE_RTOL = 1e-10    # per atom, of max(|F_ref,i|, RMS(F_ref))
 per_atom_err = of.per_atom_err
 
 
-def config1(ion_height_A=10.0, skin_A=0.6, cells=(8, 8, 8), seed=1001, eV=500.0, polar=0.0,
+def slab_8x8x8(ion_height_A=10.0, skin_A=0.6, cells=(8, 8, 8), seed=1001, eV=500.0, polar=0.0,
             remove_above_A=35.0):
     """The 8x8x8-cell slab (4096 Si + 1 Ga), 500 eV Ga at normal incidence
     ion_height_A above the surface, 300 K Maxwell-Boltzmann velocities,
@@ -90,10 +90,10 @@ def check_runs(o, g, rec_o, rec_g):
 
 
 @pytest.mark.parametrize("ion_height_A", [10.0, 1.5])
-def test_spec_trajectory_config1(gpu_lib, ion_height_A):
-    """The config-1 set-up for 100 steps: with the ion 10 A up (the
+def test_spec_trajectory_8x8x8(gpu_lib, ion_height_A):
+    """The 8x8x8-cell slab for 100 steps: with the ion 10 A up (the
     approach) and 1.5 A up (the first 100 steps of the cascade)."""
-    slab = config1(ion_height_A=ion_height_A)
+    slab = slab_8x8x8(ion_height_A=ion_height_A)
     o = of.spec_oracle(slab)
     g = gpu_ctx(slab)
     F0 = g.si_force()
@@ -182,7 +182,7 @@ def test_skin_switch_keeps_trajectory(gpu_lib, graph):
     candidates, 0.75 x the start): the next step rebuilds the lists with the
     new radius and cell grid, and the trajectory stays the oracle's (which
     keeps the start skin) within 1e-8 A over 100 steps of the cascade."""
-    slab = config1(ion_height_A=1.5)
+    slab = slab_8x8x8(ion_height_A=1.5)
     o = of.spec_oracle(slab)
     g = gpu_ctx(slab, graph=graph)
     assert g.get_option("skin_candidates") == 3 and abs(g.get_option("skin") - 0.6) < 1e-9
