@@ -283,6 +283,18 @@ def flops_per_force(counts):
     return 40 * pairs + 100 * angles + 60 * mol + 100 * stale
 
 
+def tuning_chunks(md_steps):
+    """Graph chunks of one call of md_steps steps right after an upload: the
+    force path is re-timed 1000 steps after the upload and then after twice
+    the last interval, up to 8000 steps, while its choice stands."""
+    pairs, interval, n = md_steps // 2, 500, 0
+    while pairs > 0:
+        pairs -= min(pairs, interval)
+        interval = min(2 * interval, 4000)
+        n += 1
+    return n
+
+
 def replica_rate(dist, units, seconds, device):
     """Whole-job rate of independent replicas (one per rank, no data-path
     collective): the units all ranks processed over the slowest rank's
@@ -464,8 +476,8 @@ def bench_ours(args, rank, world, dist):
         "data": "synthetic (seeded)",
         "config": workload_config(args, cells, N),
         "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
-        "autotune": {"force_path": "before every 1000 steps among 6 or 10 staged legs per "
-                                   "thread (in blocks of 128 or 64) and 8 lanes per centre (1)",
+        "autotune": {"force_path": "1000 steps after the upload, then after doubling "
+                                   "intervals, among 6 or 10 staged legs per thread (in blocks of 128 or 64) and 8 lanes per centre (1)",
                      "force_path_at_end": stage_end,
                      "force_reactions": "stored and gathered per atom" if args.reactions
                                         else "binary64 atomics",
@@ -515,13 +527,14 @@ def bench_ours(args, rank, world, dist):
         # per MD step: drift, rebuild condition, force (main with the Moliere
         # blocks, many-leg; one kernel on the 8-lanes-per-centre path), kick,
         # kick reduction = 6; per step pair the loop control; 9 kernels per
-        # list rebuild; the loop set-up per 1000-step chunk. Launch by launch:
+        # list rebuild; the loop set-up per chunk between force-path tunings
+        # (1000 steps after the upload, then doubling). Launch by launch:
         # the 9 list kernels every step (they return at once when no rebuild
         # is due), no condition or loop kernels
         "gpu_launches": int((14 if stage_end != 1 else 13) * args.md_steps * args.steps
                             if args.no_graph else
                             (6.5 if stage_end != 1 else 5.5) * args.md_steps * args.steps +
-                            9 * rebuilds + args.steps * ((args.md_steps + 999) // 1000)),
+                            9 * rebuilds + args.steps * tuning_chunks(args.md_steps)),
         "rebuild_fraction": rebuilds / float(args.md_steps * args.steps),
         "wall_s_timed": wall,
         "clocks": clk.summary(),
@@ -593,7 +606,8 @@ def bench_large(args):
         "atom_steps_per_s": rate, "us_per_md_step": 1e6 * secs / args.large_steps,
         "simulated_ps": t_sim * 1e12,
         "rebuild_fraction": rebuilds / float(args.large_steps),
-        "force_stage": "autotuned every 1000 steps among 6 or 10 staged legs per thread "
+        "force_stage": "autotuned at doubling intervals from 1000 steps among 6 or 10 "
+                       "staged legs per thread "
                        "and 8 lanes per centre (1); "
                        f"{stage_end} at the end",
         "list_skin_at_end_A": skin_end,

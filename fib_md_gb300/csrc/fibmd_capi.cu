@@ -85,9 +85,15 @@ struct fibmd_ctx {
   int graph_nfired = -1;
   int graph_stage = 0;               // the force stage size it was captured with
   // binary32 force kernel: stage size, re-chosen by timing (autotune) before
-  // each chunk of kTuneSteps spec-mode steps
+  // each chunk of spec-mode steps (kTuneSteps, doubling up to 8 times that
+  // while the choice stands)
   int stage = kStageSmall;
   bool autotune = true;
+  long long tune_pairs = 0;   // step pairs between tunings (0: kTuneSteps / 2)
+  long long tune_left = 0;    // step pairs left before the next tuning
+  int tune_count = 0;         // tunings so far
+  float tune_ms[5] = {};      // each candidate's last timing
+  bool tune_switched = false; // the last tuning changed the path
   // atoms per block of the binary32 force kernel (128 or 64, tuned with the
   // force path) and of the pair-list build (64, 128 or 256, tuned with the
   // skin); the graph is captured again when one changes
@@ -1104,6 +1110,9 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
+  // a new state: the force path is timed again before its first steps
+  ctx->tune_pairs = 0;
+  ctx->tune_left = 0;
   // a slab without Ge takes the binary32 force kernel's single-species path
   ctx->uniform = uniform;
   ctx->P.uniform = uniform;
@@ -1845,21 +1854,35 @@ static int tune_stage(fibmd_ctx* ctx) {
   constexpr int kCand = 5;
   const int stages[kCand] = {kStageSmall, kStageSmall, kStageLarge, kStageLarge, kStageGroup};
   const int blocks[kCand] = {128, 64, 128, 64, 128};
-  float ms[kCand] = {};
+  int cur = 0;
+  for (int q = 0; q < kCand; q++)
+    if (stages[q] == ctx->stage && (stages[q] == kStageGroup || blocks[q] == ctx->force_block))
+      cur = q;
+  // every fourth tuning times all candidates; the others skip those that
+  // were over 1.5 times the best last time (the tuning runs are steps'
+  // worth of force evaluations)
+  float* ms = ctx->tune_ms;
+  float last_best = 0.f;
+  const bool full = ctx->tune_count % 4 == 0;
+  if (!full) {
+    last_best = ms[0];
+    for (int q = 1; q < kCand; q++) last_best = std::min(last_best, ms[q]);
+  }
   int rc = FIBMD_OK;
-  for (int q = 0; q < kCand && rc == FIBMD_OK; q++)
+  for (int q = 0; q < kCand && rc == FIBMD_OK; q++) {
+    if (!full && q != cur && ms[q] > 1.5f * last_best) continue;
     rc = time_force_graph(ctx, stages[q], blocks[q], ctx->react, a, b, &ms[q]);
+  }
   ctx->pool.push_back(a);
   ctx->pool.push_back(b);
   if (rc) return rc;
+  ctx->tune_count++;
   // switch only for a clear gain: a switch recaptures the step graph
-  int cur = 0, best = 0;
-  for (int q = 0; q < kCand; q++) {
-    if (stages[q] == ctx->stage && (stages[q] == kStageGroup || blocks[q] == ctx->force_block))
-      cur = q;
+  int best = 0;
+  for (int q = 0; q < kCand; q++)
     if (ms[q] < ms[best]) best = q;
-  }
-  if (ms[best] < 0.97f * ms[cur]) {
+  ctx->tune_switched = ms[best] < 0.97f * ms[cur];
+  if (ctx->tune_switched) {
     ctx->stage = stages[best];
     ctx->force_block = blocks[best];
   }
@@ -1984,8 +2007,10 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
   CK(cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, ctx->stream));
   long long todo = max_steps;
   if (ctx->use_graph && todo >= 2) {
-    // in chunks of kTuneSteps steps, before each of which the binary32 force
-    // kernel's stage size is re-chosen on the current state
+    // in chunks, before each of which the binary32 force kernel's stage size
+    // is re-chosen on the current state when it is due: kTuneSteps steps
+    // after an upload or a change of path, then twice as many as last time,
+    // up to 8 * kTuneSteps, counted across calls
     const bool tune = ctx->autotune && P.precision == FIBMD_PREC_MIXED && ctx->lists_built;
     // and in long calls, before every kSkinTuneEvery-th chunk, the list skin
     const bool stune = ctx->skin_tune && ctx->skins.size() > 1 && ctx->lists_built &&
@@ -2003,17 +2028,25 @@ static int spec_steps(fibmd_ctx* ctx, long long max_steps, long long* lt, double
         if (rs) return rs;
         pairs -= pr;
       }
-      const long long chunk = (tune || stune) ? std::min(pairs, kTuneSteps / 2) : pairs;
       ctx->graph_chunks++;
-      if (tune) {
+      if (tune && ctx->tune_left <= 0) {
         CK(cudaStreamSynchronize(ctx->stream));
         int rt = tune_stage(ctx);
         if (rt) return rt;
         CK(cudaMemsetAsync(ctx->S.frc_new, 0, sizeof(double4_32a) * (size_t)P.N, ctx->stream));
+        // the next tuning comes later while the choice stands
+        const long long base = kTuneSteps / 2;
+        ctx->tune_pairs = (ctx->tune_switched || ctx->tune_pairs <= 0)
+                              ? base
+                              : std::min(2 * ctx->tune_pairs, 8 * base);
+        ctx->tune_left = ctx->tune_pairs;
       }
+      const long long chunk =
+          tune ? std::min(pairs, ctx->tune_left) : stune ? std::min(pairs, kTuneSteps / 2) : pairs;
       int rc = run_spec_graph(ctx, chunk);
       if (rc) return rc;
       pairs -= chunk;
+      if (tune) ctx->tune_left -= chunk;
     }
     *lt += 2 * (todo / 2);
     todo -= 2 * (todo / 2);

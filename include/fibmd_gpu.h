@@ -287,11 +287,12 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    kernel, default 0), "graph" (spec mode runs step pairs as one CUDA
    graph launch with device-side rebuild decisions, default 1; phase and
    kernel timers see only the steps run outside the graph), "autotune"
-   (mixed precision: before every 1000 spec-mode steps of a graph run, and
-   before a dose, time the binary32 force paths (each stage with 128 or 64
-   centres per block, and eight lanes per centre) on the current state and
-   keep the fastest, default 1) and "stage" (the binary32 force path: 8 or
-   10 staged leg candidates per centre with one thread per centre, or 1 for
+   (mixed precision: before a dose, and in the spec-mode steps of a graph
+   run 1000 steps after an upload or a change of path and then after
+   doubling intervals up to 8000 steps, time the binary32 force paths (each
+   stage with 128 or 64 centres per block, and eight lanes per centre) on
+   the current state and keep the fastest, default 1) and "stage" (the
+   binary32 force path: 6 or 10 staged leg candidates per centre with one thread per centre, or 1 for
    eight lanes per centre, the faster on small systems; setting it turns
    "autotune" off) and "pdl" (default 0; 1: the step loop's kernels are
    launched as programmatic dependents of the kernel before them, so each
