@@ -99,7 +99,7 @@ struct fibmd_ctx {
   // skin); the graph is captured again when one changes
   int force_block = 128;
   int build_block = 128;
-  int graph_force_block = -1, graph_build_block = -1, graph_uniform = -1;
+  int graph_force_block = -1, graph_build_block = -1, graph_uniform = -1, graph_pair = -1;
   int uniform = 0;  // the uploaded lattice holds no Ge
   bool react = false;  // binary32 path: stored reactions instead of atomics
   int graph_react = -1;
@@ -114,6 +114,10 @@ struct fibmd_ctx {
   // the graph's kick of each step fused with the next step's drift (option
   // "fuse"), in a grid of at most kd_blocks resident blocks
   bool fuse = true;
+  // spec-mode rebuild rule of a single system (option "rebuild_rule"): 1, the
+  // two largest displacements since the build reach the skin; 0, any atom's
+  // displacement reaches half the skin (a batch always takes 0 per replica)
+  int rebuild_rule = 1;
   int kd_blocks = 0;       // resident blocks of the fused kernel (0: unavailable)
   int kd_grid = 0;         // option "kd_grid": its grid size instead (tests)
   int graph_fuse = -1;
@@ -486,6 +490,12 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   const double half = 0.5 * skin * 0.99;
   P.disp_fast2 = half * half;
   P.disp_fastA2 = (float)(half * half * 1e20);
+  // the pair rule: a pair outside the list radius at the build comes within
+  // the cutoff only once the two atoms' displacements add up to the skin;
+  // displacements under an eighth of it are counted at that bound
+  P.pair_rule = 0;
+  P.disp_skinA = (float)(2.0 * half * 1e10);
+  P.disp_lowA2 = (float)((0.25 * half * 1e10) * (0.25 * half * 1e10));
   // binary32 reduced units
   for (int a = 0; a < 2; a++)
     for (int b = 0; b < 2; b++) {
@@ -557,6 +567,7 @@ static int derive_skin(const fibmd_ctx* ctx, double skin, fibmd_ctx::SkinSet& ou
   int rc = derive_dev_params(q, ctx->impact, ctx->umax, ctx->tab_last, out.P, g0, err, errlen);
   if (rc) return rc;
   out.P.uniform = ctx->uniform;
+  out.P.pair_rule = (ctx->rebuild_rule == 1 && q.mode == FIBMD_MODE_SPEC) ? 1 : 0;
   out.skin = skin;
   if (ctx->reps.empty()) {
     out.geo.assign(1, g0);
@@ -585,6 +596,7 @@ static int derive_skin(const fibmd_ctx* ctx, double skin, fibmd_ctx::SkinSet& ou
     return FIBMD_EINVAL;
   }
   out.P.nrep = nrep;
+  if (nrep > 1) out.P.pair_rule = 0;
   out.P.nion = (int)nion;
   out.P.nfired = q.Natm;
   out.P.ncell = (int)cells;
@@ -1107,6 +1119,7 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemsetAsync(&ctx->S.sc->nan_flag, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(&ctx->S.sc->kd_timeout, 0, sizeof(int), ctx->stream));
+  CK(cudaMemsetAsync(&ctx->S.sc->disp_top[0], 0, 3 * sizeof(unsigned), ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
@@ -1462,6 +1475,12 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
     ctx->pdl = value != 0.0;
   } else if (!std::strcmp(key, "fuse")) {
     ctx->fuse = value != 0.0;
+  } else if (!std::strcmp(key, "rebuild_rule")) {
+    if (value != 0.0 && value != 1.0) return fail(ctx, FIBMD_EINVAL, "rebuild_rule must be 0 or 1");
+    ctx->rebuild_rule = (int)value;
+    const int pr = (ctx->rebuild_rule == 1 && ctx->p.mode == FIBMD_MODE_SPEC && ctx->P.nrep == 1);
+    ctx->P.pair_rule = pr;
+    for (auto& k : ctx->skins) k.P.pair_rule = pr;
   } else if (!std::strcmp(key, "skin_tune")) {
     ctx->skin_tune = value != 0.0;
   } else if (!std::strcmp(key, "heavy_if")) {
@@ -1543,6 +1562,8 @@ int fibmd_gpu_get_option(fibmd_ctx* ctx, const char* key, double* value) {
     *value = ctx->pdl ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "fuse")) {
     *value = fuse_in_use(ctx) ? 1.0 : 0.0;
+  } else if (!std::strcmp(key, "rebuild_rule")) {
+    *value = (double)ctx->P.pair_rule;
   } else if (!std::strcmp(key, "skin_tune")) {
     *value = ctx->skin_tune ? 1.0 : 0.0;
   } else if (!std::strcmp(key, "heavy_if")) {
@@ -1795,6 +1816,7 @@ static int build_spec_graph(fibmd_ctx* ctx) {
   ctx->graph_force_block = ctx->force_block;
   ctx->graph_build_block = ctx->build_block;
   ctx->graph_uniform = ctx->P.uniform;
+  ctx->graph_pair = ctx->P.pair_rule;
   ctx->graph_react = ctx->react ? 1 : 0;
   ctx->graph_heavy_if = ctx->heavy_if ? 1 : 0;
   return FIBMD_OK;
@@ -1894,7 +1916,8 @@ static int run_spec_graph(fibmd_ctx* ctx, long long pairs, double relax = 0.0) {
       ctx->graph_stage != ctx->stage || ctx->graph_pdl != (ctx->pdl ? 1 : 0) ||
       ctx->graph_fuse != (ctx->fuse ? 1 : 0) || ctx->graph_skin != ctx->skin_cur ||
       ctx->graph_force_block != ctx->force_block || ctx->graph_build_block != ctx->build_block ||
-      ctx->graph_uniform != ctx->P.uniform || ctx->graph_react != (ctx->react ? 1 : 0) ||
+      ctx->graph_uniform != ctx->P.uniform || ctx->graph_pair != ctx->P.pair_rule ||
+      ctx->graph_react != (ctx->react ? 1 : 0) ||
       ctx->graph_heavy_if != (ctx->heavy_if ? 1 : 0)) {
     int rc = build_spec_graph(ctx);
     if (rc && ctx->pdl) {

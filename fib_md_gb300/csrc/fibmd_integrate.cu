@@ -327,16 +327,69 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // stores. BATCH = 0 (a single system) takes the replica's geometry and
 // scalars without reading the flags first.
 
+// ---- the pair rule's reductions ----
+// The block's two largest reported |d|^2 (non-negative binary32, ordered as
+// their bit patterns) go into the step's running pair with two atomics: the
+// first atomicMax returns the running largest, and whichever of it and the
+// block's largest is smaller, like the block's second, can only be the
+// step's second or below. Called by every thread of the block.
+__device__ __forceinline__ void pair_report(DevScalars* sc, float rep) {
+  __shared__ unsigned top[2][kKickThreads / 32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const unsigned u = __float_as_uint(rep);
+  const unsigned m1 = __reduce_max_sync(0xffffffffu, u);
+  const unsigned first = __ffs(__ballot_sync(0xffffffffu, u == m1)) - 1;
+  const unsigned m2 = __reduce_max_sync(0xffffffffu, lane == (int)first ? 0u : u);
+  if (lane == 0) {
+    top[0][w] = m1;
+    top[1][w] = m2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned b1 = 0u, b2 = 0u;
+    for (int k = 0; k < kKickThreads / 32; k++) {
+      const unsigned a1 = top[0][k], a2 = top[1][k];
+      if (a1 > b1) {
+        b2 = max(b1, a2);
+        b1 = a1;
+      } else {
+        b2 = max(b2, a1);
+      }
+    }
+    const unsigned old = atomicMax(&sc->disp_top[0], b1);
+    const unsigned sec = max(min(old, b1), b2);
+    if (sec) atomicMax(&sc->disp_top[1], sec);
+  }
+}
+
+// Whether the step's reports call for a rebuild: d1 + max(d2, the bound)
+// reaching the skin, d1 >= d2 the two largest reported displacements (the
+// unreported ones are below the bound). Clears the reports for the next
+// step. One thread, after every chunk of the step has drifted.
+__device__ __forceinline__ bool pair_decide(const DevParams& P, DevScalars* sc) {
+  const unsigned a = atomicExch(&sc->disp_top[0], 0u);
+  const unsigned b = atomicExch(&sc->disp_top[1], 0u);
+  if (a == 0u) return false;
+  const float d1 = sqrtf(__uint_as_float(a));
+  const float d2 = sqrtf(fmaxf(__uint_as_float(b), P.disp_lowA2));
+  return d1 + d2 >= P.disp_skinA;
+}
+
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z (and, with an open z axis, of atoms 10 A below the lowest plane),
-// and the rebuild trigger at half the list skin: the kKickThreads atoms of
-// chunk c, one per thread. Returns, in every thread, whether an atom of the
-// chunk moved half the skin since the last list build.
+// and the rebuild trigger: the kKickThreads atoms of chunk c, one per
+// thread. Returns, in every thread, whether an atom of the chunk moved half
+// the skin since the last list build. With the pair rule (a single system)
+// it returns 0 and instead reports the chunk's two largest squared
+// displacements at or above disp_lowA2 (pair_report); the step's rebuild is
+// decided from the reports once every chunk has drifted (pair_decide).
 template <int BATCH>
 __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
   const int i = c * kKickThreads + threadIdx.x;
+  const bool pair = !BATCH && P.pair_rule;
   bool trig = false, soon = false;
+  float rep = 0.f;  // pair rule: this atom's reported |d|^2
   if (i < P.N) {
     uint32_t fl = S.flags[i];
     double4_32a x = S.pos[i];
@@ -402,11 +455,19 @@ __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevSta
       S.posq[i] = q;
       const float3 d = qsep(q, qb, G.qinvA);
       const float d2 = d.x * d.x + d.y * d.y + d.z * d.z;
-      if (!removed && d2 >= P.disp_fastA2) trig = true;
+      if (pair) {
+        if (!removed && d2 >= P.disp_lowA2) rep = d2;
+      } else if (!removed && d2 >= P.disp_fastA2) {
+        trig = true;
+      }
       // a batch also rebuilds, with a replica that must, those that have
       // moved a quarter of the skin: rebuilds stay few and in step
       if (BATCH && !removed && d2 >= 0.25f * P.disp_fastA2) soon = true;
     }
+  }
+  if (pair) {
+    if (__syncthreads_or(rep > 0.f)) pair_report(S.sc, rep);
+    return 0;
   }
   const int any = __syncthreads_or(trig) ? 1 : 0;
   if (!BATCH) return any;
@@ -436,19 +497,30 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevSta
   if (blockIdx.x == 0) reset_force_counters(S);
 }
 
-// Sets the graph's rebuild condition from the drift's flag. A kernel of its
-// own rather than a last-block ticket in the drift: a same-address atomic
-// from each of ~1000 blocks serialises in L2 for longer than a launch.
-// With has_heavy, it also closes the step's many-leg IF node (heavy), which
-// the force kernel opens when it finds such a centre.
-__global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond,
+// Sets the graph's rebuild condition from the drift's flag (or, with the
+// pair rule, from its reports). A kernel of its own rather than a last-block
+// ticket in the drift: a same-address atomic from each of ~1000 blocks
+// serialises in L2 for longer than a launch. With has_heavy, it also closes
+// the step's many-leg IF node (heavy), which the force kernel opens when it
+// finds such a centre.
+__global__ void k_spec_cond(DevParams P, DevState S, cudaGraphConditionalHandle cond,
                             cudaGraphConditionalHandle heavy, int has_heavy) {
   pdl_wait();
   pdl_trigger();
   if (threadIdx.x == 0) {
-    cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
+    int need = ((volatile DevScalars*)S.sc)->need_rebuild;
+    if (P.pair_rule && pair_decide(P, S.sc)) {
+      S.sc->need_rebuild = 1;
+      need = 1;
+    }
+    cudaGraphSetConditional(cond, need ? 1u : 0u);
     if (has_heavy) cudaGraphSetConditional(heavy, 0u);
   }
+}
+
+// The pair rule's decision outside a graph (launch by launch).
+__global__ void k_pair_decide(DevParams P, DevState S) {
+  if (threadIdx.x == 0 && pair_decide(P, S.sc)) S.sc->need_rebuild = 1;
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
@@ -460,8 +532,10 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
                            L.stream, L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
   if (e == cudaSuccess && cond)
-    e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond,
+    e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, P, S, *cond,
                  heavy ? *heavy : cudaGraphConditionalHandle(0), heavy ? 1 : 0);
+  else if (e == cudaSuccess && P.pair_rule && P.nrep == 1)
+    e = launch_k(k_pair_decide, 1, 32, 0, L.stream, false, P, S);
   return e;
 }
 
@@ -733,6 +807,18 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
         if (moved & 2) R.rep_soon = 1;
       }
       if (moved & 1) {
+        sc->need_rebuild = 1;
+        cudaGraphSetConditional(hif, 1u);
+      }
+    }
+  }
+  // the pair rule: the block that drifts last decides from every block's
+  // reports (a ticket that wraps to 0 at the grid's size)
+  if (!BATCH && P.pair_rule && threadIdx.x == 0) {
+    __threadfence();
+    if (atomicInc(&sc->disp_ticket, gridDim.x - 1) == gridDim.x - 1) {
+      __threadfence();
+      if (pair_decide(P, sc)) {
         sc->need_rebuild = 1;
         cudaGraphSetConditional(hif, 1u);
       }

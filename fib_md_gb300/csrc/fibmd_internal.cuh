@@ -106,6 +106,12 @@ struct DevParams {
   // stale-list bookkeeping
   double disp_fast2;  // squared displacement (m^2) that marks an atom fast
   float disp_fastA2;  // the same in A^2
+  // spec-mode rebuild rule of a single system: 0, any atom displaced half the
+  // skin; 1 (pair_rule), the two largest displacements together reaching the
+  // skin, atoms below disp_lowA2 counted at that bound
+  int pair_rule;
+  float disp_skinA;   // the skin (A, with the 1 % margin of disp_fast2)
+  float disp_lowA2;   // squared reporting bound of the pair rule (A^2)
   // mixed precision, reduced units (A, eV)
   float epsA[2][2], sigA[2][2], lepsA[2][2][2];
   float isigA[2][2], epssigA[2][2];  // 1/sigma (1/A), eps/sigma (eV/A)
@@ -166,6 +172,8 @@ struct DevScalars {
   unsigned long long acc_vmax2;  // spec kick: running max |v|^2 (bits), sum m v^2
   double acc_tsum;               //            and count of the thermostat layer,
   int acc_tcnt;                  //            cleared by the replica's last chunk
+  unsigned disp_top[2];  // pair rule: the two largest reported |d|^2 (float bits)
+  unsigned disp_ticket;  //            fused kick-drift: drift blocks done this step
   unsigned int ticket[8];
   unsigned long long counters[4];
 };

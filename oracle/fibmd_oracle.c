@@ -224,6 +224,7 @@ int orc_init(orc_sys* s, const fibmd_params* p) {
     if (s->rclj - rlj2 < skin) skin = s->rclj - rlj2;
     double half = 0.5 * skin * 0.99;
     s->sp_trig2 = half * half;
+    s->sp_rule = 1;
     s->sp_zopen = p->remove_z > 0.0 && p->remove_z + s->rc < s->Lb[2];
     s->sp_remove_zlo = s->sp_zopen ? -10.0e-10 : -1.0e300;
     s->sp_thermo_s = 1.0;
@@ -1301,6 +1302,10 @@ int orc_spec_step(orc_sys* s, int nthreads) {
   double qs[3];
   for (int d = 0; d < 3; d++) qs[d] = 4294967296.0 / s->Lb[d];
   int trig = 0;
+  /* the pair rule's two largest squared displacements at or above the
+     reporting bound (an eighth of the skin) */
+  const double low2 = 0.0625 * s->sp_trig2;
+  double top1 = 0.0, top2 = 0.0;
   /* drift: thermostat scaling, X += V dt + F dt^2/(2m), pinning, removal
      (on the unwrapped height), wrap of atoms that left the box, and the
      rebuild test against the positions of the last build */
@@ -1346,9 +1351,23 @@ int orc_spec_step(orc_sys* s, int nthreads) {
         e = e - f_nint(e * s->iLb[d]) * s->Lb[d];
         dd = dd + e * e;
       }
-      if (dd >= s->sp_trig2) trig = 1;
+      if (!s->sp_rule) {
+        if (dd >= s->sp_trig2) trig = 1;
+      } else if (dd >= low2) {
+        if (dd > top1) {
+          top2 = top1;
+          top1 = dd;
+        } else if (dd > top2) {
+          top2 = dd;
+        }
+      }
     }
   }
+  /* a pair outside the list radius at the build comes within the cutoff
+     only once the two atoms' displacements add up to the skin */
+  if (s->sp_rule && top1 > 0.0 &&
+      sqrt(top1) + sqrt(top2 > low2 ? top2 : low2) >= 2.0 * sqrt(s->sp_trig2))
+    trig = 1;
   if (trig || s->sp_force_rebuild) {
     orc_si_nlist(s, s->X);
     s->sp_rebuilds++;
@@ -1374,6 +1393,8 @@ int orc_spec_step(orc_sys* s, int nthreads) {
   spec_reduce(s);
   return trig;
 }
+
+void orc_spec_set_rule(orc_sys* s, int rule) { s->sp_rule = rule ? 1 : 0; }
 
 void orc_spec_scalars(orc_sys* s, double* out7) {
   out7[0] = s->sp_time;

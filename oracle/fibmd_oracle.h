@@ -82,6 +82,7 @@ typedef struct orc_sys {
   double sp_time, sp_vmax2;    /* simulated time, max |v|^2 of the last kick */
   double sp_remove_zlo;        /* atoms below are removed (open z axis)      */
   double sp_trig2;             /* squared half skin: the rebuild trigger     */
+  int sp_rule;                 /* 1: pair rule (default), 0: half skin        */
   int sp_zopen;                /* z is an open axis (not wrapped)            */
   int sp_force_rebuild;        /* the next step rebuilds the lists           */
   int sp_removed, sp_ions_removed;
@@ -164,6 +165,11 @@ void orc_spec_init(orc_sys* s, const unsigned* tags, double time0);
 /* One spec-mode step (nthreads > 1: the OpenMP force). Returns 1 when the
    lists were rebuilt in it. */
 int orc_spec_step(orc_sys* s, int nthreads);
+/* The rebuild rule: 1 (the default), rebuild when the two largest
+   displacements since the last build add up to the skin (those under an
+   eighth of the skin counted at that bound); 0, when any atom's reaches half
+   the skin. Both with the 1 % margin of the skin. */
+void orc_spec_set_rule(orc_sys* s, int rule);
 /* time, dt, thermostat factor, vmax2, removed lattice atoms, removed ions,
    rebuilds since orc_spec_init */
 void orc_spec_scalars(orc_sys* s, double* out7);

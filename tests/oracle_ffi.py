@@ -98,6 +98,7 @@ _SIG = {
     "orc_knock": (None, [_VP, _VP, C.c_int, C.c_double, C.c_double, C.c_double, _DP, C.c_int]),
     "orc_spec_init": (None, [_VP, C.POINTER(C.c_uint), C.c_double]),
     "orc_spec_step": (C.c_int, [_VP, C.c_int]),
+    "orc_spec_set_rule": (None, [_VP, C.c_int]),
     "orc_spec_scalars": (None, [_VP, _DP]),
     "orc_spec_tags": (C.POINTER(C.c_uint), [_VP]),
     "orc_spec_inject": (None, [_VP, C.c_int, _DP, _DP]),
@@ -327,6 +328,11 @@ class Oracle:
     def spec_step(self, nthreads: int = 0) -> bool:
         """One spec-mode step; True when it rebuilt the lists."""
         return bool(lib().orc_spec_step(self.h, nthreads))
+
+    def set_rebuild_rule(self, rule: int) -> None:
+        """1 (the default): rebuild when the two largest displacements since
+        the build reach the skin; 0: when any reaches half the skin."""
+        lib().orc_spec_set_rule(self.h, int(rule))
 
     def spec_scalars(self) -> dict:
         out = (C.c_double * 7)()

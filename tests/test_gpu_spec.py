@@ -442,3 +442,56 @@ def test_fused_barrier_timeout_is_reported(gpu_lib):
     X, _, _ = g.download()
     assert lt == 20 and t > 0 and np.isfinite(X).all()
     g.close()
+
+
+@pytest.mark.parametrize("path", ["plain", "graph", "fused"])
+def test_pair_rule_lists_complete(gpu_lib, path):
+    """The pair rule (rebuild once the two largest displacements since the
+    build add up to the skin) on a 2 keV cascade, decided launch by launch,
+    in the unfused graph's condition kernel and in the fused kick-drift's
+    last block: after each of three calls of 40 steps the SW list holds
+    every pair inside the cutoff 0.999 a sigma and the Moliere list every
+    ion pair inside 2.5 sigma (minimum image in x and y); the run is the
+    half-skin rule's (positions within 1e-8 A) with fewer rebuilds."""
+    s, X, V = _spec_system(precision=0)
+    p = s.params
+    sig = max(p.sigmaSi, p.sigmaGe)
+    Lb = np.array(p.Lb[:])
+    nsg = p.Nsg
+    ctxs = {}
+    for rule in (1, 0):
+        g = _ctx(s, X, V, 0, graph=path != "plain")
+        g.set_option("rebuild_rule", rule)
+        if path == "graph":
+            g.set_option("fuse", 0)
+        assert g.get_option("rebuild_rule") == rule
+        ctxs[rule] = g
+    g = ctxs[1]
+    assert g.get_option("fuse") == (1 if path == "fused" else 0) or path == "plain"
+    lt = {0: 0, 1: 0}
+    t = {0: 0.0, 1: 0.0}
+    for call in range(3):
+        for rule, c in ctxs.items():
+            lt[rule], t[rule], _, _ = c.steps(2, 40, lt[rule], t[rule], 300.0)
+        Xg, _, _ = g.download()
+        sw = {tuple(q) for q in g.get_pairs(0)}
+        mol = {tuple(q) for q in g.get_pairs(1)}
+        for a in range(p.Natm - 1):
+            d = Xg[a + 1:] - Xg[a]
+            d[:, :2] -= Lb[:2] * np.rint(d[:, :2] / Lb[:2])
+            r2 = np.einsum("ij,ij->i", d, d)
+            if a < nsg:
+                close = np.nonzero(r2[: nsg - a - 1] < (0.999 * p.al * sig) ** 2)[0]
+                for c in close:
+                    assert (a + 1, a + 2 + c) in sw, (call, a, c)
+            near = np.nonzero(r2 < (2.5 * sig) ** 2)[0]
+            for c in near:
+                if a >= nsg or a + 1 + c >= nsg:
+                    assert (a + 1, a + 2 + c) in mol, (call, a, c)
+    X1, _, _ = ctxs[1].download()
+    X0, _, _ = ctxs[0].download()
+    assert lt[0] == lt[1] == 120 and abs(t[1] - t[0]) <= 1e-12 * t[0]
+    assert np.abs(X1 - X0).max() < 1e-18
+    assert 1 < ctxs[1].work_counters()[4] < ctxs[0].work_counters()[4]
+    for c in ctxs.values():
+        c.close()

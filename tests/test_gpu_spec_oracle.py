@@ -5,7 +5,9 @@ Both sides start from the same seeded state (the oracle's own set-up,
 oracle_ffi.spec_slab, which equals the GPU package's spec_slab bit for bit)
 and run the same step: thermostat scaling of the tagged layer, drift,
 pinning of the frozen layers, removal above remove_z (and 10 A below z = 0
-with z an open axis), the half-skin rebuild test, force, kick, and the next
+with z an open axis), the rebuild test (by default the pair rule: the two
+largest displacements since the build reach the skin; or any atom's
+reaching half of it), force, kick, and the next
 dt = min(1 fs, 0.05 A / max|v|). Bars: positions within 1e-8 A after 100
 steps, the dt of every step within 1e-12 relative, the same steps
 rebuilding the lists, the same atoms removed; forces per atom within 1e-10
@@ -41,7 +43,7 @@ def slab_8x8x8(ion_height_A=10.0, skin_A=0.6, cells=(8, 8, 8), seed=1001, eV=500
                         remove_above=remove_above_A * 1e-10, params=p)
 
 
-def gpu_ctx(slab, graph=False, precision=0):
+def gpu_ctx(slab, graph=False, precision=0, rule=1):
     import fib_md_gb300 as fm
 
     p = slab["params"].copy()
@@ -53,6 +55,7 @@ def gpu_ctx(slab, graph=False, precision=0):
     g.set_tags(slab["tags"])
     g.set_impact(1)
     g.set_option("graph", 1 if graph else 0)
+    g.set_option("rebuild_rule", rule)
     g.si_nlist()
     g.si_force()
     return g
@@ -89,13 +92,15 @@ def check_runs(o, g, rec_o, rec_g):
     return dx
 
 
-@pytest.mark.parametrize("ion_height_A", [10.0, 1.5])
-def test_spec_trajectory_8x8x8(gpu_lib, ion_height_A):
+@pytest.mark.parametrize("ion_height_A,rule", [(10.0, 1), (1.5, 1), (1.5, 0)])
+def test_spec_trajectory_8x8x8(gpu_lib, ion_height_A, rule):
     """The 8x8x8-cell slab for 100 steps: with the ion 10 A up (the
-    approach) and 1.5 A up (the first 100 steps of the cascade)."""
+    approach) and 1.5 A up (the first 100 steps of the cascade), under the
+    pair rule and (the cascade) the half-skin rule."""
     slab = slab_8x8x8(ion_height_A=ion_height_A)
     o = of.spec_oracle(slab)
-    g = gpu_ctx(slab)
+    o.set_rebuild_rule(rule)
+    g = gpu_ctx(slab, rule=rule)
     F0 = g.si_force()
     assert per_atom_err(F0, o.F) < FORCE_RTOL
     rec_o, rec_g = step_both(o, g, 100)
@@ -105,11 +110,13 @@ def test_spec_trajectory_8x8x8(gpu_lib, ion_height_A):
         # the cascade has started: the ion has lost speed to the lattice
         assert rec_o[-1, 1] > 1.05 * rec_o[0, 1]
     # the CUDA-graph step loop runs the same 100 steps
-    g2 = gpu_ctx(slab, graph=True)
+    g2 = gpu_ctx(slab, graph=True, rule=rule)
     lt, t, _, _ = g2.steps(2, 100, 0, 0.0, 300.0)
     X2, _, _ = g2.download()
     assert lt == 100 and abs(t - rec_o[-1, 0]) <= DT_RTOL * rec_o[-1, 0]
     assert np.abs(X2 - o.X).max() < TRAJ_ATOL_M
+    # the graph's fused kick-drift decides the rebuilds in its last block
+    assert g2.work_counters()[4] == g.work_counters()[4]
     g.close()
     g2.close()
     o.close()

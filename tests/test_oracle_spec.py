@@ -194,3 +194,40 @@ def test_spec_energy_conservation():
     assert o.spec_scalars()["time"] == pytest.approx(400e-15, rel=1e-12)
     assert abs(E1 - E0) / o.p.ec / nsg < 2e-4
     o.close()
+
+
+def test_pair_rule_keeps_lists_complete():
+    """The two rebuild rules on the same 800 eV cascade (100 steps): with
+    the pair rule (rebuild once the two largest displacements since the
+    build add up to the skin) the lists at every step still hold each
+    lattice pair inside the SW cutoff 0.999 a sigma and each ion pair inside
+    2.5 sigma at the step's positions; the two runs are the same trajectory
+    (only the force sums' order differs with the lists), and the pair rule
+    rebuilds less often."""
+    slab = _small()
+    p = slab["params"]
+    nsg = p.Nsg
+    Lb = np.array(p.Lb[:])
+    sig = max(p.sigmaSi, p.sigmaGe)
+    lat = np.zeros(p.Natm, bool)
+    lat[:nsg] = True
+    ion = slab["atype"] == 3
+    runs = {}
+    for rule in (0, 1):
+        o = of.spec_oracle(slab)
+        o.set_rebuild_rule(rule)
+        for n in range(100):
+            o.spec_step()
+            if rule == 1:
+                keep = (o.spec_tags() & of.TAG_REMOVED) == 0
+                sw = {tuple(q) for q in o.pairs(0)}
+                need = _pairs_within(o.X, Lb, 0.999 * p.al * sig, np.ones(p.Natm, bool), keep & lat)
+                assert all(tuple(q) in sw for q in need), n
+                mol = {tuple(q) for q in o.pairs(1)}
+                need = _pairs_within(o.X, Lb, 2.5 * sig, ion, keep)
+                assert all(tuple(q) in mol for q in need), n
+        runs[rule] = (o.X.copy(), o.spec_scalars()["rebuilds"])
+        o.close()
+    (X0, rb0), (X1, rb1) = runs[0], runs[1]
+    assert np.abs(X1 - X0).max() < 1e-18
+    assert 0 < rb1 < rb0
