@@ -114,9 +114,9 @@ struct fibmd_ctx {
   // the graph's kick of each step fused with the next step's drift (option
   // "fuse"), in a grid of at most kd_blocks resident blocks
   bool fuse = true;
-  // spec-mode rebuild rule of a single system (option "rebuild_rule"): 1, the
-  // two largest displacements since the build reach the skin; 0, any atom's
-  // displacement reaches half the skin (a batch always takes 0 per replica)
+  // spec-mode rebuild rule (option "rebuild_rule"), per replica in a batch:
+  // 1, the two largest displacements since the build reach the skin; 0, any
+  // atom's displacement reaches half the skin
   int rebuild_rule = 1;
   int kd_blocks = 0;       // resident blocks of the fused kernel (0: unavailable)
   int kd_grid = 0;         // option "kd_grid": its grid size instead (tests)
@@ -596,7 +596,6 @@ static int derive_skin(const fibmd_ctx* ctx, double skin, fibmd_ctx::SkinSet& ou
     return FIBMD_EINVAL;
   }
   out.P.nrep = nrep;
-  if (nrep > 1) out.P.pair_rule = 0;
   out.P.nion = (int)nion;
   out.P.nfired = q.Natm;
   out.P.ncell = (int)cells;
@@ -1119,7 +1118,7 @@ int fibmd_gpu_upload(fibmd_ctx* ctx, const double* X, const double* V, const dou
   CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemsetAsync(&ctx->S.sc->nan_flag, 0, sizeof(int), ctx->stream));
   CK(cudaMemsetAsync(&ctx->S.sc->kd_timeout, 0, sizeof(int), ctx->stream));
-  CK(cudaMemsetAsync(&ctx->S.sc->disp_top[0], 0, 3 * sizeof(unsigned), ctx->stream));
+  CK(launch_pair_clear(L, ctx->P, ctx->S));
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->uploaded = true;
   ctx->spec_ready = false;
@@ -1478,7 +1477,7 @@ int fibmd_gpu_set_option(fibmd_ctx* ctx, const char* key, double value) {
   } else if (!std::strcmp(key, "rebuild_rule")) {
     if (value != 0.0 && value != 1.0) return fail(ctx, FIBMD_EINVAL, "rebuild_rule must be 0 or 1");
     ctx->rebuild_rule = (int)value;
-    const int pr = (ctx->rebuild_rule == 1 && ctx->p.mode == FIBMD_MODE_SPEC && ctx->P.nrep == 1);
+    const int pr = (ctx->rebuild_rule == 1 && ctx->p.mode == FIBMD_MODE_SPEC) ? 1 : 0;
     ctx->P.pair_rule = pr;
     for (auto& k : ctx->skins) k.P.pair_rule = pr;
   } else if (!std::strcmp(key, "skin_tune")) {

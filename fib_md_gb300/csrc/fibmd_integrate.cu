@@ -362,17 +362,44 @@ __device__ __forceinline__ void pair_report(DevScalars* sc, float rep) {
   }
 }
 
-// Whether the step's reports call for a rebuild: d1 + max(d2, the bound)
-// reaching the skin, d1 >= d2 the two largest reported displacements (the
-// unreported ones are below the bound). Clears the reports for the next
-// step. One thread, after every chunk of the step has drifted.
-__device__ __forceinline__ bool pair_decide(const DevParams& P, DevScalars* sc) {
-  const unsigned a = atomicExch(&sc->disp_top[0], 0u);
-  const unsigned b = atomicExch(&sc->disp_top[1], 0u);
-  if (a == 0u) return false;
+// What a replica's reports call for: 2, a rebuild (d1 + max(d2, the bound)
+// reaching the skin, d1 >= d2 the two largest reported displacements; the
+// unreported ones are below the bound); 1, half that sum reached (a batch
+// rebuilds such replicas with those that must, as the half-skin rule does
+// those that moved a quarter of the skin); 0, neither. Clears the reports
+// for the next step.
+__device__ __forceinline__ int pair_decide(const DevParams& P, DevScalars* R) {
+  const unsigned a = atomicExch(&R->disp_top[0], 0u);
+  const unsigned b = atomicExch(&R->disp_top[1], 0u);
+  if (a == 0u) return 0;
   const float d1 = sqrtf(__uint_as_float(a));
   const float d2 = sqrtf(fmaxf(__uint_as_float(b), P.disp_lowA2));
-  return d1 + d2 >= P.disp_skinA;
+  const float sum = d1 + d2;
+  return sum >= P.disp_skinA ? 2 : (sum >= 0.5f * P.disp_skinA ? 1 : 0);
+}
+
+// The pair rule's decisions of every replica, shared out over the nt
+// threads of one block (thread t takes replicas t, t + nt, ...), after the
+// whole step has drifted; sets each replica's flags and returns, in every
+// thread, whether any replica rebuilds. Called by every thread of the block.
+__device__ __forceinline__ bool pair_decide_all(const DevParams& P, const DevState& S) {
+  bool need = false;
+  for (int r = threadIdx.x; r < P.nrep; r += blockDim.x) {
+    DevScalars* R = S.sc + r;
+    const int k = pair_decide(P, R);
+    if (k == 2) {
+      R->rep_rebuild = 1;
+      need = true;
+    } else if (k == 1) {
+      R->rep_soon = 1;
+    }
+  }
+  return __syncthreads_or(need) != 0;
+}
+
+// Threads of the block that takes the pair rule's decisions.
+inline int pair_decide_threads(const DevParams& P) {
+  return P.nrep > 1 ? std::min(1024, (P.nrep + 31) / 32 * 32) : 32;
 }
 
 // Drift with the variable step held on the device, Berendsen scaling of the
@@ -382,14 +409,16 @@ __device__ __forceinline__ bool pair_decide(const DevParams& P, DevScalars* sc) 
 // thread. Returns, in every thread, whether an atom of the chunk moved half
 // the skin since the last list build. With the pair rule (a single system)
 // it returns 0 and instead reports the chunk's two largest squared
-// displacements at or above disp_lowA2 (pair_report); the step's rebuild is
-// decided from the reports once every chunk has drifted (pair_decide).
+// displacements at or above disp_lowA2 to its replica (pair_report); the
+// step's rebuilds are decided from the reports once every chunk has drifted
+// (pair_decide_all).
 template <int BATCH>
 __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
   const int i = c * kKickThreads + threadIdx.x;
-  const bool pair = !BATCH && P.pair_rule;
+  const bool pair = P.pair_rule;
   bool trig = false, soon = false;
-  float rep = 0.f;  // pair rule: this atom's reported |d|^2
+  float rep = 0.f;                 // pair rule: this atom's reported |d|^2
+  DevScalars* Rrep = S.sc;         // and its replica's scalars
   if (i < P.N) {
     uint32_t fl = S.flags[i];
     double4_32a x = S.pos[i];
@@ -401,6 +430,7 @@ __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevSta
     const int r = BATCH ? rep_of_flags(fl) : 0;
     const Geo& G = S.geo[r];
     DevScalars* R = S.sc + r;
+    Rrep = R;
     const double dt = R->dt;
     const double h2 = R->half_dt2;
     const double ts = R->thermo_s;
@@ -466,7 +496,8 @@ __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevSta
     }
   }
   if (pair) {
-    if (__syncthreads_or(rep > 0.f)) pair_report(S.sc, rep);
+    // thread 0 holds the chunk's first atom, of the chunk's replica
+    if (__syncthreads_or(rep > 0.f)) pair_report(Rrep, rep);
     return 0;
   }
   const int any = __syncthreads_or(trig) ? 1 : 0;
@@ -507,9 +538,10 @@ __global__ void k_spec_cond(DevParams P, DevState S, cudaGraphConditionalHandle 
                             cudaGraphConditionalHandle heavy, int has_heavy) {
   pdl_wait();
   pdl_trigger();
+  const bool pair_need = P.pair_rule && pair_decide_all(P, S);
   if (threadIdx.x == 0) {
     int need = ((volatile DevScalars*)S.sc)->need_rebuild;
-    if (P.pair_rule && pair_decide(P, S.sc)) {
+    if (pair_need) {
       S.sc->need_rebuild = 1;
       need = 1;
     }
@@ -518,9 +550,25 @@ __global__ void k_spec_cond(DevParams P, DevState S, cudaGraphConditionalHandle 
   }
 }
 
-// The pair rule's decision outside a graph (launch by launch).
+// The pair rule's decisions outside a graph (launch by launch).
 __global__ void k_pair_decide(DevParams P, DevState S) {
-  if (threadIdx.x == 0 && pair_decide(P, S.sc)) S.sc->need_rebuild = 1;
+  if (pair_decide_all(P, S) && threadIdx.x == 0) S.sc->need_rebuild = 1;
+}
+
+// Clears every replica's pair-rule reports and the fused kernel's ticket
+// (a new state).
+__global__ void k_pair_clear(DevState S, int nrep) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < nrep) {
+    S.sc[r].disp_top[0] = 0u;
+    S.sc[r].disp_top[1] = 0u;
+    S.sc[r].disp_ticket = 0u;
+  }
+}
+
+cudaError_t launch_pair_clear(const Launch& L, const DevParams& P, const DevState& S) {
+  k_pair_clear<<<(P.nrep + 255) / 256, 256, 0, L.stream>>>(S, P.nrep);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
@@ -531,11 +579,12 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
   cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, kKickThreads, 0,
                            L.stream, L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
+  const int nt = pair_decide_threads(P);
   if (e == cudaSuccess && cond)
-    e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, P, S, *cond,
+    e = launch_k(k_spec_cond, 1, nt, 0, L.stream, L.pdl, P, S, *cond,
                  heavy ? *heavy : cudaGraphConditionalHandle(0), heavy ? 1 : 0);
-  else if (e == cudaSuccess && P.pair_rule && P.nrep == 1)
-    e = launch_k(k_pair_decide, 1, 32, 0, L.stream, false, P, S);
+  else if (e == cudaSuccess && P.pair_rule)
+    e = launch_k(k_pair_decide, 1, nt, 0, L.stream, false, P, S);
   return e;
 }
 
@@ -814,14 +863,17 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
   }
   // the pair rule: the block that drifts last decides from every block's
   // reports (a ticket that wraps to 0 at the grid's size)
-  if (!BATCH && P.pair_rule && threadIdx.x == 0) {
-    __threadfence();
-    if (atomicInc(&sc->disp_ticket, gridDim.x - 1) == gridDim.x - 1) {
+  if (P.pair_rule) {
+    __shared__ int last;
+    if (threadIdx.x == 0) {
       __threadfence();
-      if (pair_decide(P, sc)) {
-        sc->need_rebuild = 1;
-        cudaGraphSetConditional(hif, 1u);
-      }
+      last = atomicInc(&sc->disp_ticket, gridDim.x - 1) == gridDim.x - 1;
+      if (last) __threadfence();
+    }
+    __syncthreads();
+    if (last && pair_decide_all(P, S) && threadIdx.x == 0) {
+      sc->need_rebuild = 1;
+      cudaGraphSetConditional(hif, 1u);
     }
   }
 }

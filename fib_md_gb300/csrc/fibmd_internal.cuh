@@ -106,7 +106,7 @@ struct DevParams {
   // stale-list bookkeeping
   double disp_fast2;  // squared displacement (m^2) that marks an atom fast
   float disp_fastA2;  // the same in A^2
-  // spec-mode rebuild rule of a single system: 0, any atom displaced half the
+  // spec-mode rebuild rule (per replica): 0, any atom displaced half the
   // skin; 1 (pair_rule), the two largest displacements together reaching the
   // skin, atoms below disp_lowA2 counted at that bound
   int pair_rule;
@@ -525,6 +525,7 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // pdl_first: the drift may itself be launched as a programmatic dependent of
 // the kernel before it (a kick); the condition kernel always is (L.pdl)
 // heavy (with cond): the IF handle of the step's many-leg kernel, closed here
+cudaError_t launch_pair_clear(const Launch& L, const DevParams& P, const DevState& S);
 cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevState& S,
                               double Ttar, const cudaGraphConditionalHandle* cond = nullptr,
                               bool pdl_first = false,

@@ -307,11 +307,13 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    invalid until the next upload) and "kd_grid" (that kernel's grid; 0, the
    default, is the number of its blocks the device holds at once, which
    every wait relies on; a larger value makes the waits give up, a hook for
-   testing the time-out), "rebuild_rule" (spec mode, a single system:
-   default 1, the lists are rebuilt once the two largest displacements
-   since the last build add up to the skin, those under an eighth of it
-   counted at that bound; 0, once any atom's displacement reaches half the
-   skin; a batch context always takes 0 per replica and reads 0), "skin_tune" (default 1: in spec-mode calls of at
+   testing the time-out), "rebuild_rule" (spec mode, per replica in a
+   batch: default 1, the lists are rebuilt once the two largest
+   displacements since the last build add up to the skin, those under an
+   eighth of it counted at that bound, and in a batch with them those of
+   the replicas whose sum has reached half the skin; 0, once any atom's
+   displacement reaches half the skin, in a batch with those that moved a
+   quarter of it), "skin_tune" (default 1: in spec-mode calls of at
    least 2000 steps, before every 5000 steps, each candidate list skin runs
    one step pair and then 20 timed pairs of the graph step loop, and the
    fastest per step is kept; the trial steps are steps of the run, and the

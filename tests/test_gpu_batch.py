@@ -36,11 +36,13 @@ def _single(sl, steps):
     return X, V, t
 
 
-def _batch(slabs, steps):
+def _batch(slabs, steps, rule=None):
     import fib_md_gb300 as fm
 
     reps = [(s.params.Natm, s.params.Nsg, list(s.params.Lb), s.params.remove_z) for s in slabs]
     b = fm.FibMDBatch(slabs[0].params, reps)
+    if rule is not None:
+        b.set_option("rebuild_rule", rule)
     X = b.pad([s.X for s in slabs])
     V = b.pad([s.V for s in slabs])
     Xi = b.pad([s.Xi for s in slabs])
@@ -117,14 +119,17 @@ def test_impact_stats_on_device(gpu_lib):
     b.close()
 
 
-def test_batch_lists_hold_every_pair(gpu_lib):
+@pytest.mark.parametrize("rule", [1, 0])
+def test_batch_lists_hold_every_pair(gpu_lib, rule):
     """After 150 steps of the three cascades in one batch, whose replicas
-    rebuild their SW lists separately (those that moved half the skin and
-    those that moved a quarter), every replica's list still holds each pair
-    of its atoms inside the SW cutoff 0.999*a*sigma at the current positions
-    (minimum image in x and y), and no pair across replicas."""
+    rebuild their SW lists separately (under the pair rule those whose two
+    largest displacements reach the skin and those halfway there; under
+    the half-skin rule those that moved half the skin and those that moved
+    a quarter), every replica's list still holds each pair of its atoms
+    inside the SW cutoff 0.999*a*sigma at the current positions (minimum
+    image in x and y), and no pair across replicas."""
     slabs = _slabs(1)
-    b, Xb, Vb, tb, X0 = _batch(slabs, 150)
+    b, Xb, Vb, tb, X0 = _batch(slabs, 150, rule)
     listed = {tuple(p) for p in b.get_pairs(0)}
     tags = b.get_tags()
     lo = [int(b.offsets[r]) for r in range(b.nrep)]
@@ -151,3 +156,23 @@ def test_batch_lists_hold_every_pair(gpu_lib):
                 assert (lo[r] + a + 1, lo[r] + a + 2 + c) in listed, (r, a, c)
         assert need > nsg  # about 2 bonds per atom in a diamond lattice
     b.close()
+
+
+def test_batch_pair_rule_fewer_rebuilds(gpu_lib):
+    """The same 150 steps of the three cascades under both rules: the same
+    motion (binary64: positions within 1e-6 A, the order of the force sums
+    aside) with fewer list builds under the pair rule."""
+    slabs = _slabs(0)
+    runs = {}
+    for rule in (1, 0):
+        b, Xb, Vb, tb, X0 = _batch(slabs, 150, rule)
+        runs[rule] = (Xb, tb, b.work_counters()[4], [b.rows(r) for r in range(b.nrep)])
+        b.close()
+    (X1, t1, rb1, rows), (X0, t0, rb0, _) = runs[1], runs[0]
+    assert np.all(np.abs(t1 - t0) <= 1e-10 * t0)
+    for r, sl in enumerate(slabs):
+        Lb = np.array(sl.params.Lb[:])
+        d = X1[rows[r]] - X0[rows[r]]
+        d[:, :2] -= Lb[:2] * np.rint(d[:, :2] / Lb[:2])
+        assert np.abs(d).max() < 1e-16, (r, np.abs(d).max())
+    assert 1 < rb1 < rb0, (rb1, rb0)
