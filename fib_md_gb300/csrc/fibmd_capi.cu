@@ -492,10 +492,11 @@ int derive_dev_params(const fibmd_params& p, int impact, double umax, int tab_la
   P.disp_fastA2 = (float)(half * half * 1e20);
   // the pair rule: a pair outside the list radius at the build comes within
   // the cutoff only once the two atoms' displacements add up to the skin;
-  // displacements under an eighth of it are counted at that bound
+  // displacements under a quarter of it are counted at that bound (so that
+  // the thermal atoms of a slab report nothing for most of a list's life)
   P.pair_rule = 0;
   P.disp_skinA = (float)(2.0 * half * 1e10);
-  P.disp_lowA2 = (float)((0.25 * half * 1e10) * (0.25 * half * 1e10));
+  P.disp_lowA2 = (float)((0.5 * half * 1e10) * (0.5 * half * 1e10));
   // binary32 reduced units
   for (int a = 0; a < 2; a++)
     for (int b = 0; b < 2; b++) {

@@ -327,13 +327,22 @@ cudaError_t launch_energy_sum(const Launch& L, const DevParams& P, const DevStat
 // stores. BATCH = 0 (a single system) takes the replica's geometry and
 // scalars without reading the flags first.
 
-// ---- the pair rule's reductions ----
-// The block's two largest reported |d|^2 (non-negative binary32, ordered as
-// their bit patterns) go into the step's running pair with two atomics: the
-// first atomicMax returns the running largest, and whichever of it and the
-// block's largest is smaller, like the block's second, can only be the
-// step's second or below. Called by every thread of the block.
-__device__ __forceinline__ void pair_report(DevScalars* sc, float rep) {
+// ---- the pair rule, decided where the displacements are ----
+// The chunk's two largest reported |d|^2 b1 >= b2 (non-negative binary32,
+// ordered as their bit patterns) and one atomicMax on the replica's running
+// largest of the step, which returns the largest reported before: the
+// chunk's candidate pair is (max(b1, old), max(min(b1, old), b2)). The
+// step's two largest t1 >= t2 are the candidate pair of the chunk holding
+// both, or of the later of the two chunks holding them (the running largest
+// it sees is the other one), and no chunk's pair exceeds them, so some chunk
+// reaches each threshold exactly when (t1, t2) does: the rule needs no pass
+// after the drift. Returns, in thread 0: 2, a rebuild (sqrt(p1) +
+// sqrt(max(p2, the bound)) reaching the skin; the unreported displacements
+// are below the bound); 1, half of it reached (a batch rebuilds such
+// replicas with those that must, as the half-skin rule does those that
+// moved a quarter of the skin); 0, neither. Called by every thread of the
+// block; the kick's last chunk clears the running largest for the next step.
+__device__ __forceinline__ int pair_report(const DevParams& P, DevScalars* R, float rep) {
   __shared__ unsigned top[2][kKickThreads / 32];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned u = __float_as_uint(rep);
@@ -345,73 +354,34 @@ __device__ __forceinline__ void pair_report(DevScalars* sc, float rep) {
     top[1][w] = m2;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned b1 = 0u, b2 = 0u;
-    for (int k = 0; k < kKickThreads / 32; k++) {
-      const unsigned a1 = top[0][k], a2 = top[1][k];
-      if (a1 > b1) {
-        b2 = max(b1, a2);
-        b1 = a1;
-      } else {
-        b2 = max(b2, a1);
-      }
+  if (threadIdx.x != 0) return 0;
+  unsigned b1 = 0u, b2 = 0u;
+  for (int k = 0; k < kKickThreads / 32; k++) {
+    const unsigned a1 = top[0][k], a2 = top[1][k];
+    if (a1 > b1) {
+      b2 = max(b1, a2);
+      b1 = a1;
+    } else {
+      b2 = max(b2, a1);
     }
-    const unsigned old = atomicMax(&sc->disp_top[0], b1);
-    const unsigned sec = max(min(old, b1), b2);
-    if (sec) atomicMax(&sc->disp_top[1], sec);
   }
-}
-
-// What a replica's reports call for: 2, a rebuild (d1 + max(d2, the bound)
-// reaching the skin, d1 >= d2 the two largest reported displacements; the
-// unreported ones are below the bound); 1, half that sum reached (a batch
-// rebuilds such replicas with those that must, as the half-skin rule does
-// those that moved a quarter of the skin); 0, neither. Clears the reports
-// for the next step.
-__device__ __forceinline__ int pair_decide(const DevParams& P, DevScalars* R) {
-  const unsigned a = atomicExch(&R->disp_top[0], 0u);
-  const unsigned b = atomicExch(&R->disp_top[1], 0u);
-  if (a == 0u) return 0;
-  const float d1 = sqrtf(__uint_as_float(a));
-  const float d2 = sqrtf(fmaxf(__uint_as_float(b), P.disp_lowA2));
-  const float sum = d1 + d2;
+  const unsigned old = atomicMax(&R->disp_max, b1);
+  const float p1 = __uint_as_float(max(b1, old));
+  const float p2 = __uint_as_float(max(min(b1, old), b2));
+  const float sum = sqrtf(p1) + sqrtf(fmaxf(p2, P.disp_lowA2));
   return sum >= P.disp_skinA ? 2 : (sum >= 0.5f * P.disp_skinA ? 1 : 0);
-}
-
-// The pair rule's decisions of every replica, shared out over the nt
-// threads of one block (thread t takes replicas t, t + nt, ...), after the
-// whole step has drifted; sets each replica's flags and returns, in every
-// thread, whether any replica rebuilds. Called by every thread of the block.
-__device__ __forceinline__ bool pair_decide_all(const DevParams& P, const DevState& S) {
-  bool need = false;
-  for (int r = threadIdx.x; r < P.nrep; r += blockDim.x) {
-    DevScalars* R = S.sc + r;
-    const int k = pair_decide(P, R);
-    if (k == 2) {
-      R->rep_rebuild = 1;
-      need = true;
-    } else if (k == 1) {
-      R->rep_soon = 1;
-    }
-  }
-  return __syncthreads_or(need) != 0;
-}
-
-// Threads of the block that takes the pair rule's decisions.
-inline int pair_decide_threads(const DevParams& P) {
-  return P.nrep > 1 ? std::min(1024, (P.nrep + 31) / 32 * 32) : 32;
 }
 
 // Drift with the variable step held on the device, Berendsen scaling of the
 // tagged thermostat layer, fixed-layer pinning, removal of atoms above
 // remove_z (and, with an open z axis, of atoms 10 A below the lowest plane),
 // and the rebuild trigger: the kKickThreads atoms of chunk c, one per
-// thread. Returns, in every thread, whether an atom of the chunk moved half
-// the skin since the last list build. With the pair rule (a single system)
-// it returns 0 and instead reports the chunk's two largest squared
-// displacements at or above disp_lowA2 to its replica (pair_report); the
-// step's rebuilds are decided from the reports once every chunk has drifted
-// (pair_decide_all).
+// thread. Returns, in every thread, bit 0 if an atom of the chunk moved half
+// the skin since the last list build and (a batch) bit 1 if one moved a
+// quarter of it. With the pair rule the chunk's two largest squared
+// displacements at or above disp_lowA2 decide the same bits instead
+// (pair_report: a rebuild of the replica, one halfway due), in thread 0
+// only, which is where the callers read them.
 template <int BATCH>
 __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevState& S, int c) {
   const int i = c * kKickThreads + threadIdx.x;
@@ -497,8 +467,9 @@ __device__ __forceinline__ int spec_drift_chunk(const DevParams& P, const DevSta
   }
   if (pair) {
     // thread 0 holds the chunk's first atom, of the chunk's replica
-    if (__syncthreads_or(rep > 0.f)) pair_report(Rrep, rep);
-    return 0;
+    if (!__syncthreads_or(rep > 0.f)) return 0;
+    const int k = pair_report(P, Rrep, rep);
+    return k == 2 ? 3 : (k == 1 ? 2 : 0);
   }
   const int any = __syncthreads_or(trig) ? 1 : 0;
   if (!BATCH) return any;
@@ -513,7 +484,7 @@ __device__ __forceinline__ void reset_force_counters(const DevState& S) {
 }
 
 template <int BATCH>
-__global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevState S) {
+__global__ void __launch_bounds__(kKickThreads, 6) k_spec_drift(DevParams P, DevState S) {
   pdl_wait();
   pdl_trigger();
   const int moved = spec_drift_chunk<BATCH>(P, S, blockIdx.x);
@@ -528,42 +499,26 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_drift(DevParams P, DevSta
   if (blockIdx.x == 0) reset_force_counters(S);
 }
 
-// Sets the graph's rebuild condition from the drift's flag (or, with the
-// pair rule, from its reports). A kernel of its own rather than a last-block
-// ticket in the drift: a same-address atomic from each of ~1000 blocks
-// serialises in L2 for longer than a launch. With has_heavy, it also closes
-// the step's many-leg IF node (heavy), which the force kernel opens when it
-// finds such a centre.
-__global__ void k_spec_cond(DevParams P, DevState S, cudaGraphConditionalHandle cond,
+// Sets the graph's rebuild condition from the drift's flag. A kernel of its
+// own rather than a last-block ticket in the drift: a same-address atomic
+// from each of ~1000 blocks serialises in L2 for longer than a launch.
+// With has_heavy, it also closes the step's many-leg IF node (heavy), which
+// the force kernel opens when it finds such a centre.
+__global__ void k_spec_cond(DevState S, cudaGraphConditionalHandle cond,
                             cudaGraphConditionalHandle heavy, int has_heavy) {
   pdl_wait();
   pdl_trigger();
-  const bool pair_need = P.pair_rule && pair_decide_all(P, S);
   if (threadIdx.x == 0) {
-    int need = ((volatile DevScalars*)S.sc)->need_rebuild;
-    if (pair_need) {
-      S.sc->need_rebuild = 1;
-      need = 1;
-    }
-    cudaGraphSetConditional(cond, need ? 1u : 0u);
+    cudaGraphSetConditional(cond, ((volatile DevScalars*)S.sc)->need_rebuild ? 1u : 0u);
     if (has_heavy) cudaGraphSetConditional(heavy, 0u);
   }
 }
 
-// The pair rule's decisions outside a graph (launch by launch).
-__global__ void k_pair_decide(DevParams P, DevState S) {
-  if (pair_decide_all(P, S) && threadIdx.x == 0) S.sc->need_rebuild = 1;
-}
-
-// Clears every replica's pair-rule reports and the fused kernel's ticket
-// (a new state).
+// Clears every replica's running largest displacement of the pair rule (a
+// new state).
 __global__ void k_pair_clear(DevState S, int nrep) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r < nrep) {
-    S.sc[r].disp_top[0] = 0u;
-    S.sc[r].disp_top[1] = 0u;
-    S.sc[r].disp_ticket = 0u;
-  }
+  if (r < nrep) S.sc[r].disp_max = 0u;
 }
 
 cudaError_t launch_pair_clear(const Launch& L, const DevParams& P, const DevState& S) {
@@ -579,12 +534,9 @@ cudaError_t launch_spec_drift(const Launch& L, const DevParams& P, const DevStat
   cudaError_t e = launch_k(P.nrep > 1 ? k_spec_drift<1> : k_spec_drift<0>, nb, kKickThreads, 0,
                            L.stream, L.pdl && pdl_first, P, S);
   // in a graph, the rebuild condition of the IF node that follows
-  const int nt = pair_decide_threads(P);
   if (e == cudaSuccess && cond)
-    e = launch_k(k_spec_cond, 1, nt, 0, L.stream, L.pdl, P, S, *cond,
+    e = launch_k(k_spec_cond, 1, 32, 0, L.stream, L.pdl, S, *cond,
                  heavy ? *heavy : cudaGraphConditionalHandle(0), heavy ? 1 : 0);
-  else if (e == cudaSuccess && P.pair_rule)
-    e = launch_k(k_pair_decide, 1, nt, 0, L.stream, false, P, S);
   return e;
 }
 
@@ -722,6 +674,8 @@ __device__ __forceinline__ int spec_kick_chunk(const DevParams& P, const DevStat
   R->thermo_sum = tsum;
   R->thermo_cnt = tcnt;
   R->vmax2 = mx;
+  // the pair rule's running largest displacement, for the next drift
+  R->disp_max = 0u;
   if (apply) R->time += R->dt;
   const double vm = sqrt(mx);
   double nd = P.dt_max;
@@ -859,21 +813,6 @@ __global__ void __launch_bounds__(kKickThreads) k_spec_kd(DevParams P, DevState 
         sc->need_rebuild = 1;
         cudaGraphSetConditional(hif, 1u);
       }
-    }
-  }
-  // the pair rule: the block that drifts last decides from every block's
-  // reports (a ticket that wraps to 0 at the grid's size)
-  if (P.pair_rule) {
-    __shared__ int last;
-    if (threadIdx.x == 0) {
-      __threadfence();
-      last = atomicInc(&sc->disp_ticket, gridDim.x - 1) == gridDim.x - 1;
-      if (last) __threadfence();
-    }
-    __syncthreads();
-    if (last && pair_decide_all(P, S) && threadIdx.x == 0) {
-      sc->need_rebuild = 1;
-      cudaGraphSetConditional(hif, 1u);
     }
   }
 }

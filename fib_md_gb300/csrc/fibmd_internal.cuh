@@ -172,8 +172,8 @@ struct DevScalars {
   unsigned long long acc_vmax2;  // spec kick: running max |v|^2 (bits), sum m v^2
   double acc_tsum;               //            and count of the thermostat layer,
   int acc_tcnt;                  //            cleared by the replica's last chunk
-  unsigned disp_top[2];  // pair rule: the two largest reported |d|^2 (float bits)
-  unsigned disp_ticket;  //            fused kick-drift: drift blocks done this step
+  unsigned disp_max;     // pair rule: the step's largest reported |d|^2 (float
+                         // bits), cleared by the kick's last chunk
   unsigned int ticket[8];
   unsigned long long counters[4];
 };

@@ -309,8 +309,8 @@ int fibmd_gpu_phase_times(fibmd_ctx* ctx, double* seconds7, long long* counts7,
    every wait relies on; a larger value makes the waits give up, a hook for
    testing the time-out), "rebuild_rule" (spec mode, per replica in a
    batch: default 1, the lists are rebuilt once the two largest
-   displacements since the last build add up to the skin, those under an
-   eighth of it counted at that bound, and in a batch with them those of
+   displacements since the last build add up to the skin, those under a
+   quarter of it counted at that bound, and in a batch with them those of
    the replicas whose sum has reached half the skin; 0, once any atom's
    displacement reaches half the skin, in a batch with those that moved a
    quarter of it), "skin_tune" (default 1: in spec-mode calls of at

@@ -1303,8 +1303,8 @@ int orc_spec_step(orc_sys* s, int nthreads) {
   for (int d = 0; d < 3; d++) qs[d] = 4294967296.0 / s->Lb[d];
   int trig = 0;
   /* the pair rule's two largest squared displacements at or above the
-     reporting bound (an eighth of the skin) */
-  const double low2 = 0.0625 * s->sp_trig2;
+     reporting bound (a quarter of the skin) */
+  const double low2 = 0.25 * s->sp_trig2;
   double top1 = 0.0, top2 = 0.0;
   /* drift: thermostat scaling, X += V dt + F dt^2/(2m), pinning, removal
      (on the unwrapped height), wrap of atoms that left the box, and the

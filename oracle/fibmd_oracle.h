@@ -166,8 +166,8 @@ void orc_spec_init(orc_sys* s, const unsigned* tags, double time0);
    lists were rebuilt in it. */
 int orc_spec_step(orc_sys* s, int nthreads);
 /* The rebuild rule: 1 (the default), rebuild when the two largest
-   displacements since the last build add up to the skin (those under an
-   eighth of the skin counted at that bound); 0, when any atom's reaches half
+   displacements since the last build add up to the skin (those under a
+   quarter of the skin counted at that bound); 0, when any atom's reaches half
    the skin. Both with the 1 % margin of the skin. */
 void orc_spec_set_rule(orc_sys* s, int rule);
 /* time, dt, thermostat factor, vmax2, removed lattice atoms, removed ions,
