@@ -343,6 +343,7 @@ def bench_ours(args, rank, world, dist):
         wall = time.perf_counter() - w0
     stage_end = int(g.get_option("stage"))
     skin_end = g.get_option("skin")
+    pdl_end = g.get_option("pdl") == 1.0
     blocks_end = {"force_block": int(g.get_option("force_block")),
                   "build_block": int(g.get_option("build_block"))}
     X_end, _, _ = g.download()
@@ -475,7 +476,8 @@ def bench_ours(args, rank, world, dist):
         "dtype": "f32 force arithmetic, f64 accumulation/positions/VV",
         "data": "synthetic (seeded)",
         "config": workload_config(args, cells, N),
-        "step_loop": "launch by launch" if args.no_graph else "CUDA graph",
+        "step_loop": "launch by launch" if args.no_graph else
+                     ("CUDA graph, kernels as programmatic dependents" if pdl_end else "CUDA graph"),
         "autotune": {"force_path": "1000 steps after the upload, then after doubling "
                                    "intervals, among 6 or 10 staged legs per thread (in blocks of 128 or 64) and 8 lanes per centre (1)",
                      "force_path_at_end": stage_end,

@@ -495,3 +495,26 @@ def test_pair_rule_lists_complete(gpu_lib, path):
     assert 1 < ctxs[1].work_counters()[4] < ctxs[0].work_counters()[4]
     for c in ctxs.values():
         c.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_pdl_graph_matches_plain_launches(gpu_lib, precision):
+    """The unfused step graph with programmatic dependent launches (option
+    "pdl") runs the same steps as the same graph with plain launches."""
+    s, X, V = _spec_system(precision=precision)
+    a = _ctx(s, X, V, precision)
+    b = _ctx(s, X, V, precision)
+    for g in (a, b):
+        g.set_option("fuse", 0)
+        g.set_option("autotune", 0)
+    a.set_option("pdl", 1)
+    assert a.get_option("pdl") == 1 and b.get_option("pdl") == 0
+    la, ta, _, _ = a.steps(2, 120, 0, 0.0, 300.0)
+    lb, tb, _, _ = b.steps(2, 120, 0, 0.0, 300.0)
+    Xa, _, _ = a.download()
+    Xb, _, _ = b.download()
+    assert la == lb == 120 and abs(ta - tb) <= 1e-12 * tb
+    assert np.abs(Xa - Xb).max() < 1e-18
+    assert a.work_counters()[4] == b.work_counters()[4]
+    a.close()
+    b.close()
