@@ -6,7 +6,8 @@ Workload (the single-cascade configuration): a diamond-cubic Si slab of
 one Ga ion at 5 keV, 7 degrees off normal, seeded azimuth and impact point
 10 A above the surface; Maxwell-Boltzmann velocities at 300 K (seeded);
 bottom 2 atomic layers fixed, next 4 Berendsen-thermostatted at 300 K;
-variable dt = min(1 fs, 0.05 A / max|v|); lists rebuilt at half the skin.
+variable dt = min(1 fs, 0.05 A / max|v|); lists rebuilt once the two largest
+displacements since the last build add up to the skin.
 Synthetic data, seeded (spec_slab, seed 2001).
 
 One bench step = MD steps 1..`--md-steps` (default 5000) of that cascade,

@@ -1651,7 +1651,7 @@ static int onestep(fibmd_ctx* ctx, int whichctrl, long long lt, double* time, in
 // The spec-mode step loop as one CUDA graph: a WHILE node runs step pairs
 // (the force buffers swap back after two steps) until the device-side loop
 // counter or the relaxation's end time stops it; after each drift an IF node
-// runs the list rebuild only when an atom moved half the skin.
+// runs the list rebuild only when the drift found it due (the rebuild rule).
 //   unfused: WHILE { [drift, cond, IF{rebuild}, force, kick] x 2, loop control }
 //   fused ("fuse", the default): drift, cond, IF{rebuild},
 //            WHILE { [force, kick + next drift, IF{rebuild}] x 2 }

@@ -2,8 +2,8 @@
 //
 // The spec-mode step sequence is captured once into a graph whose WHILE node
 // runs pairs of MD steps until a device counter reaches zero, and whose IF
-// nodes run the list rebuild only on the steps where the drift found an atom
-// beyond half the skin (the drift kernel's last block sets that condition).
+// nodes run the list rebuild only on the steps where the drift found it due
+// (the drift sets a flag, the condition kernel after it the IF node).
 // These single-thread kernels count the step pairs down (and stop a
 // relaxation at its end time) on the device, so no step needs the host.
 #include "fibmd_internal.cuh"

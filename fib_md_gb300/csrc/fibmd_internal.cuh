@@ -158,8 +158,8 @@ struct DevScalars {
   int cell_oob;
   int nan_flag;
   int need_rebuild;
-  int rep_rebuild;     // spec batch: an atom of this replica moved half the skin
-  int rep_soon;        //             ... a quarter of the skin
+  int rep_rebuild;     // spec batch: this replica is due a rebuild (the rule)
+  int rep_soon;        //             ... halfway there
   int rebuild_all;     // spec batch: the next rebuild covers every replica
                        // (a skin switch, an injection)
   int removed_count;   // spec: lattice atoms removed (sputtered)

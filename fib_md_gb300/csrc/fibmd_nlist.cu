@@ -40,7 +40,7 @@ __device__ __forceinline__ bool rebuild_skipped(const DevState& S, int from_flag
 }
 
 // Whether replica r's SW lists are rebuilt (from_flag 2: per replica, those
-// that moved half the skin and, with them, those that moved a quarter).
+// due by the rebuild rule and, with them, those halfway there).
 __device__ __forceinline__ bool rep_rebuilt(const DevParams& P, const DevState& S, int from_flag,
                                             int r) {
   if (from_flag != 2 || P.nrep <= 1 || ((volatile DevScalars*)S.sc)->rebuild_all) return true;

@@ -74,7 +74,8 @@ typedef struct orc_sys {
   int atom_is_fast, atom_is_slow;
 
   /* spec mode: the specified set-up, which the reference does not have
-     (variable dt, half-skin rebuild, layer tags, removal); see orc_spec_* */
+     (variable dt, skin-triggered rebuild, layer tags, removal); see
+     orc_spec_* */
   int spec;                    /* lists and steps follow spec mode           */
   unsigned* tags;              /* FIBMD_TAG_* bits per atom                  */
   double* Xb;                  /* positions at the last list build (Natm,3)  */
@@ -149,8 +150,10 @@ void orc_knock(orc_sys* s, orc_rng* r, int knc, double eV, double phiz,
    FIBMD_MODE_SPEC):
    variable dt = min(dt_max, dx_max / max|v|); lists of radius cutoff + skin
    (0.999 a sigma + list_skin for Si/Ge pairs, 2.5 sigma + list_skin for
-   pairs with an ion, every such pair found) rebuilt when an atom has moved
-   half the skin since the last build; frozen and thermostatted layers as
+   pairs with an ion, every such pair found) rebuilt when the two largest
+   displacements since the last build add up to the skin (orc_spec_set_rule
+   1, the default) or one reaches half of it (0); frozen and thermostatted
+   layers as
    per-atom tags; atoms above remove_z removed (and, with z an open axis,
    atoms 10 A below z = 0). A step: thermostat scaling of the tagged layer,
    drift, pinning, removal, wrap, the rebuild test, [rebuild], force, kick,
