@@ -429,25 +429,33 @@ __global__ void __launch_bounds__(BLK, 896 / BLK) k_force_mixed(DevParams P, Dev
       const float ar = lb.x, ag = lb.y;
       const int ia = sI[a * BLK + t];
       const int tbA = (unsigned)ia >> 30;
-      float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+      // The force on leg a from its terms with the other legs b, with
+      // q = pref (cos + 1/3), pref = lambda E_a E_b:
+      //   sum_b pref [W g_a a + 2 (cos + 1/3) r_a^-1 (b - cos a)]
+      //     = a sum_b q ((cos + 1/3) g_a - 2 r_a^-1 cos) + 2 r_a^-1 sum_b q b,
+      // so the loop sums one scalar and one vector per pair.
+      const float m2ar = -2.0f * ar;
+      float sw = 0.f, sbx = 0.f, sby = 0.f, sbz = 0.f, ae = 0.f;
 #pragma unroll 2
       for (int b = 0; b < nl; b++) {
         if (b == a) continue;
         const float4 lbb = sA[b * BLK + t];
-        const float bx = lbb.x, by = lbb.y, bz = lbb.z;
         const int tbB = (unsigned)sI[b * BLK + t] >> 30;
-        const float cs = ax * bx + ay * by + az * bz;
+        const float cs = ax * lbb.x + ay * lbb.y + az * lbb.z;
         const float c3 = cs + thrd;
-        const float W = c3 * c3;
         const float pref = P.lepsA[ta][UNI ? 0 : tbA][UNI ? 0 : tbB] * aE * lbb.w;
-        const float s2 = 2.0f * c3;
-        const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
-        afx += pref * (wa * ax + sa * bx);
-        afy += pref * (wa * ay + sa * by);
-        afz += pref * (wa * az + sa * bz);
-        if (ENERGY) ae += pref * W;
+        const float q = pref * c3;
+        sw += q * (c3 * ag + m2ar * cs);
+        sbx += q * lbb.x;
+        sby += q * lbb.y;
+        sbz += q * lbb.z;
+        if (ENERGY) ae += q * c3;
         if (COUNT && b > a && pref != 0.f) cnt_ang++;
       }
+      const float tar = -m2ar;
+      const float afx = sw * ax + tar * sbx;
+      const float afy = sw * ay + tar * sby;
+      const float afz = sw * az + tar * sbz;
       if (REACT) {
         S.react[(size_t)a * P.N + i] = make_float4(afx, afy, afz, 0.f);
         lpos |= (unsigned long long)(ia & 63) << (6 * a);
@@ -788,7 +796,10 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
       const R ax = sl[sg][0][a], ay = sl[sg][1][a], az = sl[sg][2][a];
       const R ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
       const int ja = sj[sg][a];
-      R afx = 0, afy = 0, afz = 0, ae = 0;
+      // leg a's force as in the one-thread kernel: one scalar and one vector
+      // summed per pair, a's direction applied once
+      const R m2ar = (R)-2 * ar;
+      R sw = 0, sbx = 0, sby = 0, sbz = 0, ae = 0;
       // unrolled for independent shared-memory loads; leg a itself enters
       // with a zero weight (its terms are finite)
 #pragma unroll 4
@@ -796,18 +807,23 @@ __device__ __forceinline__ void heavy_centres(const DevParams& P, const DevState
         const R bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
         const int jb = sj[sg][b];
         const R cs = ax * bx + ay * by + az * bz;
-        const R c3 = cs + thrd, W = c3 * c3, s2 = (R)2 * c3;
+        const R c3 = cs + thrd;
         R lp;
         if constexpr (MIXED)
           lp = UNI ? P.lepsA[0][0][0] : P.lepsA[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         else lp = P.leps[tc - 1][(unsigned)ja >> 30][(unsigned)jb >> 30];
         const R pref = b == a ? (R)0 : lp * aE * sl[sg][4][b];
-        const R wa = W * ag - s2 * cs * ar, sa = s2 * ar;
-        afx += pref * (wa * ax + sa * bx);
-        afy += pref * (wa * ay + sa * by);
-        afz += pref * (wa * az + sa * bz);
-        if (ENERGY) ae += pref * W;
+        const R q = pref * c3;
+        sw += q * (c3 * ag + m2ar * cs);
+        sbx += q * bx;
+        sby += q * by;
+        sbz += q * bz;
+        if (ENERGY) ae += q * c3;
       }
+      const R tar = -m2ar;
+      const R afx = sw * ax + tar * sbx;
+      const R afy = sw * ay + tar * sby;
+      const R afz = sw * az + tar * sbz;
       const int j = ja & 0x3fffffff;
       if constexpr (MIXED) {
         // eV/A -> N in binary32 (as in the one-thread kernel): one conversion
@@ -983,24 +999,32 @@ __global__ void __launch_bounds__(32 * kHeavyWarps) k_force_group(DevParams P, D
     const float ax = sl[sg][0][a], ay = sl[sg][1][a], az = sl[sg][2][a];
     const float ar = sl[sg][3][a], aE = sl[sg][4][a], ag = sl[sg][5][a];
     const int ja = sj[sg][a];
-    float afx = 0.f, afy = 0.f, afz = 0.f, ae = 0.f;
+    // leg a's force as in the one-thread kernel: one scalar and one vector
+    // summed per pair, a's direction applied once
+    const float m2ar = -2.0f * ar;
+    float sw = 0.f, sbx = 0.f, sby = 0.f, sbz = 0.f, ae = 0.f;
     // unrolled for independent shared-memory loads; leg a itself enters
     // with a zero weight (its terms are finite)
 #pragma unroll 4
     for (int b = 0; b < nl; b++) {
       const float bx = sl[sg][0][b], by = sl[sg][1][b], bz = sl[sg][2][b];
       const float cs = ax * bx + ay * by + az * bz;
-      const float c3 = cs + thrd, W = c3 * c3, s2 = 2.0f * c3;
+      const float c3 = cs + thrd;
       const float lp = UNI ? P.lepsA[0][0][0]
                            : P.lepsA[ta][(unsigned)ja >> 30][(unsigned)sj[sg][b] >> 30];
       const float pref = b == a ? 0.f : lp * aE * sl[sg][4][b];
-      const float wa = W * ag - s2 * cs * ar, sa = s2 * ar;
-      afx += pref * (wa * ax + sa * bx);
-      afy += pref * (wa * ay + sa * by);
-      afz += pref * (wa * az + sa * bz);
-      if (ENERGY) ae += pref * W;
+      const float q = pref * c3;
+      sw += q * (c3 * ag + m2ar * cs);
+      sbx += q * bx;
+      sby += q * by;
+      sbz += q * bz;
+      if (ENERGY) ae += q * c3;
       if (COUNT && b > a && pref != 0.f) cnt_ang++;
     }
+    const float tar = -m2ar;
+    const float afx = sw * ax + tar * sbx;
+    const float afy = sw * ay + tar * sby;
+    const float afz = sw * az + tar * sbz;
     const int j = ja & 0x3fffffff;
     atomic_add3(S.frc_new, j, (double)(conv * afx), (double)(conv * afy), (double)(conv * afz));
     if (ENERGY && ae != 0.f) atomicAdd(&S.epot[j], P.e_eV_to_J * (double)ae / 3.0);
