@@ -196,45 +196,47 @@ __global__ void __launch_bounds__(kBlock64) k_force_fp64(DevParams P, DevState S
       const double ax = leg.at(a, 0), ay = leg.at(a, 1), az = leg.at(a, 2);
       const double ar = leg.at(a, 3), aE = leg.at(a, 4), ag = leg.at(a, 5);
       const int tbA = (unsigned)leg.idx(a) >> 30;
-      double afx = 0, afy = 0, afz = 0, ae = 0;
+      // F_a = pref [W g_a p_a + 2(c+1/3)(p_b - c p_a)/r_a], p = unit(X_c - X_a),
+      // summed over b as p_a sum_b q (c3 g_a - 2 c / r_a) + (2 / r_a) sum_b q p_b
+      // with q = pref c3, c3 = c + 1/3 (leg a in registers), and leg b's
+      // term q (c3 g_b - 2 c / r_b) p_b + (2 q / r_b) p_a into its slots
+      const double m2ar = -2.0 * ar;
+      double swa = 0, sbx = 0, sby = 0, sbz = 0, ae = 0;
       for (int b = a + 1; b < nl; b++) {
         const double bx = leg.at(b, 0), by = leg.at(b, 1), bz = leg.at(b, 2);
         const double br = leg.at(b, 3), bE = leg.at(b, 4), bg = leg.at(b, 5);
         const int tbB = (unsigned)leg.idx(b) >> 30;
         const double cs = ax * bx + ay * by + az * bz;
         const double c3 = cs + thrd;
-        const double W = c3 * c3;
         const double pref = P.leps[ta][tbA][tbB] * aE * bE;
-        const double s2 = 2.0 * c3;
-        // F_a = pref [W g_a p_a + 2(c+1/3)(p_b - c p_a)/r_a], p = unit(X_c - X_a)
-        const double wa = W * ag - s2 * cs * ar, sa = s2 * ar;
-        const double Fax = pref * (wa * ax + sa * bx);
-        const double Fay = pref * (wa * ay + sa * by);
-        const double Faz = pref * (wa * az + sa * bz);
-        const double wb = W * bg - s2 * cs * br, sb = s2 * br;
-        const double Fbx = pref * (wb * bx + sb * ax);
-        const double Fby = pref * (wb * by + sb * ay);
-        const double Fbz = pref * (wb * bz + sb * az);
-        afx += Fax;
-        afy += Fay;
-        afz += Faz;
-        leg.at(b, 6) += Fbx;
-        leg.at(b, 7) += Fby;
-        leg.at(b, 8) += Fbz;
-        cfx -= Fax + Fbx;
-        cfy -= Fay + Fby;
-        cfz -= Faz + Fbz;
+        const double q = pref * c3;
+        swa += q * (c3 * ag + m2ar * cs);
+        sbx += q * bx;
+        sby += q * by;
+        sbz += q * bz;
+        const double tb = q * (c3 * bg - 2.0 * br * cs), ub = 2.0 * br * q;
+        leg.at(b, 6) += tb * bx + ub * ax;
+        leg.at(b, 7) += tb * by + ub * ay;
+        leg.at(b, 8) += tb * bz + ub * az;
         if (ENERGY) {
-          const double e = pref * W;
+          const double e = q * c3;
           cu += e;
           ae += e;
           atomicAdd(&S.epot[leg.idx(b) & 0x3fffffff], e / 3.0);
         }
         if (COUNT && pref != 0.0) cnt_ang++;
       }
-      leg.at(a, 6) += afx;
-      leg.at(a, 7) += afy;
-      leg.at(a, 8) += afz;
+      // leg a's terms with the legs before it are already in its slots
+      const double tar = -m2ar;
+      const double Fax = leg.at(a, 6) + (swa * ax + tar * sbx);
+      const double Fay = leg.at(a, 7) + (swa * ay + tar * sby);
+      const double Faz = leg.at(a, 8) + (swa * az + tar * sbz);
+      leg.at(a, 6) = Fax;
+      leg.at(a, 7) = Fay;
+      leg.at(a, 8) = Faz;
+      cfx -= Fax;
+      cfy -= Fay;
+      cfz -= Faz;
       if (ENERGY && ae != 0.0) atomicAdd(&S.epot[leg.idx(a) & 0x3fffffff], ae / 3.0);
     }
     // each angle term gives a third of its energy to each of its atoms
